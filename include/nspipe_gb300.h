@@ -1,0 +1,139 @@
+/* nspipe_gb300.h -- C ABI of the GB300 pipe-flow time stepper.
+ *
+ * Drop-in replacement for the per-step entry points of nsPipe-CUDA
+ * (Mordered/nsPipe-GPU, Main_Code/src).  The reference exposes C++-linkage
+ * functions declared in head.h:77-152 and configured by compile-time #defines
+ * (head.h:16-61); this library takes the same parameters at run time, keeps the
+ * same spectral state layout and restart/checkpoint file format, and returns
+ * status codes instead of calling exit() (head.h:64-70, mod_fft.cu:12-18,
+ * mod_cublasflux.cu:33-38).
+ *
+ * State layout (head.h:73, mod_deriv.cu:15-17): each velocity component is an
+ * interleaved complex double array double2[NR][NT][NZ], index
+ * h = i*NT*NZ + it*NZ + l, radial point i, azimuthal slot it (signed mode
+ * m = it < NT/2 ? it : it-NT), axial mode l = 0..NZ-1 (k_z >= 0 only).  At step
+ * boundaries the state is in (u_r, u_theta, u_z) form.
+ *
+ * A context holds an ensemble of independent pipes ("members").  Members with
+ * equal (NR, NT, NZ, LT, LZ, Re, dt, d_im, sten) share one set of operator
+ * tables; members of different shapes (uneven batches) are allowed.  Each
+ * context owns one CUDA stream on one device; one host thread per context.
+ * All functions return NSP_OK (0) or an NSP_ERR_* code; nsp_last_error()
+ * describes the last failure.
+ */
+#ifndef NSPIPE_GB300_H
+#define NSPIPE_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NSP_OK 0
+#define NSP_ERR_ARG 1        /* invalid argument or parameter combination         */
+#define NSP_ERR_CUDA 2       /* CUDA runtime failure (message in nsp_last_error)   */
+#define NSP_ERR_IO 3         /* restart/checkpoint file missing, short or unwritable */
+#define NSP_ERR_NONFINITE 4  /* a member's field became NaN/Inf during nsp_step    */
+#define NSP_ERR_STATE 5      /* call out of order (e.g. nsp_step before nsp_setup) */
+#define NSP_ERR_NOMEM 6      /* device allocation failed                           */
+
+#define NSP_FP64 0  /* plain form: every operation in FP64 (matches the reference)         */
+#define NSP_MIXED 1 /* transforms + nonlinear product in FP32; solves, BCs, state in FP64 */
+
+/* Run-time copy of the reference's compile-time parameters (head.h:16-61). */
+typedef struct nsp_params {
+  int NR, NT, NZ;  /* radial points; 2*m_theta theta slots (even); m_z+1 axial modes (odd)  head.h:16-18 */
+  double LT, LZ;   /* azimuthal and axial domain lengths                                    head.h:21-22 */
+  double Re;       /* Reynolds number                                                        head.h:25    */
+  double dt;       /* time step (code units)                                                 head.h:48    */
+  double d_im;     /* implicitness factor                                                    head.h:49    */
+  int maxit;       /* corrector iteration cap                                                head.h:51    */
+  double tol;      /* convergence tolerance on max|du|^2/max|u|^2                            head.h:52    */
+  int sten;        /* radial stencil width; 7 (the reference's value) is supported           head.h:44    */
+  double Qdes;     /* prescribed mass flux, 0.5 in the reference                  mod_cublasflux.cu:92    */
+} nsp_params;
+
+/* Diagnostics of one member (the quantities of wrt_frc_k, mod_io_nonlinear.cu:40-52,
+ * plus the last step's corrector record). */
+typedef struct nsp_diag_out {
+  double u_centre;    /* centreline u_z(0,0) interpolated to r = 0 (dr0 weights)         */
+  double u_tau;       /* sqrt(|d u_z(0,0)/dr|_wall / Re)                                 */
+  double flux;        /* sum_i rdr_i Re u_z(0,0)(r_i)                                    */
+  double last_err;    /* convergence measure of the last corrector iteration             */
+  int last_iters;     /* corrector iterations of the last step                           */
+  int status;         /* NSP_OK or NSP_ERR_NONFINITE                                     */
+} nsp_diag_out;
+
+typedef struct nsp_ctx nsp_ctx;
+
+/* Fills *p with the reference defaults (head.h:16-61: NR=48, NT=64, NZ=257, LT=2pi,
+ * LZ=100, Re=1850, dt=0.01, d_im=0.51, maxit=10, tol=5e-8, sten=7) and Qdes=0.5. */
+int nsp_default_params(nsp_params* p);
+
+/* Creates a context for n_members pipes with parameters members[0..n_members-1] on
+ * CUDA device `device`, in precision NSP_FP64 or NSP_MIXED, and allocates every
+ * device buffer.  Replaces main.cu:16-33 (cudaSetDevice + the cudaMalloc of u, rhs). */
+int nsp_create(const nsp_params* members, int n_members, int precision, int device, nsp_ctx** out);
+
+/* Builds the radial grid, finite-difference weights, quadrature weights, the banded
+ * LU factors of the Helmholtz/Poisson operators, the influence-matrix correction
+ * vectors and the flux response.  Replaces init_fd (mod_radialFD.cu:199-312),
+ * setLinear (mod_linear.cu:685-695), setCublasFlux (mod_cublasflux.cu:56-81) and
+ * setBCon (mod_boundary.cu:205-255). */
+int nsp_setup(nsp_ctx* ctx);
+
+/* Restart files: three raw little-endian double2[NR][NT][NZ] files, byte-identical to
+ * rBufferBinary / wBufferBinary (mod_io_nonlinear.cu:528-565; initField's restart
+ * branch :426-429; the final dump main.cu:42-44). */
+int nsp_load_state(nsp_ctx* ctx, int member, const char* file_r, const char* file_t, const char* file_z);
+int nsp_save_state(nsp_ctx* ctx, int member, const char* file_r, const char* file_t, const char* file_z);
+
+/* State transfer.  Host pointers: interleaved complex double arrays of NR*NT*NZ
+ * values.  Device pointers: same layout in device memory on the context's device
+ * (the caller-owned vfield of main.cu:30-33). */
+int nsp_set_state_host(nsp_ctx* ctx, int member, const double* ur, const double* ut, const double* uz);
+int nsp_get_state_host(nsp_ctx* ctx, int member, double* ur, double* ut, double* uz);
+int nsp_set_state_device(nsp_ctx* ctx, int member, const void* ur, const void* ut, const void* uz);
+int nsp_get_state_device(nsp_ctx* ctx, int member, void* ur, void* ut, void* uz);
+
+/* Advances every member by nsteps time steps: nonlinear term, predictor, and
+ * corrector iterations until err <= tol or maxit (integrate, mod_integrate.cu:98-160;
+ * predictor :164-193; corrector :197-228; measucorr :232-241), each member with its
+ * own iteration count.  One CUDA graph per step; the corrector loop is a device-side
+ * conditional node.  iters_out (optional) receives nsteps*n_members counts,
+ * step-major.  Returns NSP_ERR_NONFINITE if any member's convergence measure became
+ * NaN/Inf (the other members are still advanced). */
+int nsp_step(nsp_ctx* ctx, int nsteps, int* iters_out);
+
+/* The nonlinear term -(u.grad)u of one member's field (r/theta form), 3/2-dealiased,
+ * with the mean pressure-gradient forcing on mode (0,0) (nonlinear,
+ * mod_io_nonlinear.cu:380-409).  All six pointers are device arrays of NR*NT*NZ
+ * complex doubles; the evaluation uses the context's precision. */
+int nsp_nonlinear(nsp_ctx* ctx, int member, const void* ur, const void* ut, const void* uz,
+                  void* nr, void* nt, void* nz);
+
+/* One banded solve on one member's operators (LUsolve_u flag 0/1/2 and LUsolve_p,
+ * mod_linear.cu:664-679): kind 0 = u+, 1 = u-, 2 = u_z, 3 = pressure.  rhs and sol
+ * are device arrays of NR*NT*NZ complex doubles (rhs is not modified). */
+int nsp_lusolve(nsp_ctx* ctx, int member, int kind, const void* rhs, void* sol);
+
+/* Diagnostics of one member (synchronises the context's stream). */
+int nsp_diag(nsp_ctx* ctx, int member, nsp_diag_out* out);
+
+/* Radial grid r[NR] and quadrature weights rdr[NR] of a member (after nsp_setup). */
+int nsp_grid(nsp_ctx* ctx, int member, double* r, double* rdr);
+
+/* Number of kernel launches issued by the last nsp_step call (all graph nodes run). */
+long long nsp_kernel_launches(nsp_ctx* ctx);
+
+/* Waits for all work of the context. */
+int nsp_sync(nsp_ctx* ctx);
+
+const char* nsp_last_error(nsp_ctx* ctx);
+int nsp_destroy(nsp_ctx* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

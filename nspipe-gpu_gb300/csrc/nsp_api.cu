@@ -1,0 +1,582 @@
+// nsp_api.cu -- the C ABI (include/nspipe_gb300.h): contexts, operator upload,
+// the CUDA-graph time step and state I/O.
+//
+// One nsp_step time step is one launch of a CUDA graph whose only node is a
+// conditional WHILE node.  Its body evaluates, for every member group, the
+// nonlinear term (3 kernels) and the predictor/corrector linear pass (1 kernel),
+// then converge_k updates each member's phase and sets the loop condition.
+// The first body iteration is the predictor of every member; later iterations
+// are corrector iterations of the members that have not converged (the others
+// skip their blocks), so each member keeps the reference's own iteration count
+// (integrate, mod_integrate.cu:112-130) without any device-to-host round trip.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "nsp_fft.cuh"
+#include "nsp_internal.h"
+
+namespace nsp {
+void configure_transform_kernels();
+void configure_linear_kernels();
+}  // namespace nsp
+
+using namespace nsp;
+
+namespace {
+
+struct Group {
+  nsp_params p;
+  std::vector<int> users;  // user member indices, in slot order
+  HostOps ops;
+  Tables tb{};
+  Bufs bf{};
+};
+
+}  // namespace
+
+struct nsp_ctx {
+  int device = 0;
+  int precision = NSP_FP64;
+  int nmem = 0;
+  std::vector<nsp_params> prm;
+  std::vector<int> grp, slot, internal;  // per user member
+  std::vector<Group> groups;
+  cudaStream_t st = nullptr;
+  Ctl hctl{};
+  Ctl* dctl = nullptr;
+  int parity = 0;  // host mirror of ctl.parity
+  bool setup_done = false;
+  cudaGraphExec_t gexec = nullptr;
+  bool use_graph = false;
+  long long launches_last = 0;
+  double2* scratch = nullptr;  // 2 x 3 x Smax, for nsp_nonlinear
+  long long Smax = 0;
+  std::vector<void*> allocs;
+  std::string err;
+};
+
+namespace {
+
+int fail(nsp_ctx* c, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+#define CK(call)                                                                                           \
+  do {                                                                                                     \
+    cudaError_t e_ = (call);                                                                               \
+    if (e_ != cudaSuccess)                                                                                 \
+      return fail(c, e_ == cudaErrorMemoryAllocation ? NSP_ERR_NOMEM : NSP_ERR_CUDA, "%s: %s (%s:%d)", #call, \
+                  cudaGetErrorString(e_), __FILE__, __LINE__);                                             \
+  } while (0)
+
+template <typename X>
+int dalloc(nsp_ctx* c, X** p, size_t bytes) {
+  void* q = nullptr;
+  cudaError_t e = cudaMalloc(&q, bytes ? bytes : 16);
+  if (e != cudaSuccess) return fail(c, NSP_ERR_NOMEM, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+  c->allocs.push_back(q);
+  *p = (X*)q;
+  return NSP_OK;
+}
+
+template <typename X>
+int upload(nsp_ctx* c, const X** dst, const std::vector<X>& v) {
+  X* d = nullptr;
+  int rc = dalloc(c, &d, sizeof(X) * v.size());
+  if (rc) return rc;
+  CK(cudaMemcpy(d, v.data(), sizeof(X) * v.size(), cudaMemcpyHostToDevice));
+  *dst = d;
+  return NSP_OK;
+}
+
+bool smooth23(int n) {
+  if (n < 2) return false;
+  while (n % 2 == 0) n /= 2;
+  while (n % 3 == 0) n /= 3;
+  return n == 1;
+}
+
+// exp(-2 pi i e / n), exact at quarter turns, long-double accurate otherwise.
+std::vector<double2> twiddles(int n) {
+  std::vector<double2> w(n);
+  const long double PI_L = 3.141592653589793238462643383279502884L;
+  for (int e = 0; e < n; e++) {
+    long long e4 = 4LL * e;
+    if (e4 % n == 0) {
+      static const double cx[4] = {1.0, 0.0, -1.0, 0.0}, sy[4] = {0.0, -1.0, 0.0, 1.0};
+      int q = (int)(e4 / n) & 3;
+      w[e] = make_double2(cx[q], sy[q]);
+    } else {
+      long double a = -2.0L * PI_L * (long double)e / (long double)n;
+      w[e] = make_double2((double)cosl(a), (double)sinl(a));
+    }
+  }
+  return w;
+}
+
+std::vector<float2> to_f32(const std::vector<double2>& v) {
+  std::vector<float2> o(v.size());
+  for (size_t i = 0; i < v.size(); i++) o[i] = make_float2((float)v[i].x, (float)v[i].y);
+  return o;
+}
+
+bool same_ops(const nsp_params& a, const nsp_params& b) {
+  return a.NR == b.NR && a.NT == b.NT && a.NZ == b.NZ && a.LT == b.LT && a.LZ == b.LZ && a.Re == b.Re &&
+         a.dt == b.dt && a.d_im == b.d_im && a.sten == b.sten && a.Qdes == b.Qdes && a.maxit == b.maxit &&
+         a.tol == b.tol;
+}
+
+int check_params(nsp_ctx* c, const nsp_params& p, int idx) {
+  if (p.NR < 8 || p.NR > 1024) return fail(c, NSP_ERR_ARG, "member %d: NR=%d outside [8, 1024]", idx, p.NR);
+  if (p.NT < 4 || p.NT % 2) return fail(c, NSP_ERR_ARG, "member %d: NT=%d must be even and >= 4", idx, p.NT);
+  if (p.NZ < 3 || p.NZ % 2 == 0) return fail(c, NSP_ERR_ARG, "member %d: NZ=%d must be odd and >= 3", idx, p.NZ);
+  if (p.sten != STEN) return fail(c, NSP_ERR_ARG, "member %d: sten=%d (only 7 is supported)", idx, p.sten);
+  int NTP = 3 * p.NT / 2, NZR = 3 * (p.NZ - 1);
+  if (!smooth23(NTP) || !smooth23(NZR))
+    return fail(c, NSP_ERR_ARG, "member %d: transform lengths %d x %d must be of the form 2^a 3^b", idx, NTP, NZR);
+  FftPlan pt, pz;
+  make_plan(NTP, pt);
+  make_plan(NZR, pz);
+  if (max_butterflies(pt, 16) > 4 * 256 || max_butterflies(pz, 6) > 4 * 512)
+    return fail(c, NSP_ERR_ARG, "member %d: transform lengths %d x %d exceed the block size limits", idx, NTP, NZR);
+  if (!(p.Re > 0) || !(p.dt > 0) || !(p.LT > 0) || !(p.LZ > 0) || p.maxit < 1 || !(p.tol >= 0) || !(p.Qdes == p.Qdes))
+    return fail(c, NSP_ERR_ARG, "member %d: Re, dt, LT, LZ must be > 0, maxit >= 1, tol >= 0", idx);
+  return NSP_OK;
+}
+
+int check_member(nsp_ctx* c, int m) {
+  if (!c) return NSP_ERR_ARG;
+  if (m < 0 || m >= c->nmem) return fail(c, NSP_ERR_ARG, "member %d out of range [0, %d)", m, c->nmem);
+  return NSP_OK;
+}
+
+double2* state_ptr(nsp_ctx* c, int m, int comp) {
+  Group& g = c->groups[c->grp[m]];
+  return g.bf.U[c->parity] + ((size_t)c->slot[m] * 3 + comp) * g.tb.S;
+}
+
+int build_graph(nsp_ctx* c) {
+  if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+  cudaGraph_t g = nullptr;
+  CK(cudaGraphCreate(&g, 0));
+  cudaGraphConditionalHandle h;
+  cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
+  if (e != cudaSuccess) {
+    cudaGraphDestroy(g);
+    cudaGetLastError();
+    c->use_graph = false;
+    return NSP_OK;
+  }
+  cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp));
+  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  CK(cudaStreamBeginCaptureToGraph(c->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  for (auto& gr : c->groups) {
+    launch_nonlinear(gr.tb, gr.bf, c->dctl, c->precision == NSP_MIXED, nullptr, nullptr, c->st);
+    launch_linear(gr.tb, gr.bf, c->dctl, c->st);
+  }
+  launch_converge(c->dctl, c->nmem, (unsigned long long)h, 1, c->st);
+  cudaGraph_t cap = nullptr;
+  CK(cudaStreamEndCapture(c->st, &cap));
+  CK(cudaGraphInstantiate(&c->gexec, g, 0));
+  cudaGraphDestroy(g);
+  c->use_graph = true;
+  return NSP_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int nsp_default_params(nsp_params* p) {
+  if (!p) return NSP_ERR_ARG;
+  p->NR = 48; p->NT = 64; p->NZ = 257;
+  p->LT = PI2; p->LZ = 100.0;
+  p->Re = 1850.0;
+  p->dt = 0.01; p->d_im = 0.51;
+  p->maxit = 10; p->tol = 5e-8;
+  p->sten = 7;
+  p->Qdes = 0.5;
+  return NSP_OK;
+}
+
+int nsp_create(const nsp_params* members, int n_members, int precision, int device, nsp_ctx** out) {
+  if (!out || !members || n_members < 1) return NSP_ERR_ARG;
+  *out = nullptr;
+  if (precision != NSP_FP64 && precision != NSP_MIXED) return NSP_ERR_ARG;
+  nsp_ctx* c = new nsp_ctx();
+  *out = c;
+  c->device = device;
+  c->precision = precision;
+  c->nmem = n_members;
+  c->prm.assign(members, members + n_members);
+  for (int m = 0; m < n_members; m++) {
+    int rc = check_params(c, members[m], m);
+    if (rc) return rc;
+  }
+  // Group members with identical operators; internal order is group-major.
+  c->grp.assign(n_members, -1);
+  c->slot.assign(n_members, -1);
+  for (int m = 0; m < n_members; m++) {
+    int gi = -1;
+    for (size_t g = 0; g < c->groups.size(); g++)
+      if (same_ops(c->groups[g].p, members[m])) { gi = (int)g; break; }
+    if (gi < 0) {
+      Group g;
+      g.p = members[m];
+      c->groups.push_back(g);
+      gi = (int)c->groups.size() - 1;
+    }
+    c->grp[m] = gi;
+    c->slot[m] = (int)c->groups[gi].users.size();
+    c->groups[gi].users.push_back(m);
+  }
+  c->internal.assign(n_members, 0);
+  int base = 0;
+  for (auto& g : c->groups) {
+    for (size_t s = 0; s < g.users.size(); s++) c->internal[g.users[s]] = base + (int)s;
+    base += (int)g.users.size();
+  }
+  CK(cudaSetDevice(device));
+  CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+  // Member buffers.
+  base = 0;
+  for (auto& g : c->groups) {
+    const nsp_params& p = g.p;
+    Tables& tb = g.tb;
+    tb.NR = p.NR; tb.NT = p.NT; tb.NZ = p.NZ;
+    tb.NTP = 3 * p.NT / 2;
+    tb.NZP = 3 * (p.NZ - 1) / 2 + 1;
+    tb.NZR = 2 * tb.NZP - 2;
+    tb.NTNZ = p.NT * p.NZ;
+    tb.S = (long long)p.NR * tb.NTNZ;
+    tb.nmem = (int)g.users.size();
+    tb.mem0 = base;
+    base += tb.nmem;
+    size_t S3 = (size_t)tb.nmem * 3 * tb.S;
+    size_t csz = (precision == NSP_MIXED) ? sizeof(float2) : sizeof(double2);
+    size_t gsz = (size_t)tb.nmem * 9 * tb.NR * tb.NTP * tb.NZ * csz;
+    size_t hsz = (size_t)tb.nmem * 3 * tb.NR * tb.NTP * tb.NZ * csz;
+    int rc;
+    if ((rc = dalloc(c, &g.bf.U[0], S3 * sizeof(double2)))) return rc;
+    if ((rc = dalloc(c, &g.bf.U[1], S3 * sizeof(double2)))) return rc;
+    if ((rc = dalloc(c, &g.bf.RHSW, S3 * sizeof(double2)))) return rc;
+    if ((rc = dalloc(c, &g.bf.N, S3 * sizeof(double2)))) return rc;
+    if ((rc = dalloc(c, &g.bf.G, gsz))) return rc;
+    if ((rc = dalloc(c, &g.bf.H, hsz))) return rc;
+    CK(cudaMemset(g.bf.U[0], 0, S3 * sizeof(double2)));
+    CK(cudaMemset(g.bf.U[1], 0, S3 * sizeof(double2)));
+    CK(cudaMemset(g.bf.H, 0, hsz));
+    if (tb.S > c->Smax) c->Smax = tb.S;
+  }
+  if (int rc = dalloc(c, &c->scratch, sizeof(double2) * 6 * (size_t)c->Smax)) return rc;
+  // Control block.
+  Ctl& h = c->hctl;
+  h.parity = 0; h.step = 0; h.any = 0; h.nmem = n_members;
+  h.maxit = members[0].maxit;
+  h.tol = members[0].tol;
+  h.hist_cap = 1024;
+  int rc;
+  if ((rc = dalloc(c, &h.phase, sizeof(int) * n_members))) return rc;
+  if ((rc = dalloc(c, &h.ite, sizeof(int) * n_members))) return rc;
+  if ((rc = dalloc(c, &h.status, sizeof(int) * n_members))) return rc;
+  if ((rc = dalloc(c, &h.num, sizeof(unsigned long long) * n_members))) return rc;
+  if ((rc = dalloc(c, &h.den, sizeof(unsigned long long) * n_members))) return rc;
+  if ((rc = dalloc(c, &h.err, sizeof(double) * n_members))) return rc;
+  if ((rc = dalloc(c, &h.hist, sizeof(int) * n_members * (size_t)h.hist_cap))) return rc;
+  CK(cudaMemset(h.phase, 0, sizeof(int) * n_members));
+  CK(cudaMemset(h.ite, 0, sizeof(int) * n_members));
+  CK(cudaMemset(h.status, 0, sizeof(int) * n_members));
+  CK(cudaMemset(h.num, 0, sizeof(unsigned long long) * n_members));
+  CK(cudaMemset(h.den, 0, sizeof(unsigned long long) * n_members));
+  CK(cudaMemset(h.err, 0, sizeof(double) * n_members));
+  if ((rc = dalloc(c, &c->dctl, sizeof(Ctl)))) return rc;
+  CK(cudaMemcpy(c->dctl, &h, sizeof(Ctl), cudaMemcpyHostToDevice));
+  return NSP_OK;
+}
+
+int nsp_setup(nsp_ctx* c) {
+  if (!c) return NSP_ERR_ARG;
+  CK(cudaSetDevice(c->device));
+  for (auto& g : c->groups) {
+    // maxit/tol are per context in the device control block: all groups must agree.
+    if (g.p.maxit != c->hctl.maxit || g.p.tol != c->hctl.tol)
+      return fail(c, NSP_ERR_ARG, "all members must share maxit and tol");
+    build_operators(g.p, g.ops);
+    Tables& tb = g.tb;
+    const nsp_params& p = g.p;
+    HostOps& o = g.ops;
+    std::vector<double> rinv(p.NR), rinv2(p.NR);
+    for (int i = 0; i < p.NR; i++) { rinv[i] = 1.0 / o.r[i]; rinv2[i] = 1.0 / (o.r[i] * o.r[i]); }
+    int rc;
+    if ((rc = upload(c, &tb.r, o.r)) || (rc = upload(c, &tb.rinv, rinv)) || (rc = upload(c, &tb.rinv2, rinv2)) ||
+        (rc = upload(c, &tb.rdr, o.rdr)) || (rc = upload(c, &tb.uc, o.uc)) || (rc = upload(c, &tb.D, o.D)) ||
+        (rc = upload(c, &tb.Lu, o.Lu)) || (rc = upload(c, &tb.fac, o.fac)) || (rc = upload(c, &tb.V, o.V)))
+      return rc;
+    std::vector<double2> wt = twiddles(tb.NTP), wz = twiddles(tb.NZR);
+    if ((rc = upload(c, &tb.tw_t, wt)) || (rc = upload(c, &tb.tw_z, wz)) || (rc = upload(c, &tb.tw_t32, to_f32(wt))) ||
+        (rc = upload(c, &tb.tw_z32, to_f32(wz))))
+      return rc;
+    make_plan(tb.NTP, tb.pt);
+    make_plan(tb.NZR, tb.pz);
+    tb.kts = PI2 / p.LT;
+    tb.kzs = PI2 / p.LZ;
+    tb.inv_dt = 1.0 / p.dt;
+    tb.c_ex = (1.0 - p.d_im) / p.Re;
+    tb.d_im = p.d_im;
+    tb.one_m_dim = 1.0 - p.d_im;
+    tb.two_re = 2.0 / p.Re;
+    tb.Qdes = p.Qdes;
+    tb.Qc = o.Qc;
+    tb.inv_norm = 1.0 / ((double)tb.NTP * (double)tb.NZR);
+    // Release the large host tables; keep grid data for diagnostics.
+    std::vector<double>().swap(o.fac);
+    std::vector<double2>().swap(o.V);
+  }
+  configure_transform_kernels();
+  configure_linear_kernels();
+  CK(cudaGetLastError());
+  int rc = build_graph(c);
+  if (rc) return rc;
+  c->setup_done = true;
+  return NSP_OK;
+}
+
+int nsp_load_state(nsp_ctx* c, int m, const char* fr, const char* ft, const char* fz) {
+  if (int rc = check_member(c, m)) return rc;
+  Group& g = c->groups[c->grp[m]];
+  size_t n = (size_t)g.tb.S;
+  std::vector<double> buf(2 * n * 3);
+  const char* names[3] = {fr, ft, fz};
+  for (int k = 0; k < 3; k++) {
+    if (!names[k]) return fail(c, NSP_ERR_ARG, "null file name");
+    FILE* f = fopen(names[k], "rb");
+    if (!f) return fail(c, NSP_ERR_IO, "reading error: %s", names[k]);
+    size_t got = fread(buf.data() + 2 * n * k, 16, n, f);
+    int extra = fgetc(f);
+    fclose(f);
+    if (got != n) return fail(c, NSP_ERR_IO, "reading error: %s holds %zu of %zu values", names[k], got, n);
+    if (extra != EOF) return fail(c, NSP_ERR_IO, "reading error: %s is longer than %zu values", names[k], n);
+  }
+  return nsp_set_state_host(c, m, buf.data(), buf.data() + 2 * n, buf.data() + 4 * n);
+}
+
+int nsp_save_state(nsp_ctx* c, int m, const char* fr, const char* ft, const char* fz) {
+  if (int rc = check_member(c, m)) return rc;
+  Group& g = c->groups[c->grp[m]];
+  size_t n = (size_t)g.tb.S;
+  std::vector<double> buf(2 * n * 3);
+  if (int rc = nsp_get_state_host(c, m, buf.data(), buf.data() + 2 * n, buf.data() + 4 * n)) return rc;
+  const char* names[3] = {fr, ft, fz};
+  for (int k = 0; k < 3; k++) {
+    if (!names[k]) return fail(c, NSP_ERR_ARG, "null file name");
+    FILE* f = fopen(names[k], "wb");
+    if (!f) return fail(c, NSP_ERR_IO, "writing error: %s", names[k]);
+    size_t put = fwrite(buf.data() + 2 * n * k, 16, n, f);
+    int cl = fclose(f);
+    if (put != n || cl != 0) return fail(c, NSP_ERR_IO, "writing error: %s", names[k]);
+  }
+  return NSP_OK;
+}
+
+int nsp_set_state_host(nsp_ctx* c, int m, const double* ur, const double* ut, const double* uz) {
+  if (int rc = check_member(c, m)) return rc;
+  if (!ur || !ut || !uz) return fail(c, NSP_ERR_ARG, "null state pointer");
+  size_t bytes = sizeof(double2) * (size_t)c->groups[c->grp[m]].tb.S;
+  const double* src[3] = {ur, ut, uz};
+  for (int k = 0; k < 3; k++) CK(cudaMemcpyAsync(state_ptr(c, m, k), src[k], bytes, cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return NSP_OK;
+}
+
+int nsp_get_state_host(nsp_ctx* c, int m, double* ur, double* ut, double* uz) {
+  if (int rc = check_member(c, m)) return rc;
+  if (!ur || !ut || !uz) return fail(c, NSP_ERR_ARG, "null state pointer");
+  size_t bytes = sizeof(double2) * (size_t)c->groups[c->grp[m]].tb.S;
+  double* dst[3] = {ur, ut, uz};
+  for (int k = 0; k < 3; k++) CK(cudaMemcpyAsync(dst[k], state_ptr(c, m, k), bytes, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return NSP_OK;
+}
+
+int nsp_set_state_device(nsp_ctx* c, int m, const void* ur, const void* ut, const void* uz) {
+  if (int rc = check_member(c, m)) return rc;
+  if (!ur || !ut || !uz) return fail(c, NSP_ERR_ARG, "null state pointer");
+  size_t bytes = sizeof(double2) * (size_t)c->groups[c->grp[m]].tb.S;
+  const void* src[3] = {ur, ut, uz};
+  for (int k = 0; k < 3; k++) CK(cudaMemcpyAsync(state_ptr(c, m, k), src[k], bytes, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return NSP_OK;
+}
+
+int nsp_get_state_device(nsp_ctx* c, int m, void* ur, void* ut, void* uz) {
+  if (int rc = check_member(c, m)) return rc;
+  if (!ur || !ut || !uz) return fail(c, NSP_ERR_ARG, "null state pointer");
+  size_t bytes = sizeof(double2) * (size_t)c->groups[c->grp[m]].tb.S;
+  void* dst[3] = {ur, ut, uz};
+  for (int k = 0; k < 3; k++) CK(cudaMemcpyAsync(dst[k], state_ptr(c, m, k), bytes, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return NSP_OK;
+}
+
+int nsp_step(nsp_ctx* c, int nsteps, int* iters_out) {
+  if (!c) return NSP_ERR_ARG;
+  if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_step before nsp_setup");
+  if (nsteps < 0) return fail(c, NSP_ERR_ARG, "nsteps < 0");
+  CK(cudaSetDevice(c->device));
+  const int nm = c->nmem;
+  const int cap = c->hctl.hist_cap;
+  long long launches = 0;
+  const long long per_iter = 4LL * (long long)c->groups.size() + 1;
+  std::vector<int> hist;
+  for (int done = 0; done < nsteps;) {
+    int chunk = std::min(cap, nsteps - done);
+    CK(cudaMemsetAsync(&c->dctl->step, 0, sizeof(int), c->st));
+    if (c->use_graph) {
+      for (int s = 0; s < chunk; s++) CK(cudaGraphLaunch(c->gexec, c->st));
+    } else {
+      for (int s = 0; s < chunk; s++) {
+        for (int it = 0; it <= c->hctl.maxit; it++) {
+          for (auto& g : c->groups) {
+            launch_nonlinear(g.tb, g.bf, c->dctl, c->precision == NSP_MIXED, nullptr, nullptr, c->st);
+            launch_linear(g.tb, g.bf, c->dctl, c->st);
+          }
+          launch_converge(c->dctl, nm, 0ull, 0, c->st);
+          CK(cudaGetLastError());
+          int any = 1;
+          CK(cudaMemcpyAsync(&any, &c->dctl->any, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+          CK(cudaStreamSynchronize(c->st));
+          if (!any) break;
+        }
+      }
+    }
+    CK(cudaGetLastError());
+    hist.resize((size_t)chunk * nm);
+    CK(cudaMemcpyAsync(hist.data(), c->hctl.hist, sizeof(int) * hist.size(), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (int s = 0; s < chunk; s++) {
+      int mx = 0;
+      for (int m = 0; m < nm; m++) mx = std::max(mx, hist[(size_t)s * nm + m]);
+      launches += (1 + mx) * per_iter;
+      if (iters_out)
+        for (int m = 0; m < nm; m++) iters_out[(size_t)(done + s) * nm + m] = hist[(size_t)s * nm + c->internal[m]];
+    }
+    c->parity ^= (chunk & 1);
+    done += chunk;
+  }
+  c->launches_last = launches;
+  std::vector<int> status(nm);
+  CK(cudaMemcpy(status.data(), c->hctl.status, sizeof(int) * nm, cudaMemcpyDeviceToHost));
+  for (int m = 0; m < nm; m++)
+    if (status[c->internal[m]] & NSP_ERR_NONFINITE)
+      return fail(c, NSP_ERR_NONFINITE, "member %d: non-finite velocity or convergence measure", m);
+  return NSP_OK;
+}
+
+int nsp_nonlinear(nsp_ctx* c, int m, const void* ur, const void* ut, const void* uz, void* nr, void* nt, void* nz) {
+  if (int rc = check_member(c, m)) return rc;
+  if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_nonlinear before nsp_setup");
+  Group& g = c->groups[c->grp[m]];
+  size_t S = (size_t)g.tb.S, bytes = sizeof(double2) * S;
+  double2* in = c->scratch;
+  double2* out = c->scratch + 3 * S;
+  const void* src[3] = {ur, ut, uz};
+  void* dst[3] = {nr, nt, nz};
+  for (int k = 0; k < 3; k++) CK(cudaMemcpyAsync(in + k * S, src[k], bytes, cudaMemcpyDeviceToDevice, c->st));
+  launch_nonlinear(g.tb, g.bf, c->dctl, c->precision == NSP_MIXED, in, out, c->st);
+  CK(cudaGetLastError());
+  for (int k = 0; k < 3; k++) CK(cudaMemcpyAsync(dst[k], out + k * S, bytes, cudaMemcpyDeviceToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return NSP_OK;
+}
+
+int nsp_lusolve(nsp_ctx* c, int m, int kind, const void* rhs, void* sol) {
+  if (int rc = check_member(c, m)) return rc;
+  if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_lusolve before nsp_setup");
+  if (kind < 0 || kind > 3) return fail(c, NSP_ERR_ARG, "kind %d not in 0..3", kind);
+  Group& g = c->groups[c->grp[m]];
+  launch_lusolve(g.tb, kind, (const double2*)rhs, (double2*)sol, c->st);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->st));
+  return NSP_OK;
+}
+
+int nsp_diag(nsp_ctx* c, int m, nsp_diag_out* out) {
+  if (int rc = check_member(c, m)) return rc;
+  if (!out) return fail(c, NSP_ERR_ARG, "null output");
+  if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_diag before nsp_setup");
+  Group& g = c->groups[c->grp[m]];
+  const int NR = g.tb.NR;
+  std::vector<double2> uz(NR);
+  CK(cudaMemcpy2DAsync(uz.data(), sizeof(double2), state_ptr(c, m, 2), sizeof(double2) * g.tb.NTNZ, sizeof(double2), NR,
+                       cudaMemcpyDeviceToHost, c->st));
+  int mi = c->internal[m];
+  double err = 0.0;
+  int status = 0;
+  CK(cudaMemcpyAsync(&err, c->hctl.err + mi, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(&status, c->hctl.status + mi, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  int ite = 0;
+  CK(cudaMemcpyAsync(&ite, c->hctl.ite + mi, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  const HostOps& o = g.ops;
+  double ucen = 0.0, du = 0.0, Q = 0.0;
+  for (int i = 0; i <= IW; i++) ucen += uz[i].x * o.dr0[i];
+  for (int i = 0; i < STEN; i++) du += uz[NR - STEN + i].x * o.D[(size_t)(NR - 1) * STEN + i];
+  for (int i = 0; i < NR; i++) Q += o.rdr[i] * uz[i].x;
+  out->u_centre = ucen;
+  out->u_tau = std::sqrt(std::fabs(du) / g.p.Re);
+  out->flux = Q;
+  out->last_err = err;
+  out->last_iters = ite;
+  out->status = (status & NSP_ERR_NONFINITE) ? NSP_ERR_NONFINITE : NSP_OK;
+  return NSP_OK;
+}
+
+int nsp_grid(nsp_ctx* c, int m, double* r, double* rdr) {
+  if (int rc = check_member(c, m)) return rc;
+  if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_grid before nsp_setup");
+  const HostOps& o = c->groups[c->grp[m]].ops;
+  if (r) memcpy(r, o.r.data(), sizeof(double) * o.r.size());
+  if (rdr) memcpy(rdr, o.rdr.data(), sizeof(double) * o.rdr.size());
+  return NSP_OK;
+}
+
+long long nsp_kernel_launches(nsp_ctx* c) { return c ? c->launches_last : 0; }
+
+int nsp_sync(nsp_ctx* c) {
+  if (!c) return NSP_ERR_ARG;
+  CK(cudaStreamSynchronize(c->st));
+  return NSP_OK;
+}
+
+const char* nsp_last_error(nsp_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int nsp_destroy(nsp_ctx* c) {
+  if (!c) return NSP_OK;
+  cudaSetDevice(c->device);
+  if (c->st) cudaStreamSynchronize(c->st);
+  if (c->gexec) cudaGraphExecDestroy(c->gexec);
+  for (void* p : c->allocs) cudaFree(p);
+  if (c->st) cudaStreamDestroy(c->st);
+  delete c;
+  return NSP_OK;
+}
+
+}  // extern "C"

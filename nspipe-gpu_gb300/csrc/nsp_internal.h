@@ -1,0 +1,99 @@
+// nsp_internal.h -- device-side data structures shared by the kernels and the host API.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <string>
+#include <vector>
+
+#include "../../include/nspipe_gb300.h"
+
+namespace nsp {
+
+constexpr double PI2 = 6.283185307179586;  // the reference's 2*pi literal (head.h:12)
+constexpr int STEN = 7;                     // radial stencil width (head.h:44)
+constexpr int IW = 3;                       // half stencil (head.h:45)
+constexpr int NFAC = 7;                     // stored factor entries per row: L(i-3..i-1), 1/U_ii, U(i+1..i+3)
+constexpr int MAXPLAN = 12;                 // radix stages of one transform length
+
+// FFT plan for one length: radices applied in order (Stockham, natural order out).
+struct FftPlan {
+  int n;
+  int nst;
+  int rad[MAXPLAN];
+};
+
+// Operator tables of one group of members sharing (NR, NT, NZ, LT, LZ, Re, dt, d_im).
+// All pointers are device memory; the struct is passed to kernels by value.
+struct Tables {
+  int NR, NT, NZ, NTP, NZP, NZR, NTNZ;
+  long long S;         // NR*NT*NZ
+  int nmem;            // members in this group
+  int mem0;            // global index of the group's first member
+  double kts, kzs;     // 2pi/LT, 2pi/LZ (wavenumber scales, mod_deriv.cu:17,31)
+  double inv_dt, c_ex, d_im, one_m_dim, two_re, Qdes, Qc, inv_norm;
+  const double* r;
+  const double* rinv;
+  const double* rinv2;  // 1/(r*r)
+  const double* rdr;
+  const double* uc;
+  const double* D;     // [2][NR][7]: first derivative, parity tables (0 even-extended, 1 odd)
+  const double* Lu;    // [2][NR][7]: radial Laplacian rows with identity wall row
+  const double* fac;   // [4][NR][7][NTNZ]: banded LU factors of u+, u-, u_z, p
+  const double2* V;    // [3][NR][NTNZ]: influence-matrix correction profiles (+, -, z)
+  const double2* tw_t; // [NTP] exp(-2 pi i e/NTP), FP64
+  const double2* tw_z; // [NZR]
+  const float2* tw_t32;
+  const float2* tw_z32;
+  FftPlan pt, pz;
+};
+
+// Batched per-group member buffers.
+struct Bufs {
+  double2* U[2];       // [nmem][3][S]: state / corrector iterate, roles swap each step (parity)
+  double2* RHSW;       // [nmem][3][S]: N(u^n) in +/- form (rhsw of mod_integrate.cu:100-107)
+  double2* N;          // [nmem][3][S]: nonlinear term output
+  void* G;             // [nmem][9][NR][NTP][NZ] complex T: theta-inverse of u, dr u, i m u / r
+  void* H;             // [nmem][3][NR][NTP][NZ] complex T: z-forward of the nonlinear product
+};
+
+// Device control block of one context.  phase[m]: 0 = predictor pending,
+// p > 0 = corrector iteration p pending, -1 = converged for this step.
+struct Ctl {
+  int parity;          // U[parity] holds the state u^n, U[parity^1] the iterate
+  int step;            // steps completed in the current nsp_step call
+  int any;             // host-visible copy of the loop condition
+  int nmem;
+  int maxit;
+  double tol;
+  int* phase;
+  int* ite;
+  int* status;
+  unsigned long long* num;  // max |u_i - u|^2 as ordered bits (>= 0)
+  unsigned long long* den;  // max |u_i|^2
+  double* err;
+  int* hist;           // [cap][nmem]: iterations of each step of the call
+  int hist_cap;
+};
+
+// Kernel launchers (nsp_transform.cu, nsp_linear.cu).
+// Nonlinear term of every active member of a group (or of one explicit field).
+void launch_nonlinear(const Tables& tb, const Bufs& bf, Ctl* dctl, bool mixed, const double2* src_override,
+                      double2* dst_override, cudaStream_t st);
+void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st);
+void launch_converge(Ctl* dctl, int nmem, unsigned long long cond_handle, int use_cond, cudaStream_t st);
+void launch_lusolve(const Tables& tb, int kind, const double2* rhs, double2* sol, cudaStream_t st);
+int kernels_per_nonlinear();
+
+// Host-side operator construction (nsp_setup.cpp).
+struct HostOps {
+  int NR;
+  std::vector<double> r, rdr, D, D2, Lu, Lp, dr0;
+  std::vector<double> fac;     // [4][NR][7][NTNZ]
+  std::vector<double2> V;      // [3][NR][NTNZ]
+  std::vector<double> uc;
+  double Qc;
+};
+void build_operators(const nsp_params& p, HostOps& out);
+void radial_fd(int NR, HostOps& out);
+
+}  // namespace nsp

@@ -1,0 +1,403 @@
+// nsp_linear.cu -- the linear part of the predictor and corrector, one CTA per
+// block of LM (m, k_z) mode lines of one member, all in FP64.
+//
+// One launch replaces the ~28 launches of predictor()/corrector()
+// (mod_integrate.cu:164-228): decoupleForward/Backward (mod_utils.cu:30-59),
+// addRHS_k (mod_integrate.cu:43-59), addLaplacian (mod_linear.cu:12-51,652-661),
+// divergence (mod_radialFD.cu:67-96), write_bcon (mod_utils.cu:20-27), LUsolve_p
+// and LUsolve_u x3 (mod_linear.cu:55-646), addGrad (mod_radialFD.cu:115-143),
+// corBCon (mod_boundary.cu:269-278), modeZZ (mod_integrate.cu:63-68), adj_flux
+// (mod_cublasflux.cu:90-103) and, in the corrector, the convergence measure
+// mcor_k + iden_max (mod_integrate.cu:9-40, mod_cublasflux.cu:106-116) as a
+// block max reduction and one atomicMax per CTA.
+//
+// The radial lines of the block's modes are staged in shared memory as
+// [component][r][mode]; pointwise and stencil phases use all threads over
+// (r, mode), the banded solves one thread per (component, mode) sweeping r with
+// the precomputed factors (read coalesced across modes).  u^n in +/- form (uw)
+// is recomputed from the state instead of stored.
+#include <cstdio>
+
+#include "nsp_internal.h"
+
+namespace nsp {
+
+constexpr int LIN_THREADS = 256;
+
+__device__ __forceinline__ double2 c2(double x, double y) { return make_double2(x, y); }
+
+// Forward + backward substitution of one mode line held in X[i*ld] (i = 0..NR-1).
+__device__ __forceinline__ void solve_line(double2* X, int ld, const double* __restrict__ f, int NTNZ, int NR) {
+  const size_t rs = (size_t)NFAC * NTNZ;  // row stride of the factor table
+  double2 xm1 = c2(0, 0), xm2 = c2(0, 0), xm3 = c2(0, 0);
+  for (int i = 0; i < NR; i++) {
+    const double* fr = f + i * rs;
+    double2 x = X[i * ld];
+    if (i >= 3) { double l = __ldg(fr); x.x -= l * xm3.x; x.y -= l * xm3.y; }
+    if (i >= 2) { double l = __ldg(fr + NTNZ); x.x -= l * xm2.x; x.y -= l * xm2.y; }
+    if (i >= 1) { double l = __ldg(fr + 2 * NTNZ); x.x -= l * xm1.x; x.y -= l * xm1.y; }
+    X[i * ld] = x;
+    xm3 = xm2; xm2 = xm1; xm1 = x;
+  }
+  double2 xp1 = c2(0, 0), xp2 = c2(0, 0), xp3 = c2(0, 0);
+  for (int i = NR - 1; i >= 0; i--) {
+    const double* fr = f + i * rs;
+    double2 x = X[i * ld];
+    if (i + 1 < NR) { double u = __ldg(fr + 4 * NTNZ); x.x -= u * xp1.x; x.y -= u * xp1.y; }
+    if (i + 2 < NR) { double u = __ldg(fr + 5 * NTNZ); x.x -= u * xp2.x; x.y -= u * xp2.y; }
+    if (i + 3 < NR) { double u = __ldg(fr + 6 * NTNZ); x.x -= u * xp3.x; x.y -= u * xp3.y; }
+    double ui = __ldg(fr + 3 * NTNZ);
+    x.x *= ui;
+    x.y *= ui;
+    X[i * ld] = x;
+    xp3 = xp2; xp2 = xp1; xp1 = x;
+  }
+}
+
+template <int LM>
+__global__ void __launch_bounds__(LIN_THREADS) linear_k(Tables tb, Bufs bf, Ctl* ctl) {
+  const int mloc = blockIdx.y, gm = tb.mem0 + mloc;
+  const int ph = ctl->phase[gm];
+  if (ph < 0) return;
+  const bool pred = (ph == 0);
+  const int par = ctl->parity;
+  const int NR = tb.NR, NT = tb.NT, NZ = tb.NZ, NTNZ = tb.NTNZ;
+  const long long S = tb.S;
+  const int k0 = blockIdx.x * LM;
+  const int LN = NR * LM;
+  extern __shared__ double2 sm[];
+  double2* W = sm;           // [3][NR][LM] u^n in +/- form
+  double2* R = sm + 3 * LN;  // [3][NR][LM] right-hand side, then the new velocity
+  double2* P = W;            // divergence / pressure (W is dead by then)
+  __shared__ double2 dvs[LM];
+  __shared__ double wnum[LIN_THREADS / 32], wden[LIN_THREADS / 32];
+  __shared__ int bad;
+  const double2* Un = bf.U[par] + (size_t)mloc * 3 * S;
+  double2* Ui = bf.U[par ^ 1] + (size_t)mloc * 3 * S;
+  const double2* Nn = bf.N + (size_t)mloc * 3 * S;
+  double2* Rw = bf.RHSW + (size_t)mloc * 3 * S;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  if (tid == 0) bad = 0;
+
+  // A. u^n -> +/- (uw), N -> +/-; predictor stores rhsw, corrector blends d_im N + (1-d_im) rhsw.
+  for (int p = tid; p < LN; p += nth) {
+    int i = p / LM, mm = p - i * LM, k = k0 + mm;
+    if (k >= NTNZ) {
+      for (int c = 0; c < 3; c++) { W[c * LN + p] = c2(0, 0); R[c * LN + p] = c2(0, 0); }
+      continue;
+    }
+    size_t h = (size_t)i * NTNZ + k;
+    double2 ur = Un[h], ut = Un[S + h], uz = Un[2 * S + h];
+    W[p] = c2(ur.x - ut.y, ur.y + ut.x);
+    W[LN + p] = c2(ur.x + ut.y, ur.y - ut.x);
+    W[2 * LN + p] = uz;
+    double2 nr = Nn[h], nt = Nn[S + h], nz = Nn[2 * S + h];
+    double2 np = c2(nr.x - nt.y, nr.y + nt.x), nm = c2(nr.x + nt.y, nr.y - nt.x);
+    if (pred) {
+      Rw[h] = np; Rw[S + h] = nm; Rw[2 * S + h] = nz;
+    } else {
+      double2 w0 = Rw[h], w1 = Rw[S + h], w2 = Rw[2 * S + h];
+      np = c2(tb.d_im * np.x + tb.one_m_dim * w0.x, tb.d_im * np.y + tb.one_m_dim * w0.y);
+      nm = c2(tb.d_im * nm.x + tb.one_m_dim * w1.x, tb.d_im * nm.y + tb.one_m_dim * w1.y);
+      nz = c2(tb.d_im * nz.x + tb.one_m_dim * w2.x, tb.d_im * nz.y + tb.one_m_dim * w2.y);
+    }
+    R[p] = np; R[LN + p] = nm; R[2 * LN + p] = nz;
+  }
+  __syncthreads();
+
+  // B. rhs += u/dt + (1-d_im)/Re (L_r - k_z^2 - m^2/r^2 [-1/r^2 -+ 2m/r^2]) u, then +/- -> r/theta.
+  for (int p = tid; p < LN; p += nth) {
+    int i = p / LM, mm = p - i * LM, k = k0 + mm;
+    if (k >= NTNZ) continue;
+    int it = k / NZ, l = k - it * NZ, m = it < NT / 2 ? it : it - NT;
+    double kt = tb.kts * (double)m, kz = tb.kzs * (double)l;
+    int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
+    double ir2 = tb.rinv2[i];
+    double base = -kz * kz - kt * kt * ir2;
+    double2 out[3];
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      int tab = abs((abs(m) % 2) - (c < 2 ? 1 : 0));
+      const double* Lr = tb.Lu + tab * STEN * NR + STEN * i + i0;
+      const double2* Wc = W + c * LN + mm;
+      double sx = 0.0, sy = 0.0;
+      for (int j = 0; j < len; j++) {
+        double de = __ldg(Lr + j);
+        double2 a = Wc[(left + j) * LM];
+        sx += de * a.x;
+        sy += de * a.y;
+      }
+      double2 aux = Wc[i * LM];
+      double de = base;
+      if (c == 0) de += -ir2 - 2.0 * kt * ir2;
+      else if (c == 1) de += -ir2 + 2.0 * kt * ir2;
+      sx += de * aux.x;
+      sy += de * aux.y;
+      sx *= tb.c_ex;
+      sy *= tb.c_ex;
+      sx += tb.inv_dt * aux.x;
+      sy += tb.inv_dt * aux.y;
+      double2 rr = R[c * LN + p];
+      out[c] = c2(rr.x + sx, rr.y + sy);
+    }
+    R[p] = c2(0.5 * (out[0].x + out[1].x), 0.5 * (out[0].y + out[1].y));
+    R[LN + p] = c2(0.5 * (out[0].y - out[1].y), -0.5 * (out[0].x - out[1].x));
+    R[2 * LN + p] = out[2];
+  }
+  __syncthreads();
+
+  // C. divergence of rhs into P; wall row = 0 (write_bcon).
+  for (int p = tid; p < LN; p += nth) {
+    int i = p / LM, mm = p - i * LM, k = k0 + mm;
+    double2 d = c2(0, 0);
+    if (k < NTNZ && i < NR - 1) {
+      int it = k / NZ, l = k - it * NZ, m = it < NT / 2 ? it : it - NT;
+      double kt = tb.kts * (double)m, kz = tb.kzs * (double)l;
+      int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
+      int tab = abs((abs(m) % 2) - 1);
+      const double* Dr = tb.D + tab * STEN * NR + STEN * i + i0;
+      double sx = 0.0, sy = 0.0;
+      for (int j = 0; j < len; j++) {
+        double de = __ldg(Dr + j);
+        double2 a = R[(left + j) * LM + mm];
+        sx += de * a.x;
+        sy += de * a.y;
+      }
+      double ri = tb.rinv[i];
+      double2 rr = R[p], rt = R[LN + p], rz = R[2 * LN + p];
+      sx += rr.x * ri; sy += rr.y * ri;
+      sx += -kt * rt.y * ri; sy += kt * rt.x * ri;
+      sx += -kz * rz.y; sy += kz * rz.x;
+      d = c2(sx, sy);
+    }
+    P[p] = d;
+  }
+  __syncthreads();
+
+  // D. pressure Poisson solve, one thread per mode.
+  if (tid < LM && k0 + tid < NTNZ) solve_line(P + tid, LM, tb.fac + 3 * (size_t)NR * NFAC * NTNZ + k0 + tid, NTNZ, NR);
+  __syncthreads();
+
+  // E. rhs -= grad p, r/theta -> +/-, wall rows = 0.
+  for (int p = tid; p < LN; p += nth) {
+    int i = p / LM, mm = p - i * LM, k = k0 + mm;
+    if (k >= NTNZ) continue;
+    double2 up = c2(0, 0), um = c2(0, 0), rz = c2(0, 0);
+    if (i < NR - 1) {
+      int it = k / NZ, l = k - it * NZ, m = it < NT / 2 ? it : it - NT;
+      double kt = tb.kts * (double)m, kz = tb.kzs * (double)l;
+      int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
+      int tab = abs(m) % 2;
+      const double* Dr = tb.D + tab * STEN * NR + STEN * i + i0;
+      double sx = 0.0, sy = 0.0;
+      for (int j = 0; j < len; j++) {
+        double de = __ldg(Dr + j);
+        double2 a = P[(left + j) * LM + mm];
+        sx += de * a.x;
+        sy += de * a.y;
+      }
+      double ri = tb.rinv[i];
+      double2 pp = P[p], rr = R[p], rt = R[LN + p];
+      rz = R[2 * LN + p];
+      rr.x -= sx; rr.y -= sy;
+      rt.x -= -kt * pp.y * ri; rt.y -= kt * pp.x * ri;
+      rz.x -= -kz * pp.y; rz.y -= kz * pp.x;
+      up = c2(rr.x - rt.y, rr.y + rt.x);
+      um = c2(rr.x + rt.y, rr.y - rt.x);
+    }
+    R[p] = up; R[LN + p] = um; R[2 * LN + p] = rz;
+  }
+  __syncthreads();
+
+  // F. Helmholtz solves for u+, u-, u_z.
+  if (tid < 3 * LM) {
+    int c = tid / LM, mm = tid - c * LM;
+    if (k0 + mm < NTNZ) solve_line(R + c * LN + mm, LM, tb.fac + (size_t)c * NR * NFAC * NTNZ + k0 + mm, NTNZ, NR);
+  }
+  __syncthreads();
+
+  // G1. wall divergence of the solution (in r/theta form) per mode.
+  if (tid < LM) {
+    int mm = tid, k = k0 + mm;
+    double2 dv = c2(0, 0);
+    if (k < NTNZ) {
+      int it = k / NZ, l = k - it * NZ, m = it < NT / 2 ? it : it - NT;
+      double kt = tb.kts * (double)m, kz = tb.kzs * (double)l;
+      int tab = abs((abs(m) % 2) - 1);
+      const double* Dw = tb.D + tab * STEN * NR + STEN * (NR - 1) + IW;
+      double sx = 0.0, sy = 0.0;
+      double2 urw = c2(0, 0), utw = c2(0, 0);
+      for (int j = 0; j <= IW; j++) {
+        int row = NR - 1 - IW + j;
+        double2 a = R[row * LM + mm], b = R[LN + row * LM + mm];
+        double2 ur = c2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y));
+        double de = __ldg(Dw + j);
+        sx += de * ur.x;
+        sy += de * ur.y;
+        if (j == IW) { urw = ur; utw = c2(0.5 * (a.y - b.y), -0.5 * (a.x - b.x)); }
+      }
+      double2 uzw = R[2 * LN + (NR - 1) * LM + mm];
+      sx += urw.x; sy += urw.y;
+      sx += -kt * utw.y; sy += kt * utw.x;
+      sx += -kz * uzw.y; sy += kz * uzw.x;
+      dv = c2(-sx, -sy);
+    }
+    dvs[mm] = dv;
+  }
+  __syncthreads();
+
+  // G2. u += (-div_wall) V, back to r/theta, mode (0,0) constraints.
+  for (int p = tid; p < LN; p += nth) {
+    int i = p / LM, mm = p - i * LM, k = k0 + mm;
+    if (k >= NTNZ) continue;
+    double2 a = R[p], b = R[LN + p], uz = R[2 * LN + p];
+    double2 ur = c2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y));
+    double2 ut = c2(0.5 * (a.y - b.y), -0.5 * (a.x - b.x));
+    double2 up = c2(ur.x - ut.y, ur.y + ut.x), um = c2(ur.x + ut.y, ur.y - ut.x);
+    double2 dv = dvs[mm];
+    size_t hv = (size_t)i * NTNZ + k;
+    double2 v0 = tb.V[hv], v1 = tb.V[S + hv], v2 = tb.V[2 * S + hv];
+    up.x += dv.x * v0.x - dv.y * v0.y; up.y += dv.x * v0.y + dv.y * v0.x;
+    um.x += dv.x * v1.x - dv.y * v1.y; um.y += dv.x * v1.y + dv.y * v1.x;
+    uz.x += dv.x * v2.x - dv.y * v2.y; uz.y += dv.x * v2.y + dv.y * v2.x;
+    ur = c2(0.5 * (up.x + um.x), 0.5 * (up.y + um.y));
+    ut = c2(0.5 * (up.y - um.y), -0.5 * (up.x - um.x));
+    if (k == 0) { ur = c2(0, 0); ut.y = 0.0; uz.y = 0.0; }
+    R[p] = ur; R[LN + p] = ut; R[2 * LN + p] = uz;
+  }
+  __syncthreads();
+
+  // H. constant mass flux on mode (0,0).
+  if (k0 == 0 && tid == 0) {
+    double Q = 0.0;
+    for (int i = 0; i < NR; i++) Q += tb.rdr[i] * R[2 * LN + i * LM].x;
+    double corr = (tb.Qdes - Q) / tb.Qc;
+    for (int i = 0; i < NR; i++) R[2 * LN + i * LM].x += corr * tb.uc[i];
+  }
+  __syncthreads();
+
+  // I. store the new iterate; corrector: convergence measure against the previous one.
+  double lnum = 0.0, lden = 0.0;
+  bool nonfin = false;
+  for (int p = tid; p < LN; p += nth) {
+    int i = p / LM, mm = p - i * LM, k = k0 + mm;
+    if (k >= NTNZ) continue;
+    size_t h = (size_t)i * NTNZ + k;
+    double n1 = 0.0, d1 = 0.0;
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      double2 v = R[c * LN + p];
+      if (!pred) {
+        double2 o = Ui[c * S + h];
+        double ex = o.x - v.x, ey = o.y - v.y;
+        n1 = fmax(n1, ex * ex + ey * ey);
+        d1 = fmax(d1, o.x * o.x + o.y * o.y);
+      }
+      nonfin |= !(isfinite(v.x) && isfinite(v.y));
+      Ui[c * S + h] = v;
+    }
+    lnum = fmax(lnum, n1);
+    lden = fmax(lden, d1);
+  }
+  if (nonfin) bad = 1;
+  if (!pred) {
+    for (int o = 16; o > 0; o >>= 1) {
+      lnum = fmax(lnum, __shfl_xor_sync(0xffffffffu, lnum, o));
+      lden = fmax(lden, __shfl_xor_sync(0xffffffffu, lden, o));
+    }
+    if ((tid & 31) == 0) { wnum[tid >> 5] = lnum; wden[tid >> 5] = lden; }
+  }
+  __syncthreads();
+  if (tid == 0) {
+    if (!pred) {
+      double a = 0.0, b = 0.0;
+      for (int w = 0; w < nth / 32; w++) { a = fmax(a, wnum[w]); b = fmax(b, wden[w]); }
+      atomicMax(ctl->num + gm, (unsigned long long)__double_as_longlong(a));
+      atomicMax(ctl->den + gm, (unsigned long long)__double_as_longlong(b));
+    }
+    if (bad) atomicOr(ctl->status + gm, NSP_ERR_NONFINITE);
+  }
+}
+
+// Per-member bookkeeping after each predictor/corrector pass; sets the graph's
+// loop condition.  Single block.
+__global__ void converge_k(Ctl* ctl, cudaGraphConditionalHandle h, int use_cond) {
+  __shared__ int any;
+  if (threadIdx.x == 0) any = 0;
+  __syncthreads();
+  const int nm = ctl->nmem;
+  for (int m = threadIdx.x; m < nm; m += blockDim.x) {
+    int ph = ctl->phase[m];
+    if (ph == 0) {
+      ph = 1;
+      ctl->ite[m] = 0;
+    } else if (ph > 0) {
+      int it = ctl->ite[m] + 1;
+      ctl->ite[m] = it;
+      double num = __longlong_as_double((long long)ctl->num[m]);
+      double den = __longlong_as_double((long long)ctl->den[m]);
+      double err = num / den;
+      ctl->err[m] = err;
+      if (!isfinite(err)) atomicOr(ctl->status + m, NSP_ERR_NONFINITE);
+      bool more = (it < ctl->maxit) && (err > ctl->tol);
+      if (!more) {
+        if (ctl->step < ctl->hist_cap) ctl->hist[(size_t)ctl->step * nm + m] = it;
+        ph = -1;
+      } else {
+        ph = ph + 1;
+      }
+    }
+    ctl->num[m] = 0ull;
+    ctl->den[m] = 0ull;
+    ctl->phase[m] = ph;
+    if (ph >= 0) any = 1;
+  }
+  __syncthreads();
+  if (!any) {  // every member converged: the step is complete, roles of state and iterate swap
+    for (int m = threadIdx.x; m < nm; m += blockDim.x) ctl->phase[m] = 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (!any) {
+      ctl->parity ^= 1;
+      ctl->step += 1;
+    }
+    ctl->any = any;
+    if (use_cond) cudaGraphSetConditional(h, any ? 1u : 0u);
+  }
+}
+
+__global__ void lusolve_k(Tables tb, int kind, const double2* rhs, double2* sol) {
+  int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= tb.NTNZ) return;
+  for (int i = 0; i < tb.NR; i++) sol[(size_t)i * tb.NTNZ + k] = rhs[(size_t)i * tb.NTNZ + k];
+  solve_line(sol + k, tb.NTNZ, tb.fac + (size_t)kind * tb.NR * NFAC * tb.NTNZ + k, tb.NTNZ, tb.NR);
+}
+
+static int lin_modes(int NR) { return NR <= 64 ? 16 : 8; }
+
+size_t linear_smem(int NR) { return sizeof(double2) * 6 * (size_t)NR * lin_modes(NR); }
+
+void configure_linear_kernels() {
+  cudaFuncSetAttribute(linear_k<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  cudaFuncSetAttribute(linear_k<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+}
+
+void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st) {
+  int LM = lin_modes(tb.NR);
+  dim3 grid((tb.NTNZ + LM - 1) / LM, tb.nmem);
+  size_t smem = linear_smem(tb.NR);
+  if (LM == 16) linear_k<16><<<grid, LIN_THREADS, smem, st>>>(tb, bf, dctl);
+  else linear_k<8><<<grid, LIN_THREADS, smem, st>>>(tb, bf, dctl);
+}
+
+void launch_converge(Ctl* dctl, int nmem, unsigned long long cond_handle, int use_cond, cudaStream_t st) {
+  (void)nmem;
+  converge_k<<<1, 256, 0, st>>>(dctl, (cudaGraphConditionalHandle)cond_handle, use_cond);
+}
+
+void launch_lusolve(const Tables& tb, int kind, const double2* rhs, double2* sol, cudaStream_t st) {
+  lusolve_k<<<(tb.NTNZ + 127) / 128, 128, 0, st>>>(tb, kind, rhs, sol);
+}
+
+}  // namespace nsp

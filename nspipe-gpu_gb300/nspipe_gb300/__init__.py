@@ -1,0 +1,210 @@
+"""Python binding of the GB300 pipe-flow stepper (libnspipe_gb300.so, include/nspipe_gb300.h).
+
+Host-side mirror of the nsPipe-CUDA driver interface: parameters as in head.h,
+the (u_r, u_theta, u_z) spectral state as complex128 arrays of shape
+(NR, NT, NZ) (the reference's double2[NR][NT][NZ] layout), restart files in the
+reference's raw format, and the per-step entry points.  All numerics run in the
+CUDA library; if it is missing this module raises instead of falling back.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from .initfield import PI2, radial_grid, read_state, seeded_field, write_state  # noqa: F401
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(os.path.dirname(_HERE), "libnspipe_gb300.so")
+
+NSP_OK, NSP_ERR_ARG, NSP_ERR_CUDA, NSP_ERR_IO, NSP_ERR_NONFINITE, NSP_ERR_STATE, NSP_ERR_NOMEM = range(7)
+NSP_FP64, NSP_MIXED = 0, 1
+
+EXPORTS = [
+    "nsp_default_params", "nsp_create", "nsp_setup", "nsp_load_state", "nsp_save_state",
+    "nsp_set_state_host", "nsp_get_state_host", "nsp_set_state_device", "nsp_get_state_device",
+    "nsp_step", "nsp_nonlinear", "nsp_lusolve", "nsp_diag", "nsp_grid", "nsp_kernel_launches",
+    "nsp_sync", "nsp_last_error", "nsp_destroy",
+]
+
+
+class NspParams(ctypes.Structure):
+    _fields_ = [
+        ("NR", ctypes.c_int), ("NT", ctypes.c_int), ("NZ", ctypes.c_int),
+        ("LT", ctypes.c_double), ("LZ", ctypes.c_double),
+        ("Re", ctypes.c_double), ("dt", ctypes.c_double), ("d_im", ctypes.c_double),
+        ("maxit", ctypes.c_int), ("tol", ctypes.c_double), ("sten", ctypes.c_int),
+        ("Qdes", ctypes.c_double),
+    ]
+
+
+class NspDiag(ctypes.Structure):
+    _fields_ = [
+        ("u_centre", ctypes.c_double), ("u_tau", ctypes.c_double), ("flux", ctypes.c_double),
+        ("last_err", ctypes.c_double), ("last_iters", ctypes.c_int), ("status", ctypes.c_int),
+    ]
+
+
+class NspError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("nspipe error %d: %s" % (code, msg))
+        self.code = code
+
+
+_LIB = None
+
+
+def lib():
+    """Load libnspipe_gb300.so (raises if it has not been built)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libnspipe_gb300.so not found at %s: run nspipe-gpu_gb300/build.py" % LIB_PATH)
+        L = ctypes.CDLL(LIB_PATH)
+        vp, ip, dp = ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)
+        L.nsp_default_params.argtypes = [ctypes.POINTER(NspParams)]
+        L.nsp_create.argtypes = [ctypes.POINTER(NspParams), ip, ip, ip, ctypes.POINTER(vp)]
+        L.nsp_setup.argtypes = [vp]
+        L.nsp_load_state.argtypes = [vp, ip, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]
+        L.nsp_save_state.argtypes = [vp, ip, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p]
+        L.nsp_set_state_host.argtypes = [vp, ip, dp, dp, dp]
+        L.nsp_get_state_host.argtypes = [vp, ip, dp, dp, dp]
+        L.nsp_set_state_device.argtypes = [vp, ip, vp, vp, vp]
+        L.nsp_get_state_device.argtypes = [vp, ip, vp, vp, vp]
+        L.nsp_step.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_int)]
+        L.nsp_nonlinear.argtypes = [vp, ip, vp, vp, vp, vp, vp, vp]
+        L.nsp_lusolve.argtypes = [vp, ip, ip, vp, vp]
+        L.nsp_diag.argtypes = [vp, ip, ctypes.POINTER(NspDiag)]
+        L.nsp_grid.argtypes = [vp, ip, dp, dp]
+        L.nsp_kernel_launches.argtypes = [vp]
+        L.nsp_kernel_launches.restype = ctypes.c_longlong
+        L.nsp_sync.argtypes = [vp]
+        L.nsp_last_error.argtypes = [vp]
+        L.nsp_last_error.restype = ctypes.c_char_p
+        L.nsp_destroy.argtypes = [vp]
+        _LIB = L
+    return _LIB
+
+
+def default_params(**kw):
+    """Reference defaults (head.h:16-61) with keyword overrides."""
+    p = NspParams()
+    lib().nsp_default_params(ctypes.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def make_params(NR, NT, NZ, Re, dt, LZ, LT=PI2, d_im=0.51, maxit=10, tol=5e-8, Qdes=0.5):
+    return default_params(NR=NR, NT=NT, NZ=NZ, Re=float(Re), dt=float(dt), LZ=float(LZ), LT=float(LT),
+                          d_im=d_im, maxit=maxit, tol=tol, Qdes=Qdes)
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def _ptr(x):
+    return x if isinstance(x, int) else x.data_ptr()
+
+
+class Stepper:
+    """An ensemble of independent pipes advanced together on one GPU."""
+
+    def __init__(self, params, precision=NSP_FP64, device=0, setup=True):
+        if isinstance(params, NspParams):
+            params = [params]
+        self.params = list(params)
+        self.n = len(self.params)
+        arr = (NspParams * self.n)(*self.params)
+        self._h = ctypes.c_void_p()
+        rc = lib().nsp_create(arr, self.n, precision, device, ctypes.byref(self._h))
+        if rc != NSP_OK:
+            msg = self.last_error()
+            self.close()
+            raise NspError(rc, msg)
+        self.precision = precision
+        if setup:
+            self._check(lib().nsp_setup(self._h))
+
+    # -- plumbing
+    def last_error(self):
+        return lib().nsp_last_error(self._h).decode() if self._h else "closed"
+
+    def _check(self, rc):
+        if rc != NSP_OK:
+            raise NspError(rc, self.last_error())
+        return rc
+
+    def close(self):
+        if self._h:
+            lib().nsp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def shape(self, m=0):
+        p = self.params[m]
+        return (p.NR, p.NT, p.NZ)
+
+    # -- state
+    def set_state(self, m, u):
+        u = [np.ascontiguousarray(a, np.complex128) for a in u]
+        for a in u:
+            if a.shape != self.shape(m):
+                raise ValueError("state shape %s != %s" % (a.shape, self.shape(m)))
+        self._check(lib().nsp_set_state_host(self._h, m, _dp(u[0]), _dp(u[1]), _dp(u[2])))
+
+    def get_state(self, m):
+        u = [np.zeros(self.shape(m), np.complex128) for _ in range(3)]
+        self._check(lib().nsp_get_state_host(self._h, m, _dp(u[0]), _dp(u[1]), _dp(u[2])))
+        return u
+
+    def set_state_device(self, m, ur, ut, uz):
+        self._check(lib().nsp_set_state_device(self._h, m, _ptr(ur), _ptr(ut), _ptr(uz)))
+
+    def get_state_device(self, m, ur, ut, uz):
+        self._check(lib().nsp_get_state_device(self._h, m, _ptr(ur), _ptr(ut), _ptr(uz)))
+
+    def load(self, m, directory, suffix="_s"):
+        f = [os.path.join(directory, "u%s%s.bin" % (c, suffix)).encode() for c in "rtz"]
+        self._check(lib().nsp_load_state(self._h, m, *f))
+
+    def save(self, m, directory, suffix=""):
+        os.makedirs(directory, exist_ok=True)
+        f = [os.path.join(directory, "u%s%s.bin" % (c, suffix)).encode() for c in "rtz"]
+        self._check(lib().nsp_save_state(self._h, m, *f))
+
+    # -- stepping and operators
+    def step(self, nsteps=1, check=True):
+        iters = np.zeros((nsteps, self.n), np.int32)
+        rc = lib().nsp_step(self._h, nsteps, iters.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+        if check:
+            self._check(rc)
+        return iters
+
+    def kernel_launches(self):
+        return lib().nsp_kernel_launches(self._h)
+
+    def nonlinear(self, m, u_dev, n_dev):
+        self._check(lib().nsp_nonlinear(self._h, m, *[_ptr(a) for a in u_dev], *[_ptr(a) for a in n_dev]))
+
+    def lusolve(self, m, kind, rhs_dev, sol_dev):
+        self._check(lib().nsp_lusolve(self._h, m, kind, _ptr(rhs_dev), _ptr(sol_dev)))
+
+    def diag(self, m):
+        d = NspDiag()
+        self._check(lib().nsp_diag(self._h, m, ctypes.byref(d)))
+        return d
+
+    def grid(self, m=0):
+        NR = self.params[m].NR
+        r, rdr = np.zeros(NR), np.zeros(NR)
+        self._check(lib().nsp_grid(self._h, m, _dp(r), _dp(rdr)))
+        return r, rdr
+
+    def sync(self):
+        self._check(lib().nsp_sync(self._h))

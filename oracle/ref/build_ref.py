@@ -1,0 +1,131 @@
+"""Build recipe for the reference nsPipe-CUDA binary (the end-to-end oracle).
+
+TEST INFRASTRUCTURE.  The reference is configured only by #defines in
+Main_Code/src/head.h (head.h:16-61), so every configuration is a separate
+build.  This script
+
+  stage()            copies Main_Code/src from the read-only reference checkout
+                     into oracle/_ref/src (git-ignored; it travels with the
+                     working tree so the GPU host can compile it there),
+  build(cfg, mode)   copies oracle/_ref/src into oracle/_ref/<cfg>/<mode>/,
+                     rewrites the parameter #defines of head.h, and compiles
+                     every reference source except main.cu together with
+                     oracle/ref/ref_driver.cu (nvcc, sm_103a, -lcufft -lcublas),
+                     wrapping nonlinear() at link time to count calls,
+  run(cfg, mode, ..) runs it in oracle/_ref/<cfg>/<mode>/run/ on given u?_s.bin.
+
+No reference source is modified other than the #define values; nothing is
+copied into the tracked tree.
+"""
+import os
+import re
+import shutil
+import subprocess
+import sys
+from concurrent.futures import ThreadPoolExecutor
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE = os.path.dirname(HERE)
+REF_OUT = os.path.join(ORACLE, "_ref")
+REF_SRC_DEFAULT = "/root/reference/Main_Code/src"
+ARCH = "-gencode=arch=compute_103a,code=sm_103a"
+
+# name -> (NR, NT, NZ, LZ expression, Re, dt in code units)
+CONFIGS = {
+    "s1": (24, 8, 9, "(1.0*PI2)", 1000.0, 0.01),
+    "s2": (32, 16, 17, "(2.0*PI2)", 3000.0, 0.005),
+    "c0": (48, 32, 65, "(2.0*PI2)", 2000.0, 0.01),
+    "c1": (96, 128, 257, "(2.5*PI2)", 5300.0, 0.004),
+    "c4b": (64, 48, 129, "(2.0*PI2)", 2700.0, 0.006),
+    "c4c": (96, 96, 193, "(2.0*PI2)", 3500.0, 0.006),
+}
+
+
+def stage(src=REF_SRC_DEFAULT):
+    """Copy the reference sources next to the build outputs (once, where the reference exists)."""
+    dst = os.path.join(REF_OUT, "src")
+    if not os.path.isdir(src):
+        if os.path.isdir(dst):
+            return dst
+        raise FileNotFoundError("reference sources not found: %s" % src)
+    os.makedirs(dst, exist_ok=True)
+    for f in os.listdir(src):
+        shutil.copy2(os.path.join(src, f), os.path.join(dst, f))
+        os.chmod(os.path.join(dst, f), 0o644)
+    return dst
+
+
+def _patch_header(text, NR, NT, NZ, LZ, Re, dt, nsteps):
+    def sub(name, value):
+        nonlocal text
+        pat = re.compile(r"^#define\s+%s\b.*$" % re.escape(name), re.M)
+        assert pat.search(text), name
+        text = pat.sub("#define %s %s" % (name, value), text, count=1)
+
+    sub("NR", NR)
+    sub("NT", NT)
+    sub("NZ", NZ)
+    sub("LZ", LZ)
+    sub("Re", "(%r)" % float(Re))
+    sub("restart", 1)
+    for k in ("dt_frc", "dt_qcr", "dt_mnp"):
+        sub(k, "1e30")
+    sub("dt", repr(float(dt)))
+    sub("nsteps", nsteps)
+    return text
+
+
+def build(cfg, mode="trace", nsteps=None, jobs=8):
+    """Compile oracle/_ref/<cfg>/<mode>/Pipe.  mode 'trace' builds nsteps=1."""
+    NR, NT, NZ, LZ, Re, dt = CONFIGS[cfg]
+    if mode == "trace":
+        nsteps = 1
+    assert nsteps is not None
+    src = stage()
+    out = os.path.join(REF_OUT, cfg, "%s%s" % (mode, "" if mode == "trace" else nsteps))
+    os.makedirs(out, exist_ok=True)
+    exe = os.path.join(out, "Pipe")
+    if os.path.exists(exe):
+        return exe
+    for f in os.listdir(src):
+        shutil.copy2(os.path.join(src, f), os.path.join(out, f))
+    with open(os.path.join(out, "head.h")) as fh:
+        hdr = fh.read()
+    with open(os.path.join(out, "head.h"), "w") as fh:
+        fh.write(_patch_header(hdr, NR, NT, NZ, LZ, Re, dt, nsteps))
+    shutil.copy2(os.path.join(HERE, "ref_driver.cu"), os.path.join(out, "ref_driver.cu"))
+    units = sorted(f for f in os.listdir(out) if f.endswith(".cu") and f != "main.cu")
+
+    def cc(u):
+        subprocess.run(["nvcc", "-O3", ARCH, "-I", out, "-c", os.path.join(out, u), "-o",
+                        os.path.join(out, u[:-3] + ".o")], check=True)
+
+    with ThreadPoolExecutor(jobs) as ex:
+        list(ex.map(cc, units))
+    objs = [os.path.join(out, u[:-3] + ".o") for u in units]
+    subprocess.run(["nvcc", ARCH, "-o", exe] + objs + ["-Xlinker", "--wrap=_Z9nonlinear6vfieldS_",
+                                                        "-lcufft", "-lcublas"], check=True)
+    return exe
+
+
+def run(cfg, mode, fields_dir, nsteps, snaps=None, nsteps_build=None):
+    """Run the reference on u?_s.bin from fields_dir; returns the run directory."""
+    exe = build(cfg, mode, nsteps=nsteps_build if mode != "trace" else None)
+    rundir = os.path.join(os.path.dirname(exe), "run")
+    os.makedirs(rundir, exist_ok=True)
+    for c in "rtz":
+        shutil.copy2(os.path.join(fields_dir, "u%s_s.bin" % c), os.path.join(rundir, "u%s_s.bin" % c))
+    args = [exe, mode, str(nsteps)] + ([",".join(str(s) for s in snaps)] if snaps else [])
+    p = subprocess.run(args, cwd=rundir, capture_output=True, text=True)
+    with open(os.path.join(rundir, "stdout.txt"), "w") as fh:
+        fh.write(p.stdout + p.stderr)
+    if p.returncode != 0:
+        raise RuntimeError("reference run failed (%d): %s" % (p.returncode, (p.stdout + p.stderr)[-2000:]))
+    return rundir
+
+
+if __name__ == "__main__":
+    if sys.argv[1] == "stage":
+        print(stage())
+    elif sys.argv[1] == "build":
+        print(build(sys.argv[2], sys.argv[3], int(sys.argv[4]) if len(sys.argv) > 4 else None))

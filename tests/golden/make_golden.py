@@ -1,0 +1,99 @@
+"""Generate the golden fixtures in tests/golden/ from the reference nsPipe-CUDA build.
+
+Run on a GPU host (the reference is CUDA-only):
+
+    python tests/golden/make_golden.py OUTDIR [cfg ...]
+
+For each configuration it writes seeded restart files (u?_s.bin), builds the
+reference with that configuration's #defines (oracle/ref/build_ref.py), runs it
+in 'trace' mode (one integrate() call per step, corrector iteration counts
+recorded) and reduces the snapshots it writes to fixtures:
+
+  * small configurations (s1, s2): full spectral fields at selected steps;
+  * c0 (NR=48, 32x64 modes) and c1 (NR=96, 128x256 modes): the low-mode block
+    |m| <= 4, l <= 5 at every radius, the mean profile u_z(0,0,r), the per-
+    component L2 norms and 8 seeded random projections of every component
+    (a checksum of the whole field).
+
+The projections use real weights w ~ N(0,1) from SplitMix64(seed ^ 0x5bd1e995):
+p = sum_h w_h u_h over the flattened field.
+"""
+import json
+import os
+import shutil
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, os.path.join(ROOT, "nspipe-gpu_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle", "ref"))
+from nspipe_gb300.initfield import PI2, SplitMix64, read_state, seeded_field, write_state  # noqa: E402
+import build_ref  # noqa: E402
+
+# name -> amplitude, seed, total steps, snapshot steps, full-field fixture?
+RUNS = {
+    "s1": (0.05, 11, 20, [1, 5, 20], True),
+    "s2": (0.1, 12, 20, [1, 10, 20], True),
+    "c0": (1e-3, 2000, 100, [1, 10, 50, 100], False),
+    "c1": (0.1, 5300, 100, [1, 10, 50, 100], False),
+}
+N_PROJ = 8
+
+
+def projection_weights(size, seed):
+    rng = np.random.default_rng(seed ^ 0x5BD1E995)
+    return rng.standard_normal((N_PROJ, size))
+
+
+def reduce_field(u, seed):
+    NR, NT, NZ = u[0].shape
+    m_slots = [0, 1, 2, 3, 4, NT - 4, NT - 3, NT - 2, NT - 1]
+    w = projection_weights(u[0].size, seed)
+    out = {
+        "low": np.stack([a[:, m_slots, :6] for a in u]),
+        "mean": u[2][:, 0, 0].copy(),
+        "norm": np.array([np.linalg.norm(a) for a in u]),
+        "proj": np.stack([w @ a.reshape(-1) for a in u]),
+    }
+    return out
+
+
+def main():
+    outdir = os.path.abspath(sys.argv[1])
+    cfgs = sys.argv[2:] or ["s1", "s2", "c0"]
+    os.makedirs(outdir, exist_ok=True)
+    summary = {}
+    for cfg in cfgs:
+        amp, seed, nsteps, snaps, full = RUNS[cfg]
+        NR, NT, NZ, LZexpr, Re, dt = build_ref.CONFIGS[cfg]
+        LZ = eval(LZexpr.replace("PI2", repr(PI2)))
+        u0 = seeded_field(NR, NT, NZ, LZ, amp, seed)
+        init_dir = os.path.join(tempfile.mkdtemp(prefix="nsp_golden_"), cfg + "_init")
+        write_state(u0, init_dir)
+        rundir = build_ref.run(cfg, "trace", init_dir, nsteps, snaps=snaps)
+        iters = np.loadtxt(os.path.join(rundir, "iters.txt"), dtype=np.int64).reshape(-1, 2)[:, 1]
+        fx = {"iters": iters, "init": np.stack(u0) if full else np.zeros(0),
+              "params": np.array([NR, NT, NZ, Re, dt, LZ, amp, seed, nsteps], dtype=np.float64)}
+        for s in snaps:
+            u = read_state(rundir, (NR, NT, NZ), suffix="_%d" % s)
+            if full:
+                fx["u_%d" % s] = np.stack(u)
+            else:
+                for k, v in reduce_field(u, seed).items():
+                    fx["%s_%d" % (k, s)] = v
+        # drop the raw snapshots of every step
+        for f in os.listdir(rundir):
+            if f.endswith(".bin") and not f.endswith("_s.bin"):
+                os.remove(os.path.join(rundir, f))
+        np.savez_compressed(os.path.join(outdir, "ref_%s.npz" % cfg), **fx)
+        summary[cfg] = {"iters": iters.tolist(), "snaps": snaps}
+        shutil.rmtree(init_dir)
+        print(cfg, "iters", iters.tolist(), flush=True)
+    with open(os.path.join(outdir, "golden_summary.json"), "w") as fh:
+        json.dump(summary, fh)
+
+
+if __name__ == "__main__":
+    main()
