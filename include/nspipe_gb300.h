@@ -127,6 +127,19 @@ int nsp_grid(nsp_ctx* ctx, int member, double* r, double* rdr);
 /* Number of kernel launches issued by the last nsp_step call (all graph nodes run). */
 long long nsp_kernel_launches(nsp_ctx* ctx);
 
+/* Makes the context launch its work on `stream` (a cudaStream_t of the context's
+ * device); NULL restores the context's own stream.  The reference runs on the
+ * legacy default stream (no equivalent entry point). */
+int nsp_set_stream(nsp_ctx* ctx, void* stream);
+
+/* Measurement hook (no reference counterpart): average device time in ms of one
+ * launch of each kernel of the step, over `reps` back-to-back launches timed with
+ * CUDA events on the context's stream, every member in corrector mode:
+ * ms_out[0] theta-inverse transforms, [1] z transforms + nonlinear product,
+ * [2] theta-forward transforms, [3] linear predictor/corrector pass, [4] convergence
+ * bookkeeping.  The state is preserved; the corrector iterate buffers are overwritten. */
+int nsp_profile_stages(nsp_ctx* ctx, int reps, double* ms_out);
+
 /* Waits for all work of the context. */
 int nsp_sync(nsp_ctx* ctx);
 

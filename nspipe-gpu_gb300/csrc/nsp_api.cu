@@ -48,6 +48,7 @@ struct nsp_ctx {
   std::vector<int> grp, slot, internal;  // per user member
   std::vector<Group> groups;
   cudaStream_t st = nullptr;
+  cudaStream_t own_st = nullptr;
   Ctl hctl{};
   Ctl* dctl = nullptr;
   int parity = 0;  // host mirror of ctl.parity
@@ -255,7 +256,8 @@ int nsp_create(const nsp_params* members, int n_members, int precision, int devi
     base += (int)g.users.size();
   }
   CK(cudaSetDevice(device));
-  CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&c->own_st, cudaStreamNonBlocking));
+  c->st = c->own_st;
   // Member buffers.
   base = 0;
   for (auto& g : c->groups) {
@@ -560,6 +562,60 @@ int nsp_grid(nsp_ctx* c, int m, double* r, double* rdr) {
 
 long long nsp_kernel_launches(nsp_ctx* c) { return c ? c->launches_last : 0; }
 
+int nsp_set_stream(nsp_ctx* c, void* stream) {
+  if (!c) return NSP_ERR_ARG;
+  CK(cudaStreamSynchronize(c->st));
+  c->st = stream ? (cudaStream_t)stream : c->own_st;
+  return NSP_OK;
+}
+
+int nsp_profile_stages(nsp_ctx* c, int reps, double* ms_out) {
+  if (!c || !ms_out || reps < 1) return NSP_ERR_ARG;
+  if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_profile_stages before nsp_setup");
+  CK(cudaSetDevice(c->device));
+  const int nm = c->nmem;
+  std::vector<int> ones(nm, 1), zeros(nm, 0);
+  CK(cudaMemcpyAsync(c->hctl.phase, ones.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, c->st));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  const bool mixed = c->precision == NSP_MIXED;
+  for (int stage = 0; stage < 5; stage++) {
+    auto launch = [&]() {
+      if (stage < 3) {
+        for (auto& g : c->groups) launch_nonlinear(g.tb, g.bf, c->dctl, mixed, nullptr, nullptr, c->st, 1 << stage);
+      } else if (stage == 3) {
+        for (auto& g : c->groups) launch_linear(g.tb, g.bf, c->dctl, c->st);
+      } else {
+        launch_converge(c->dctl, nm, 0ull, 0, c->st);
+      }
+    };
+    launch();  // warm-up
+    CK(cudaEventRecord(e0, c->st));
+    for (int r = 0; r < reps; r++) {
+      launch();
+      if (stage == 4) CK(cudaMemcpyAsync(c->hctl.phase, ones.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, c->st));
+    }
+    CK(cudaEventRecord(e1, c->st));
+    CK(cudaGetLastError());
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    ms_out[stage] = ms / reps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  // Restore the step-boundary control state.
+  CK(cudaMemcpyAsync(c->hctl.phase, zeros.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemsetAsync(c->hctl.num, 0, sizeof(unsigned long long) * nm, c->st));
+  CK(cudaMemsetAsync(c->hctl.den, 0, sizeof(unsigned long long) * nm, c->st));
+  CK(cudaMemsetAsync(c->hctl.status, 0, sizeof(int) * nm, c->st));
+  CK(cudaMemsetAsync(c->hctl.ite, 0, sizeof(int) * nm, c->st));
+  CK(cudaMemcpyAsync(&c->dctl->parity, &c->parity, sizeof(int), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return NSP_OK;
+}
+
 int nsp_sync(nsp_ctx* c) {
   if (!c) return NSP_ERR_ARG;
   CK(cudaStreamSynchronize(c->st));
@@ -574,7 +630,7 @@ int nsp_destroy(nsp_ctx* c) {
   if (c->st) cudaStreamSynchronize(c->st);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   for (void* p : c->allocs) cudaFree(p);
-  if (c->st) cudaStreamDestroy(c->st);
+  if (c->own_st) cudaStreamDestroy(c->own_st);
   delete c;
   return NSP_OK;
 }

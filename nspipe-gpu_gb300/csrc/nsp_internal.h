@@ -77,8 +77,9 @@ struct Ctl {
 
 // Kernel launchers (nsp_transform.cu, nsp_linear.cu).
 // Nonlinear term of every active member of a group (or of one explicit field).
+// mask selects the kernels: bit 0 theta-inverse, bit 1 z stage, bit 2 theta-forward.
 void launch_nonlinear(const Tables& tb, const Bufs& bf, Ctl* dctl, bool mixed, const double2* src_override,
-                      double2* dst_override, cudaStream_t st);
+                      double2* dst_override, cudaStream_t st, int mask = 7);
 void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st);
 void launch_converge(Ctl* dctl, int nmem, unsigned long long cond_handle, int use_cond, cudaStream_t st);
 void launch_lusolve(const Tables& tb, int kind, const double2* rhs, double2* sol, cudaStream_t st);

@@ -331,6 +331,12 @@ void build_operators(const nsp_params& p, HostOps& o) {
     cd iDet = {Det.x / D1, -Det.y / D1};
     cd col3[4] = {cd{a14.y, -a14.x}, cd{a24.y, -a24.x}, cd{-a34.x, -a34.y}, cd{0.0, 1.0}};
     for (int j = 0; j < 4; j++) col3[j] = cmul(col3[j], iDet);
+    // Mode (0,0): p_h is constant, so grad p_h and the determinant vanish in exact
+    // arithmetic and the reference inverts rounding noise (0/0 = NaN when the noise
+    // is exactly zero).  The exact correction only changes u_r(0,0), which modeZZ
+    // sets to zero, so no correction is applied to this mode.
+    if (m00)
+      for (int j = 0; j < 4; j++) col3[j] = cd{0.0, 0.0};
     for (int c = 0; c < 3; c++)
       for (int i = 0; i < NR; i++) {
         cd v1 = cmul(col3[c], uh[c][i]), v2 = cmul(col3[3], uP[c][i]);

@@ -252,13 +252,14 @@ static int theta_chunk(int NZ) {
 }
 
 template <typename T>
-static void launch_nl_t(const Tables& tb, const Bufs& bf, Ctl* dctl, const double2* src, double2* dst, cudaStream_t st) {
+static void launch_nl_t(const Tables& tb, const Bufs& bf, Ctl* dctl, const double2* src, double2* dst, cudaStream_t st,
+                        int mask) {
   int LC = theta_chunk(tb.NZ);
   int nchunk = (tb.NZ + LC - 1) / LC;
   int nm = src ? 1 : tb.nmem;
   dim3 g1(nchunk, tb.NR, nm);
   size_t sm1 = sizeof(cpx<T>) * tb.NTP * LC;
-  nl_theta_inv<T><<<g1, 256, sm1, st>>>(tb, bf, dctl, src, LC);
+  if (mask & 1) nl_theta_inv<T><<<g1, 256, sm1, st>>>(tb, bf, dctl, src, LC);
   // z stage: two theta rows per block when it fits, else one.
   int rpb = 2, thr = 256;
   auto fits = [&](int r, int t) { return max_butterflies(tb.pz, 6 * r) <= MAXR * t; };
@@ -268,9 +269,11 @@ static void launch_nl_t(const Tables& tb, const Bufs& bf, Ctl* dctl, const doubl
   }
   size_t sm2 = sizeof(cpx<T>) * 6 * rpb * tb.NZR;
   dim3 g2((tb.NTP + rpb - 1) / rpb, tb.NR, nm);
-  if (rpb == 2) nl_z<T, 2><<<g2, thr, sm2, st>>>(tb, bf, dctl, src ? 1 : 0);
-  else nl_z<T, 1><<<g2, thr, sm2, st>>>(tb, bf, dctl, src ? 1 : 0);
-  nl_theta_fwd<T><<<g1, 256, sm1, st>>>(tb, bf, dctl, src, dst, LC);
+  if (mask & 2) {
+    if (rpb == 2) nl_z<T, 2><<<g2, thr, sm2, st>>>(tb, bf, dctl, src ? 1 : 0);
+    else nl_z<T, 1><<<g2, thr, sm2, st>>>(tb, bf, dctl, src ? 1 : 0);
+  }
+  if (mask & 4) nl_theta_fwd<T><<<g1, 256, sm1, st>>>(tb, bf, dctl, src, dst, LC);
 }
 
 int kernels_per_nonlinear() { return 3; }
@@ -287,9 +290,9 @@ void configure_transform_kernels() {
 }
 
 void launch_nonlinear(const Tables& tb, const Bufs& bf, Ctl* dctl, bool mixed, const double2* src, double2* dst,
-                      cudaStream_t st) {
-  if (mixed) launch_nl_t<float>(tb, bf, dctl, src, dst, st);
-  else launch_nl_t<double>(tb, bf, dctl, src, dst, st);
+                      cudaStream_t st, int mask) {
+  if (mixed) launch_nl_t<float>(tb, bf, dctl, src, dst, st, mask);
+  else launch_nl_t<double>(tb, bf, dctl, src, dst, st, mask);
 }
 
 }  // namespace nsp

@@ -23,7 +23,7 @@ EXPORTS = [
     "nsp_default_params", "nsp_create", "nsp_setup", "nsp_load_state", "nsp_save_state",
     "nsp_set_state_host", "nsp_get_state_host", "nsp_set_state_device", "nsp_get_state_device",
     "nsp_step", "nsp_nonlinear", "nsp_lusolve", "nsp_diag", "nsp_grid", "nsp_kernel_launches",
-    "nsp_sync", "nsp_last_error", "nsp_destroy",
+    "nsp_sync", "nsp_last_error", "nsp_destroy", "nsp_set_stream", "nsp_profile_stages",
 ]
 
 
@@ -78,6 +78,8 @@ def lib():
         L.nsp_kernel_launches.argtypes = [vp]
         L.nsp_kernel_launches.restype = ctypes.c_longlong
         L.nsp_sync.argtypes = [vp]
+        L.nsp_set_stream.argtypes = [vp, vp]
+        L.nsp_profile_stages.argtypes = [vp, ip, dp]
         L.nsp_last_error.argtypes = [vp]
         L.nsp_last_error.restype = ctypes.c_char_p
         L.nsp_destroy.argtypes = [vp]
@@ -205,6 +207,16 @@ class Stepper:
         r, rdr = np.zeros(NR), np.zeros(NR)
         self._check(lib().nsp_grid(self._h, m, _dp(r), _dp(rdr)))
         return r, rdr
+
+    def set_stream(self, stream_handle):
+        """Launch on a given cudaStream_t (int handle, e.g. torch.cuda.Stream().cuda_stream)."""
+        self._check(lib().nsp_set_stream(self._h, stream_handle or None))
+
+    def profile_stages(self, reps=5):
+        """Average ms per launch: [theta-inverse, z stage, theta-forward, linear pass, converge]."""
+        ms = np.zeros(5)
+        self._check(lib().nsp_profile_stages(self._h, reps, _dp(ms)))
+        return ms
 
     def sync(self):
         self._check(lib().nsp_sync(self._h))

@@ -62,7 +62,7 @@ def reduce_field(u, seed):
 
 def main():
     outdir = os.path.abspath(sys.argv[1])
-    cfgs = sys.argv[2:] or ["s1", "s2", "c0"]
+    cfgs = sys.argv[2:] or ["s2", "c0", "c1"]
     os.makedirs(outdir, exist_ok=True)
     summary = {}
     for cfg in cfgs:
