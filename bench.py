@@ -265,6 +265,16 @@ def main():
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                 "algorithmic_bytes_per_launch": alg_bytes[dom], "launch_ms": stage_ms[dom],
                 "stage_ms": dict(zip(names, [float(x) for x in stage_ms]))}
+    # The linear pass is FP64-bound on GB300 (FP64 ~1/60 of FP32): its FP64 roofline,
+    # with ~390 algorithmic FP64 flops per grid point and pass (stencils, four banded
+    # solves, influence-matrix correction, +/- changes of variable, convergence).
+    if names[dom] == "linear_k":
+        fp64_peak = st.fp64_peak_tflops()
+        fl = 390.0 * S * M
+        ach = fl / (stage_ms[dom] * 1e-3) / 1e12
+        roofline["compute_bound"] = "fp64"
+        roofline["fp64"] = {"achieved_tflops": ach, "peak_tflops": fp64_peak, "frac": ach / fp64_peak,
+                            "algorithmic_flops_per_launch": fl, "peak_source": "measured live (nsp_measure_fp64_peak)"}
 
     # Plain FP64 form on the same ensemble (the metric's comparison).
     fp64 = None

@@ -140,6 +140,11 @@ int nsp_set_stream(nsp_ctx* ctx, void* stream);
  * bookkeeping.  The state is preserved; the corrector iterate buffers are overwritten. */
 int nsp_profile_stages(nsp_ctx* ctx, int reps, double* ms_out);
 
+/* Measurement hook (no reference counterpart): FP64 multiply-add throughput of the
+ * context's device in TFLOP/s (8 independent chains per thread, no memory traffic,
+ * best of 3 timed launches), the denominator of the FP64 roofline. */
+int nsp_measure_fp64_peak(nsp_ctx* ctx, double* tflops);
+
 /* Waits for all work of the context. */
 int nsp_sync(nsp_ctx* ctx);
 

@@ -9,6 +9,8 @@
 // are corrector iterations of the members that have not converged (the others
 // skip their blocks), so each member keeps the reference's own iteration count
 // (integrate, mod_integrate.cu:112-130) without any device-to-host round trip.
+#include <sys/stat.h>
+
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -24,6 +26,7 @@
 namespace nsp {
 void configure_transform_kernels();
 void configure_linear_kernels();
+bool transform_supported(int NTP, int NZR);
 }  // namespace nsp
 
 using namespace nsp;
@@ -57,6 +60,7 @@ struct nsp_ctx {
   bool use_graph = false;
   long long launches_last = 0;
   double2* scratch = nullptr;  // 2 x 3 x Smax, for nsp_nonlinear
+  float2* scratch32 = nullptr; // 3 x Smax, FP32 input of nsp_nonlinear in the mixed form
   long long Smax = 0;
   std::vector<void*> allocs;
   std::string err;
@@ -147,10 +151,7 @@ int check_params(nsp_ctx* c, const nsp_params& p, int idx) {
   int NTP = 3 * p.NT / 2, NZR = 3 * (p.NZ - 1);
   if (!smooth23(NTP) || !smooth23(NZR))
     return fail(c, NSP_ERR_ARG, "member %d: transform lengths %d x %d must be of the form 2^a 3^b", idx, NTP, NZR);
-  FftPlan pt, pz;
-  make_plan(NTP, pt);
-  make_plan(NZR, pz);
-  if (max_butterflies(pt, 16) > 4 * 256 || max_butterflies(pz, 6) > 4 * 512)
+  if (!transform_supported(NTP, NZR))
     return fail(c, NSP_ERR_ARG, "member %d: transform lengths %d x %d exceed the block size limits", idx, NTP, NZR);
   if (!(p.Re > 0) || !(p.dt > 0) || !(p.LT > 0) || !(p.LZ > 0) || p.maxit < 1 || !(p.tol >= 0) || !(p.Qdes == p.Qdes))
     return fail(c, NSP_ERR_ARG, "member %d: Re, dt, LT, LZ must be > 0, maxit >= 1, tol >= 0", idx);
@@ -166,6 +167,108 @@ int check_member(nsp_ctx* c, int m) {
 double2* state_ptr(nsp_ctx* c, int m, int comp) {
   Group& g = c->groups[c->grp[m]];
   return g.bf.U[c->parity] + ((size_t)c->slot[m] * 3 + comp) * g.tb.S;
+}
+
+// ------------------------------------------------------------ autotuner
+// Picks the block shape of the linear pass per member group by timing every
+// candidate on the context's own buffers (all members in corrector mode, CUDA
+// events, best of 3 after a warm-up).  Choices are cached in a flat JSON object
+// {"NRxNTxNZ:mM:pP": variant, ...} at $NSP_TUNE_CACHE (default
+// $HOME/.cache/nspipe_gb300/tune.json); NSP_AUTOTUNE=0 keeps the defaults.
+std::string tune_path() {
+  const char* p = getenv("NSP_TUNE_CACHE");
+  if (p && *p) return p;
+  const char* h = getenv("HOME");
+  return std::string(h ? h : "/tmp") + "/.cache/nspipe_gb300/tune.json";
+}
+
+std::map<std::string, int> tune_load() {
+  std::map<std::string, int> m;
+  FILE* f = fopen(tune_path().c_str(), "r");
+  if (!f) return m;
+  char key[256];
+  int v;
+  int ch;
+  while ((ch = fgetc(f)) != EOF) {
+    if (ch != '"') continue;
+    if (fscanf(f, "%255[^\"]\": %d", key, &v) == 2) m[key] = v;
+  }
+  fclose(f);
+  return m;
+}
+
+void tune_store(const std::map<std::string, int>& m) {
+  std::string path = tune_path();
+  for (size_t pos = path.find('/', 1); pos != std::string::npos; pos = path.find('/', pos + 1))
+    mkdir(path.substr(0, pos).c_str(), 0755);  // existing directories are fine
+  FILE* f = fopen(path.c_str(), "w");
+  if (!f) return;
+  fprintf(f, "{");
+  size_t k = 0;
+  for (auto& kv : m) fprintf(f, "%s\"%s\": %d", k++ ? ", " : "", kv.first.c_str(), kv.second);
+  fprintf(f, "}\n");
+  fclose(f);
+}
+
+int reset_control(nsp_ctx* c) {
+  const int nm = c->nmem;
+  std::vector<int> zeros(nm, 0);
+  CK(cudaMemcpyAsync(c->hctl.phase, zeros.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemsetAsync(c->hctl.num, 0, sizeof(unsigned long long) * nm, c->st));
+  CK(cudaMemsetAsync(c->hctl.den, 0, sizeof(unsigned long long) * nm, c->st));
+  CK(cudaMemsetAsync(c->hctl.status, 0, sizeof(int) * nm, c->st));
+  CK(cudaMemsetAsync(c->hctl.ite, 0, sizeof(int) * nm, c->st));
+  CK(cudaMemcpyAsync(&c->dctl->parity, &c->parity, sizeof(int), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return NSP_OK;
+}
+
+int autotune(nsp_ctx* c) {
+  for (auto& g : c->groups) g.tb.lin_variant = linear_default_variant(g.tb.NR);
+  const char* ev = getenv("NSP_AUTOTUNE");
+  if (ev && ev[0] == '0') return NSP_OK;
+  std::map<std::string, int> cache = tune_load();
+  bool dirty = false;
+  const int nm = c->nmem;
+  std::vector<int> ones(nm, 1);
+  CK(cudaMemcpyAsync(c->hctl.phase, ones.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, c->st));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  for (auto& g : c->groups) {
+    char key[128];
+    snprintf(key, sizeof key, "%dx%dx%d:m%d:p%d", g.tb.NR, g.tb.NT, g.tb.NZ, g.tb.nmem, c->precision);
+    auto it = cache.find(key);
+    if (it != cache.end() && linear_variant_fits(it->second, g.tb.NR)) {
+      g.tb.lin_variant = it->second;
+      continue;
+    }
+    float best = 1e30f;
+    for (int v = 0; v < LIN_VARIANTS; v++) {
+      if (!linear_variant_fits(v, g.tb.NR)) continue;
+      Tables tv = g.tb;
+      tv.lin_variant = v;
+      launch_linear(tv, g.bf, c->dctl, c->st);
+      float t = 1e30f;
+      for (int r = 0; r < 3; r++) {
+        CK(cudaEventRecord(e0, c->st));
+        launch_linear(tv, g.bf, c->dctl, c->st);
+        CK(cudaEventRecord(e1, c->st));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        t = std::min(t, ms);
+      }
+      CK(cudaGetLastError());
+      if (t < best) { best = t; g.tb.lin_variant = v; }
+    }
+    cache[key] = g.tb.lin_variant;
+    dirty = true;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (dirty) tune_store(cache);
+  return reset_control(c);
 }
 
 int build_graph(nsp_ctx* c) {
@@ -286,9 +389,19 @@ int nsp_create(const nsp_params* members, int n_members, int precision, int devi
     CK(cudaMemset(g.bf.U[0], 0, S3 * sizeof(double2)));
     CK(cudaMemset(g.bf.U[1], 0, S3 * sizeof(double2)));
     CK(cudaMemset(g.bf.H, 0, hsz));
+    CK(cudaMemset(g.bf.N, 0, S3 * sizeof(double2)));
+    CK(cudaMemset(g.bf.RHSW, 0, S3 * sizeof(double2)));
+    g.bf.U32[0] = g.bf.U32[1] = nullptr;
+    if (precision == NSP_MIXED) {
+      if ((rc = dalloc(c, &g.bf.U32[0], S3 * sizeof(float2)))) return rc;
+      if ((rc = dalloc(c, &g.bf.U32[1], S3 * sizeof(float2)))) return rc;
+      CK(cudaMemset(g.bf.U32[0], 0, S3 * sizeof(float2)));
+      CK(cudaMemset(g.bf.U32[1], 0, S3 * sizeof(float2)));
+    }
     if (tb.S > c->Smax) c->Smax = tb.S;
   }
   if (int rc = dalloc(c, &c->scratch, sizeof(double2) * 6 * (size_t)c->Smax)) return rc;
+  if (int rc = dalloc(c, &c->scratch32, sizeof(float2) * 3 * (size_t)c->Smax)) return rc;
   // Control block.
   Ctl& h = c->hctl;
   h.parity = 0; h.step = 0; h.any = 0; h.nmem = n_members;
@@ -325,12 +438,17 @@ int nsp_setup(nsp_ctx* c) {
     Tables& tb = g.tb;
     const nsp_params& p = g.p;
     HostOps& o = g.ops;
-    std::vector<double> rinv(p.NR), rinv2(p.NR);
+    std::vector<double> rinv(p.NR), rinv2(p.NR), Luc(o.Lu.size());
+    std::vector<float> D32(o.D.size());
     for (int i = 0; i < p.NR; i++) { rinv[i] = 1.0 / o.r[i]; rinv2[i] = 1.0 / (o.r[i] * o.r[i]); }
+    const double c_ex = (1.0 - p.d_im) / p.Re;
+    for (size_t e = 0; e < o.Lu.size(); e++) Luc[e] = c_ex * o.Lu[e];
+    for (size_t e = 0; e < o.D.size(); e++) D32[e] = (float)o.D[e];
     int rc;
     if ((rc = upload(c, &tb.r, o.r)) || (rc = upload(c, &tb.rinv, rinv)) || (rc = upload(c, &tb.rinv2, rinv2)) ||
         (rc = upload(c, &tb.rdr, o.rdr)) || (rc = upload(c, &tb.uc, o.uc)) || (rc = upload(c, &tb.D, o.D)) ||
-        (rc = upload(c, &tb.Lu, o.Lu)) || (rc = upload(c, &tb.fac, o.fac)) || (rc = upload(c, &tb.V, o.V)))
+        (rc = upload(c, &tb.D32, D32)) || (rc = upload(c, &tb.Lu, o.Lu)) || (rc = upload(c, &tb.Luc, Luc)) ||
+        (rc = upload(c, &tb.fac, o.fac)) || (rc = upload(c, &tb.V, o.V)))
       return rc;
     std::vector<double2> wt = twiddles(tb.NTP), wz = twiddles(tb.NZR);
     if ((rc = upload(c, &tb.tw_t, wt)) || (rc = upload(c, &tb.tw_z, wz)) || (rc = upload(c, &tb.tw_t32, to_f32(wt))) ||
@@ -355,8 +473,16 @@ int nsp_setup(nsp_ctx* c) {
   configure_transform_kernels();
   configure_linear_kernels();
   CK(cudaGetLastError());
-  int rc = build_graph(c);
-  if (rc) return rc;
+  if (int rc = autotune(c)) return rc;
+  // NSP_GRAPH=0 selects the host-driven corrector loop (same kernels, one D2H flag
+  // read per iteration) so that profilers can see every kernel launch.
+  const char* ge = getenv("NSP_GRAPH");
+  if (ge && ge[0] == '0') {
+    c->use_graph = false;
+  } else {
+    int rc = build_graph(c);
+    if (rc) return rc;
+  }
   c->setup_done = true;
   return NSP_OK;
 }
@@ -448,6 +574,11 @@ int nsp_step(nsp_ctx* c, int nsteps, int* iters_out) {
   long long launches = 0;
   const long long per_iter = 4LL * (long long)c->groups.size() + 1;
   std::vector<int> hist;
+  // Mixed form: the transforms read an FP32 mirror of the state, kept current by the
+  // linear pass; refresh it here because the state may have been set from outside.
+  if (c->precision == NSP_MIXED && nsteps > 0)
+    for (auto& g : c->groups)
+      launch_to_f32(g.bf.U[c->parity], g.bf.U32[c->parity], (long long)g.tb.nmem * 3 * g.tb.S, c->st);
   for (int done = 0; done < nsteps;) {
     int chunk = std::min(cap, nsteps - done);
     CK(cudaMemsetAsync(&c->dctl->step, 0, sizeof(int), c->st));
@@ -502,7 +633,9 @@ int nsp_nonlinear(nsp_ctx* c, int m, const void* ur, const void* ut, const void*
   const void* src[3] = {ur, ut, uz};
   void* dst[3] = {nr, nt, nz};
   for (int k = 0; k < 3; k++) CK(cudaMemcpyAsync(in + k * S, src[k], bytes, cudaMemcpyDeviceToDevice, c->st));
-  launch_nonlinear(g.tb, g.bf, c->dctl, c->precision == NSP_MIXED, in, out, c->st);
+  const bool mixed = c->precision == NSP_MIXED;
+  if (mixed) launch_to_f32(in, c->scratch32, 3LL * (long long)S, c->st);
+  launch_nonlinear(g.tb, g.bf, c->dctl, mixed, in, out, c->st, 7, mixed ? c->scratch32 : nullptr);
   CK(cudaGetLastError());
   for (int k = 0; k < 3; k++) CK(cudaMemcpyAsync(dst[k], out + k * S, bytes, cudaMemcpyDeviceToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
@@ -574,7 +707,7 @@ int nsp_profile_stages(nsp_ctx* c, int reps, double* ms_out) {
   if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_profile_stages before nsp_setup");
   CK(cudaSetDevice(c->device));
   const int nm = c->nmem;
-  std::vector<int> ones(nm, 1), zeros(nm, 0);
+  std::vector<int> ones(nm, 1);
   CK(cudaMemcpyAsync(c->hctl.phase, ones.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, c->st));
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
@@ -606,13 +739,36 @@ int nsp_profile_stages(nsp_ctx* c, int reps, double* ms_out) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   // Restore the step-boundary control state.
-  CK(cudaMemcpyAsync(c->hctl.phase, zeros.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, c->st));
-  CK(cudaMemsetAsync(c->hctl.num, 0, sizeof(unsigned long long) * nm, c->st));
-  CK(cudaMemsetAsync(c->hctl.den, 0, sizeof(unsigned long long) * nm, c->st));
-  CK(cudaMemsetAsync(c->hctl.status, 0, sizeof(int) * nm, c->st));
-  CK(cudaMemsetAsync(c->hctl.ite, 0, sizeof(int) * nm, c->st));
-  CK(cudaMemcpyAsync(&c->dctl->parity, &c->parity, sizeof(int), cudaMemcpyHostToDevice, c->st));
+  return reset_control(c);
+}
+
+int nsp_measure_fp64_peak(nsp_ctx* c, double* tflops) {
+  if (!c || !tflops) return NSP_ERR_ARG;
+  CK(cudaSetDevice(c->device));
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, c->device));
+  const int blocks = prop.multiProcessorCount * 8, threads = 256, iters = 4096;
+  double* out = nullptr;
+  CK(cudaMallocAsync(&out, sizeof(double) * blocks * threads, c->st));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  for (int w = 0; w < 2; w++) launch_fp64_peak(out, blocks, threads, iters, c->st);
+  float best = 1e30f;
+  for (int r = 0; r < 3; r++) {
+    CK(cudaEventRecord(e0, c->st));
+    launch_fp64_peak(out, blocks, threads, iters, c->st);
+    CK(cudaEventRecord(e1, c->st));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    best = std::min(best, ms);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  CK(cudaFreeAsync(out, c->st));
   CK(cudaStreamSynchronize(c->st));
+  *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (best * 1e-3) / 1e12;
   return NSP_OK;
 }
 

@@ -116,6 +116,76 @@ __device__ void fft_batch(cpx<T>* buf, const FftPlan& pl, int nb, int es, int bs
   }
 }
 
+// ---------------------------------------------------------------------------
+// Compile-time variant: length N, batch NB, element stride ES, batch stride BS
+// and block size NTH are template parameters, so every index division is by a
+// constant (multiply-shift) and the register staging holds exactly the rounds
+// each stage needs.
+__host__ __device__ constexpr int ct_radix(int n, int s) {
+  int k = 0;
+  while (n % 4 == 0) { if (k == s) return 4; n /= 4; k++; }
+  while (n % 2 == 0) { if (k == s) return 2; n /= 2; k++; }
+  while (n % 3 == 0) { if (k == s) return 3; n /= 3; k++; }
+  return 0;
+}
+__host__ __device__ constexpr int ct_nstages(int n) {
+  int k = 0;
+  while (ct_radix(n, k)) k++;
+  return k;
+}
+
+template <typename T, int SIGN, int N, int NB, int ES, int BS, bool TFAST, int NTH, int P, int NS>
+__device__ __forceinline__ void fft_stage_ct(cpx<T>* buf, const typename vec2<T>::type* __restrict__ tw) {
+  constexpr int NBF = N / P;
+  constexpr int TOTAL = NB * NBF;
+  constexpr int R = (TOTAL + NTH - 1) / NTH;
+  constexpr int TSTR = N / (NS * P);
+  cpx<T> v[R][P];
+#pragma unroll
+  for (int rr = 0; rr < R; rr++) {
+    int b = threadIdx.x + rr * NTH;
+    if (TOTAL % NTH == 0 || b < TOTAL) {
+      int t = TFAST ? b % NB : b / NBF;
+      int j = TFAST ? b / NB : b - t * NBF;
+      const cpx<T>* x = buf + t * BS;
+#pragma unroll
+      for (int q = 0; q < P; q++) v[rr][q] = x[(j + q * NBF) * ES];
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int rr = 0; rr < R; rr++) {
+    int b = threadIdx.x + rr * NTH;
+    if (TOTAL % NTH == 0 || b < TOTAL) {
+      int t = TFAST ? b % NB : b / NBF;
+      int j = TFAST ? b / NB : b - t * NBF;
+      int k = (NS == 1) ? 0 : j % NS;
+      if (NS > 1) {
+#pragma unroll
+        for (int q = 1; q < P; q++) {
+          typename vec2<T>::type w = __ldg(tw + q * k * TSTR);
+          v[rr][q] = cmulv(v[rr][q], mk<T>(w.x, SIGN > 0 ? -w.y : w.y));
+        }
+      }
+      dft<T, SIGN, P>(v[rr]);
+      cpx<T>* x = buf + t * BS;
+      int base = (NS == 1) ? j * P : (j / NS) * NS * P + k;
+#pragma unroll
+      for (int q = 0; q < P; q++) x[(base + q * NS) * ES] = v[rr][q];
+    }
+  }
+  __syncthreads();
+}
+
+template <typename T, int SIGN, int N, int NB, int ES, int BS, bool TFAST, int NTH, int S = 0, int NS = 1>
+__device__ __forceinline__ void fft_ct(cpx<T>* buf, const typename vec2<T>::type* __restrict__ tw) {
+  if constexpr (S < ct_nstages(N)) {
+    constexpr int P = ct_radix(N, S);
+    fft_stage_ct<T, SIGN, N, NB, ES, BS, TFAST, NTH, P, NS>(buf, tw);
+    fft_ct<T, SIGN, N, NB, ES, BS, TFAST, NTH, S + 1, NS * P>(buf, tw);
+  }
+}
+
 // Largest butterfly count of any stage (for the MAXR bound check on the host).
 inline int max_butterflies(const FftPlan& pl, int nb) {
   int mx = 0;

@@ -37,7 +37,9 @@ struct Tables {
   const double* rdr;
   const double* uc;
   const double* D;     // [2][NR][7]: first derivative, parity tables (0 even-extended, 1 odd)
+  const float* D32;    // the same in FP32 (mixed-form transforms)
   const double* Lu;    // [2][NR][7]: radial Laplacian rows with identity wall row
+  const double* Luc;   // (1-d_im)/Re * Lu (explicit part of the Laplacian, pre-scaled)
   const double* fac;   // [4][NR][7][NTNZ]: banded LU factors of u+, u-, u_z, p
   const double2* V;    // [3][NR][NTNZ]: influence-matrix correction profiles (+, -, z)
   const double2* tw_t; // [NTP] exp(-2 pi i e/NTP), FP64
@@ -45,11 +47,17 @@ struct Tables {
   const float2* tw_t32;
   const float2* tw_z32;
   FftPlan pt, pz;
+  int lin_variant;     // block shape of the linear pass (autotuned at setup)
 };
+
+constexpr int LIN_VARIANTS = 4;
+int linear_default_variant(int NR);
+bool linear_variant_fits(int v, int NR);
 
 // Batched per-group member buffers.
 struct Bufs {
   double2* U[2];       // [nmem][3][S]: state / corrector iterate, roles swap each step (parity)
+  float2* U32[2];      // mixed form only: FP32 copies of U[0], U[1] read by the transforms
   double2* RHSW;       // [nmem][3][S]: N(u^n) in +/- form (rhsw of mod_integrate.cu:100-107)
   double2* N;          // [nmem][3][S]: nonlinear term output
   void* G;             // [nmem][9][NR][NTP][NZ] complex T: theta-inverse of u, dr u, i m u / r
@@ -78,11 +86,15 @@ struct Ctl {
 // Kernel launchers (nsp_transform.cu, nsp_linear.cu).
 // Nonlinear term of every active member of a group (or of one explicit field).
 // mask selects the kernels: bit 0 theta-inverse, bit 1 z stage, bit 2 theta-forward.
+// src32_override: FP32 copy of src_override (mixed form, explicit-field calls only).
 void launch_nonlinear(const Tables& tb, const Bufs& bf, Ctl* dctl, bool mixed, const double2* src_override,
-                      double2* dst_override, cudaStream_t st, int mask = 7);
+                      double2* dst_override, cudaStream_t st, int mask = 7, const float2* src32_override = nullptr);
 void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st);
 void launch_converge(Ctl* dctl, int nmem, unsigned long long cond_handle, int use_cond, cudaStream_t st);
 void launch_lusolve(const Tables& tb, int kind, const double2* rhs, double2* sol, cudaStream_t st);
+void launch_fp64_peak(double* out, int blocks, int threads, int iters, cudaStream_t st);
+// FP32 copy of nmem x 3 x S complex values (the mixed form's transform input).
+void launch_to_f32(const double2* src, float2* dst, long long n, cudaStream_t st);
 int kernels_per_nonlinear();
 
 // Host-side operator construction (nsp_setup.cpp).

@@ -22,7 +22,6 @@
 
 namespace nsp {
 
-constexpr int LIN_THREADS = 256;
 
 __device__ __forceinline__ double2 c2(double x, double y) { return make_double2(x, y); }
 
@@ -54,8 +53,8 @@ __device__ __forceinline__ void solve_line(double2* X, int ld, const double* __r
   }
 }
 
-template <int LM>
-__global__ void __launch_bounds__(LIN_THREADS) linear_k(Tables tb, Bufs bf, Ctl* ctl) {
+template <int LM, int NTH>
+__global__ void __launch_bounds__(NTH) linear_k(Tables tb, Bufs bf, Ctl* ctl) {
   const int mloc = blockIdx.y, gm = tb.mem0 + mloc;
   const int ph = ctl->phase[gm];
   if (ph < 0) return;
@@ -70,10 +69,11 @@ __global__ void __launch_bounds__(LIN_THREADS) linear_k(Tables tb, Bufs bf, Ctl*
   double2* R = sm + 3 * LN;  // [3][NR][LM] right-hand side, then the new velocity
   double2* P = W;            // divergence / pressure (W is dead by then)
   __shared__ double2 dvs[LM];
-  __shared__ double wnum[LIN_THREADS / 32], wden[LIN_THREADS / 32];
+  __shared__ double wnum[NTH / 32], wden[NTH / 32];
   __shared__ int bad;
   const double2* Un = bf.U[par] + (size_t)mloc * 3 * S;
   double2* Ui = bf.U[par ^ 1] + (size_t)mloc * 3 * S;
+  float2* Ui32 = bf.U32[par ^ 1] ? bf.U32[par ^ 1] + (size_t)mloc * 3 * S : nullptr;  // mixed form
   const double2* Nn = bf.N + (size_t)mloc * 3 * S;
   double2* Rw = bf.RHSW + (size_t)mloc * 3 * S;
   const int tid = threadIdx.x, nth = blockDim.x;
@@ -114,13 +114,15 @@ __global__ void __launch_bounds__(LIN_THREADS) linear_k(Tables tb, Bufs bf, Ctl*
     int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
     double ir2 = tb.rinv2[i];
     double base = -kz * kz - kt * kt * ir2;
+    double pm = -ir2 - 2.0 * kt * ir2, mm2 = -ir2 + 2.0 * kt * ir2;
     double2 out[3];
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       int tab = abs((abs(m) % 2) - (c < 2 ? 1 : 0));
-      const double* Lr = tb.Lu + tab * STEN * NR + STEN * i + i0;
+      const double* Lr = tb.Luc + tab * STEN * NR + STEN * i + i0;  // (1-d_im)/Re * L_r
       const double2* Wc = W + c * LN + mm;
-      double sx = 0.0, sy = 0.0;
+      double2 rr = R[c * LN + p];
+      double sx = rr.x, sy = rr.y;
       for (int j = 0; j < len; j++) {
         double de = __ldg(Lr + j);
         double2 a = Wc[(left + j) * LM];
@@ -128,17 +130,11 @@ __global__ void __launch_bounds__(LIN_THREADS) linear_k(Tables tb, Bufs bf, Ctl*
         sy += de * a.y;
       }
       double2 aux = Wc[i * LM];
-      double de = base;
-      if (c == 0) de += -ir2 - 2.0 * kt * ir2;
-      else if (c == 1) de += -ir2 + 2.0 * kt * ir2;
-      sx += de * aux.x;
-      sy += de * aux.y;
-      sx *= tb.c_ex;
-      sy *= tb.c_ex;
-      sx += tb.inv_dt * aux.x;
-      sy += tb.inv_dt * aux.y;
-      double2 rr = R[c * LN + p];
-      out[c] = c2(rr.x + sx, rr.y + sy);
+      double de = base + (c == 0 ? pm : (c == 1 ? mm2 : 0.0));
+      double dd = tb.c_ex * de + tb.inv_dt;  // diagonal: (1-d_im)/Re (-k_z^2 - m^2/r^2 ...) + 1/dt
+      sx += dd * aux.x;
+      sy += dd * aux.y;
+      out[c] = c2(sx, sy);
     }
     R[p] = c2(0.5 * (out[0].x + out[1].x), 0.5 * (out[0].y + out[1].y));
     R[LN + p] = c2(0.5 * (out[0].y - out[1].y), -0.5 * (out[0].x - out[1].x));
@@ -250,18 +246,15 @@ __global__ void __launch_bounds__(LIN_THREADS) linear_k(Tables tb, Bufs bf, Ctl*
   for (int p = tid; p < LN; p += nth) {
     int i = p / LM, mm = p - i * LM, k = k0 + mm;
     if (k >= NTNZ) continue;
-    double2 a = R[p], b = R[LN + p], uz = R[2 * LN + p];
-    double2 ur = c2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y));
-    double2 ut = c2(0.5 * (a.y - b.y), -0.5 * (a.x - b.x));
-    double2 up = c2(ur.x - ut.y, ur.y + ut.x), um = c2(ur.x + ut.y, ur.y - ut.x);
+    double2 up = R[p], um = R[LN + p], uz = R[2 * LN + p];
     double2 dv = dvs[mm];
     size_t hv = (size_t)i * NTNZ + k;
     double2 v0 = tb.V[hv], v1 = tb.V[S + hv], v2 = tb.V[2 * S + hv];
     up.x += dv.x * v0.x - dv.y * v0.y; up.y += dv.x * v0.y + dv.y * v0.x;
     um.x += dv.x * v1.x - dv.y * v1.y; um.y += dv.x * v1.y + dv.y * v1.x;
     uz.x += dv.x * v2.x - dv.y * v2.y; uz.y += dv.x * v2.y + dv.y * v2.x;
-    ur = c2(0.5 * (up.x + um.x), 0.5 * (up.y + um.y));
-    ut = c2(0.5 * (up.y - um.y), -0.5 * (up.x - um.x));
+    double2 ur = c2(0.5 * (up.x + um.x), 0.5 * (up.y + um.y));
+    double2 ut = c2(0.5 * (up.y - um.y), -0.5 * (up.x - um.x));
     if (k == 0) { ur = c2(0, 0); ut.y = 0.0; uz.y = 0.0; }
     R[p] = ur; R[LN + p] = ut; R[2 * LN + p] = uz;
   }
@@ -295,6 +288,7 @@ __global__ void __launch_bounds__(LIN_THREADS) linear_k(Tables tb, Bufs bf, Ctl*
       }
       nonfin |= !(isfinite(v.x) && isfinite(v.y));
       Ui[c * S + h] = v;
+      if (Ui32) Ui32[c * S + h] = make_float2((float)v.x, (float)v.y);
     }
     lnum = fmax(lnum, n1);
     lden = fmax(lden, d1);
@@ -367,6 +361,26 @@ __global__ void converge_k(Ctl* ctl, cudaGraphConditionalHandle h, int use_cond)
   }
 }
 
+// FP64 throughput probe: 8 independent multiply-add chains per thread, no memory
+// traffic; the measured denominator of the FP64 roofline.
+__global__ void fp64_peak_k(double* out, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int k = 0; k < 8; k++) x[k] = threadIdx.x + k;
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int k = 0; k < 8; k++) x[k] = x[k] * a + b;
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; k++) s += x[k];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+void launch_fp64_peak(double* out, int blocks, int threads, int iters, cudaStream_t st) {
+  fp64_peak_k<<<blocks, threads, 0, st>>>(out, iters, 0.999999, 1e-7);
+}
+
 __global__ void lusolve_k(Tables tb, int kind, const double2* rhs, double2* sol) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= tb.NTNZ) return;
@@ -374,21 +388,36 @@ __global__ void lusolve_k(Tables tb, int kind, const double2* rhs, double2* sol)
   solve_line(sol + k, tb.NTNZ, tb.fac + (size_t)kind * tb.NR * NFAC * tb.NTNZ + k, tb.NTNZ, tb.NR);
 }
 
-static int lin_modes(int NR) { return NR <= 64 ? 16 : 8; }
+// Block shapes of the linear pass (modes per block, threads): the candidates of the
+// setup-time autotuner.  Shared memory per block is 6 radial lines per mode.
+struct LinShape { int LM, NTH; };
+static const LinShape kLinShapes[LIN_VARIANTS] = {{16, 256}, {8, 128}, {8, 256}, {4, 128}};
 
-size_t linear_smem(int NR) { return sizeof(double2) * 6 * (size_t)NR * lin_modes(NR); }
+int linear_default_variant(int NR) { return NR <= 64 ? 0 : 2; }
+
+bool linear_variant_fits(int v, int NR) {
+  return v >= 0 && v < LIN_VARIANTS && sizeof(double2) * 6 * (size_t)NR * kLinShapes[v].LM <= 200 * 1024;
+}
 
 void configure_linear_kernels() {
-  cudaFuncSetAttribute(linear_k<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  cudaFuncSetAttribute(linear_k<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  const int big = 200 * 1024;
+  cudaFuncSetAttribute(linear_k<16, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(linear_k<8, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(linear_k<8, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(linear_k<4, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
 }
 
 void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st) {
-  int LM = lin_modes(tb.NR);
-  dim3 grid((tb.NTNZ + LM - 1) / LM, tb.nmem);
-  size_t smem = linear_smem(tb.NR);
-  if (LM == 16) linear_k<16><<<grid, LIN_THREADS, smem, st>>>(tb, bf, dctl);
-  else linear_k<8><<<grid, LIN_THREADS, smem, st>>>(tb, bf, dctl);
+  int v = linear_variant_fits(tb.lin_variant, tb.NR) ? tb.lin_variant : linear_default_variant(tb.NR);
+  const LinShape s = kLinShapes[v];
+  dim3 grid((tb.NTNZ + s.LM - 1) / s.LM, tb.nmem);
+  size_t smem = sizeof(double2) * 6 * (size_t)tb.NR * s.LM;
+  switch (v) {
+    case 0: linear_k<16, 256><<<grid, 256, smem, st>>>(tb, bf, dctl); break;
+    case 1: linear_k<8, 128><<<grid, 128, smem, st>>>(tb, bf, dctl); break;
+    case 2: linear_k<8, 256><<<grid, 256, smem, st>>>(tb, bf, dctl); break;
+    default: linear_k<4, 128><<<grid, 128, smem, st>>>(tb, bf, dctl); break;
+  }
 }
 
 void launch_converge(Ctl* dctl, int nmem, unsigned long long cond_handle, int use_cond, cudaStream_t st) {

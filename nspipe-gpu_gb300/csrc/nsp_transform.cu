@@ -6,22 +6,25 @@
 // padBackward x3 (:195-214) and pressGrad (mod_radialFD.cu:100-111).  Three
 // kernels per evaluation:
 //
-//   nl_theta_inv  per (member, level, l-chunk): builds the padded theta columns
-//                 of u, d_r u (7-point stencil over levels, parity tables) and
-//                 i m u / r straight from the spectral state and runs the
-//                 length-NTP inverse FFTs -> G[f][level][theta_j][l] (9 fields);
+//   nl_theta_inv  per (member, level, 16 (field, l) columns): builds the padded
+//                 theta columns of u, d_r u (7-point stencil over levels, parity
+//                 tables) and i m u / r straight from the spectral state and runs
+//                 the length-NTP inverse FFTs -> G[f][level][theta_j][l] (9 fields);
 //   nl_z          per (member, level, theta rows): forms the 12 Hermitian z
 //                 spectra (d_z u = i k_z times the u columns of G), packs them
 //                 two real fields per complex length-NZR inverse FFT, evaluates
 //                 -(u.grad)u pointwise, packs the 3 products into complex forward
 //                 FFTs and unpacks the half spectra l < NZ-1 -> H;
-//   nl_theta_fwd  per (member, level, l-chunk): length-NTP forward FFTs of H,
-//                 scale by 1/(NTP*NZR), keep the retained modes (theta Nyquist and
-//                 l = NZ-1 zeroed) and apply the wall-shear forcing to N_z(0,0).
+//   nl_theta_fwd  per (member, level, 16 (component, l) columns): length-NTP
+//                 forward FFTs of H, scale by 1/(NTP*NZR), keep the retained modes
+//                 (theta Nyquist and l = NZ-1 zeroed) and apply the wall-shear
+//                 forcing to N_z(0,0).
 //
-// T = double gives the plain FP64 form; T = float the mixed form (the state,
-// d_r u and i m u / r are formed in FP64 and rounded to FP32 on load; N is
-// written back in FP64).
+// T = double gives the plain FP64 form; T = float the mixed form (the state is
+// rounded to FP32 on load, the stencils and products run in FP32, N is written
+// back in FP64).  Transform lengths used by the supported configurations are
+// compile-time template arguments (all index arithmetic by constants); other
+// 2^a 3^b lengths use the run-time FFT.
 #include <cstdio>
 
 #include "nsp_fft.cuh"
@@ -29,7 +32,10 @@
 
 namespace nsp {
 
-constexpr int MAXR = 4;
+constexpr int MAXR = 4;   // register rounds of the run-time FFT
+constexpr int LC = 16;    // theta columns per block
+constexpr int TTH = 256;  // threads of the theta kernels
+constexpr int ZTH = 256;  // threads of the z kernel
 
 template <typename T> __device__ __forceinline__ const typename vec2<T>::type* tw_t(const Tables& tb);
 template <> __device__ __forceinline__ const double2* tw_t<double>(const Tables& tb) { return tb.tw_t; }
@@ -49,83 +55,127 @@ __device__ __forceinline__ const double2* member_source(const Tables& tb, const 
   return bf.U[which] + (size_t)mloc * 3 * tb.S;
 }
 
-// ---------------------------------------------------------------- theta inverse
+// Transform input in the working precision: the FP64 state, or its FP32 mirror.
+template <typename T> struct StateIn;
+template <> struct StateIn<double> {
+  const double2* p;
+  __device__ __forceinline__ cpx<double> ld(size_t h) const { double2 a = p[h]; return mk<double>(a.x, a.y); }
+};
+template <> struct StateIn<float> {
+  const float2* p;
+  __device__ __forceinline__ cpx<float> ld(size_t h) const { float2 a = __ldg(p + h); return mk<float>(a.x, a.y); }
+};
+template <typename T> __device__ __forceinline__ const T* dtab(const Tables& tb);
+template <> __device__ __forceinline__ const double* dtab<double>(const Tables& tb) { return tb.D; }
+template <> __device__ __forceinline__ const float* dtab<float>(const Tables& tb) { return tb.D32; }
+
 template <typename T>
-__global__ void __launch_bounds__(256) nl_theta_inv(Tables tb, Bufs bf, const Ctl* ctl, const double2* src_override,
-                                                    int LC) {
-  const int mloc = blockIdx.z, i = blockIdx.y, l0 = blockIdx.x * LC;
+__device__ __forceinline__ StateIn<T> member_input(const Tables& tb, const Bufs& bf, const Ctl* ctl, int mloc,
+                                                  const double2* src, const float2* src32) {
+  StateIn<T> s;
+  int which = 0;
+  if (!src) {
+    int ph = ctl->phase[tb.mem0 + mloc];
+    which = (ph == 0) ? ctl->parity : (ctl->parity ^ 1);
+  }
+  if constexpr (sizeof(T) == 8) s.p = src ? src : bf.U[which] + (size_t)mloc * 3 * tb.S;
+  else s.p = src ? src32 : bf.U32[which] + (size_t)mloc * 3 * tb.S;
+  return s;
+}
+
+template <typename T, int NTPC>
+__device__ __forceinline__ void theta_fft(cpx<T>* buf, const Tables& tb, int sign) {
+  if constexpr (NTPC > 0) {
+    if (sign > 0) fft_ct<T, +1, NTPC, LC, LC, 1, true, TTH>(buf, tw_t<T>(tb));
+    else fft_ct<T, -1, NTPC, LC, LC, 1, true, TTH>(buf, tw_t<T>(tb));
+  } else {
+    if (sign > 0) fft_batch<T, +1, MAXR, true>(buf, tb.pt, LC, LC, 1, tw_t<T>(tb));
+    else fft_batch<T, -1, MAXR, true>(buf, tb.pt, LC, LC, 1, tw_t<T>(tb));
+  }
+}
+
+// ---------------------------------------------------------------- theta inverse
+template <typename T, int NTPC>
+__global__ void __launch_bounds__(TTH) nl_theta_inv(Tables tb, Bufs bf, const Ctl* ctl, const double2* src_override,
+                                                    const float2* src32_override) {
+  const int mloc = blockIdx.z, i = blockIdx.y, c0 = blockIdx.x * LC;
   bool skip;
-  const double2* U = member_source(tb, bf, ctl, mloc, src_override, skip);
+  member_source(tb, bf, ctl, mloc, src_override, skip);
   if (skip) return;
+  const StateIn<T> U = member_input<T>(tb, bf, ctl, mloc, src_override, src32_override);
   extern __shared__ __align__(16) unsigned char smraw[];
   cpx<T>* buf = reinterpret_cast<cpx<T>*>(smraw);
-  const int NR = tb.NR, NT = tb.NT, NZ = tb.NZ, NTP = tb.NTP, NTNZ = tb.NTNZ;
+  __shared__ int colf[LC], coll[LC];
+  const int NR = tb.NR, NT = tb.NT, NZ = tb.NZ, NTNZ = tb.NTNZ;
+  const int NTP = NTPC > 0 ? NTPC : tb.NTP;
   const long long S = tb.S;
-  const int lc_n = min(LC, NZ - l0);
+  if (threadIdx.x < LC) {
+    int c = c0 + threadIdx.x;
+    colf[threadIdx.x] = c < 9 * NZ ? c / NZ : -1;
+    coll[threadIdx.x] = c % NZ;
+  }
+  __syncthreads();
   const int left = max(0, i - IW), right = min(i + IW, NR - 1);
   const int len = right + 1 - left, i0 = i + IW - right;
-  const double rinv = tb.rinv[i];
-  cpx<T>* G = reinterpret_cast<cpx<T>*>(bf.G) + (size_t)mloc * 9 * NR * NTP * NZ;
-  for (int f = 0; f < 9; f++) {
-    const int c = f % 3;
-    const double2* Uc = U + c * S;
-    for (int idx = threadIdx.x; idx < NTP * LC; idx += blockDim.x) {
-      int p = idx / LC, lc = idx - p * LC;
-      double2 v = make_double2(0.0, 0.0);
-      int it = (p < NT / 2) ? p : (p >= NT ? p - NT / 2 : -1);
-      if (lc < lc_n && it >= 0) {
-        int l = l0 + lc;
-        size_t col = (size_t)it * NZ + l;
-        if (f < 3) {
-          v = Uc[(size_t)i * NTNZ + col];
-        } else if (f < 6) {  // derivr_k, mod_radialFD.cu:10-30 (flag 1 for u_r, u_theta; 0 for u_z)
-          int m = it < NT / 2 ? it : it - NT;
-          int flag = (c < 2) ? 1 : 0;
-          int tab = abs((abs(m) % 2) - flag);
-          const double* Dr = tb.D + tab * STEN * NR + STEN * i + i0;
-          double sx = 0.0, sy = 0.0;
-          for (int j = 0; j < len; j++) {
-            double de = __ldg(Dr + j);
-            double2 a = Uc[(size_t)(left + j) * NTNZ + col];
-            sx += de * a.x;
-            sy += de * a.y;
-          }
-          v = make_double2(sx, sy);
-        } else {  // derivt_k, mod_deriv.cu:10-21
-          int m = it < NT / 2 ? it : it - NT;
-          double kt = tb.kts * (double)m;
-          double2 a = Uc[(size_t)i * NTNZ + col];
-          v = make_double2(-kt * a.y * rinv, kt * a.x * rinv);
+  const T rinv = (T)tb.rinv[i];
+  const T ktsT = (T)tb.kts;
+  for (int idx = threadIdx.x; idx < NTP * LC; idx += TTH) {
+    int p = idx / LC, lc = idx % LC;
+    int f = colf[lc];
+    int it = (p < NT / 2) ? p : (p >= NT ? p - NT / 2 : -1);
+    cpx<T> v = mk<T>(0, 0);
+    if (f >= 0 && it >= 0) {
+      int comp = f % 3;
+      size_t col = (size_t)comp * S + (size_t)it * NZ + coll[lc];
+      if (f < 3) {
+        v = U.ld((size_t)i * NTNZ + col);
+      } else if (f < 6) {  // derivr_k, mod_radialFD.cu:10-30 (flag 1 for u_r, u_theta; 0 for u_z)
+        int m = it < NT / 2 ? it : it - NT;
+        int tab = abs((abs(m) % 2) - (comp < 2 ? 1 : 0));
+        const T* Dr = dtab<T>(tb) + tab * STEN * NR + STEN * i + i0;
+        T sx = 0, sy = 0;
+        for (int j = 0; j < len; j++) {
+          T de = __ldg(Dr + j);
+          cpx<T> a = U.ld((size_t)(left + j) * NTNZ + col);
+          sx += de * a.x;
+          sy += de * a.y;
         }
+        v = mk<T>(sx, sy);
+      } else {  // derivt_k, mod_deriv.cu:10-21
+        int m = it < NT / 2 ? it : it - NT;
+        T kt = (sizeof(T) == 8) ? (T)(tb.kts * (double)m) : (T)m * ktsT;
+        cpx<T> a = U.ld((size_t)i * NTNZ + col);
+        v = mk<T>(-kt * a.y * rinv, kt * a.x * rinv);
       }
-      buf[idx] = mk<T>((T)v.x, (T)v.y);
     }
-    __syncthreads();
-    fft_batch<T, +1, MAXR, true>(buf, tb.pt, LC, LC, 1, tw_t<T>(tb));
-    cpx<T>* Gf = G + ((size_t)f * NR + i) * NTP * NZ;
-    for (int idx = threadIdx.x; idx < NTP * LC; idx += blockDim.x) {
-      int p = idx / LC, lc = idx - p * LC;
-      if (lc < lc_n) Gf[(size_t)p * NZ + l0 + lc] = buf[idx];
-    }
-    __syncthreads();
+    buf[idx] = v;
+  }
+  __syncthreads();
+  theta_fft<T, NTPC>(buf, tb, +1);
+  cpx<T>* G = reinterpret_cast<cpx<T>*>(bf.G) + (size_t)mloc * 9 * NR * NTP * NZ;
+  for (int idx = threadIdx.x; idx < NTP * LC; idx += TTH) {
+    int p = idx / LC, lc = idx % LC;
+    int f = colf[lc];
+    if (f >= 0) G[(((size_t)f * NR + i) * NTP + p) * NZ + coll[lc]] = buf[idx];
   }
 }
 
 // ---------------------------------------------------------------- z stage
 // Field order of the 12 physical arrays: u_r,u_t,u_z, dr u_r,dr u_t,dr u_z,
 // dt u_r,dt u_t,dt u_z, dz u_r,dz u_t,dz u_z.  Pair t holds fields (2t, 2t+1).
-template <typename T, int RPB>
-__global__ void __launch_bounds__(512) nl_z(Tables tb, Bufs bf, const Ctl* ctl, int standalone) {
+template <typename T, int NZRC, int RPB>
+__global__ void __launch_bounds__(ZTH) nl_z(Tables tb, Bufs bf, const Ctl* ctl, int standalone) {
   const int mloc = blockIdx.z, i = blockIdx.y, j0 = blockIdx.x * RPB;
   if (!standalone && ctl->phase[tb.mem0 + mloc] < 0) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   cpx<T>* Z = reinterpret_cast<cpx<T>*>(smraw);  // [RPB*6][NZR]
-  const int NR = tb.NR, NZ = tb.NZ, NTP = tb.NTP, NZR = tb.NZR;
+  const int NR = tb.NR, NZ = tb.NZ, NTP = tb.NTP;
+  const int NZR = NZRC > 0 ? NZRC : tb.NZR;
   const cpx<T>* G = reinterpret_cast<const cpx<T>*>(bf.G) + (size_t)mloc * 9 * NR * NTP * NZ;
   cpx<T>* H = reinterpret_cast<cpx<T>*>(bf.H) + (size_t)mloc * 3 * NR * NTP * NZ;
   const T kzs = (T)tb.kzs;
   // Hermitian-extended spectra, two real fields per complex transform.
-  for (int idx = threadIdx.x; idx < RPB * 6 * NZR; idx += blockDim.x) {
+  for (int idx = threadIdx.x; idx < RPB * 6 * NZR; idx += ZTH) {
     int q = idx % NZR, t = (idx / NZR) % 6, rr = idx / (6 * NZR);
     int j = j0 + rr;
     cpx<T> z = mk<T>(0, 0);
@@ -153,11 +203,12 @@ __global__ void __launch_bounds__(512) nl_z(Tables tb, Bufs bf, const Ctl* ctl, 
     Z[(size_t)(rr * 6 + t) * NZR + q] = z;
   }
   __syncthreads();
-  fft_batch<T, +1, MAXR, false>(Z, tb.pz, RPB * 6, 1, NZR, tw_z<T>(tb));
+  if constexpr (NZRC > 0) fft_ct<T, +1, NZRC, RPB * 6, 1, NZRC, false, ZTH>(Z, tw_z<T>(tb));
+  else fft_batch<T, +1, MAXR, false>(Z, tb.pz, RPB * 6, 1, NZR, tw_z<T>(tb));
   // -(u.grad)u (calcNonlinear_k), packed for the forward transforms:
   // RPB 2: slot0 = (Nr0, Nt0), slot1 = (Nr1, Nt1), slot2 = (Nz0, Nz1); RPB 1: slot0 = (Nr, Nt), slot1 = (Nz, 0).
   const T rinv = (T)tb.rinv[i];
-  for (int n = threadIdx.x; n < NZR; n += blockDim.x) {
+  for (int n = threadIdx.x; n < NZR; n += ZTH) {
     T nr[RPB], nt[RPB], nz[RPB];
 #pragma unroll
     for (int rr = 0; rr < RPB; rr++) {
@@ -180,11 +231,12 @@ __global__ void __launch_bounds__(512) nl_z(Tables tb, Bufs bf, const Ctl* ctl, 
     }
   }
   __syncthreads();
-  const int nfwd = (RPB == 2) ? 3 : 2;
-  fft_batch<T, -1, MAXR, false>(Z, tb.pz, nfwd, 1, NZR, tw_z<T>(tb));
+  constexpr int NFWD = (RPB == 2) ? 3 : 2;
+  if constexpr (NZRC > 0) fft_ct<T, -1, NZRC, NFWD, 1, NZRC, false, ZTH>(Z, tw_z<T>(tb));
+  else fft_batch<T, -1, MAXR, false>(Z, tb.pz, NFWD, 1, NZR, tw_z<T>(tb));
   // Unpack: x = a + i b  ->  A_q = (X_q + conj X_{-q})/2,  B_q = (X_q - conj X_{-q})/(2i).
   const int NQ = NZ - 1;
-  for (int idx = threadIdx.x; idx < RPB * 3 * NQ; idx += blockDim.x) {
+  for (int idx = threadIdx.x; idx < RPB * 3 * NQ; idx += ZTH) {
     int q = idx % NQ, c = (idx / NQ) % 3, rr = idx / (3 * NQ);
     int j = j0 + rr;
     if (j >= NTP) continue;
@@ -201,98 +253,166 @@ __global__ void __launch_bounds__(512) nl_z(Tables tb, Bufs bf, const Ctl* ctl, 
 }
 
 // ---------------------------------------------------------------- theta forward
-template <typename T>
-__global__ void __launch_bounds__(256) nl_theta_fwd(Tables tb, Bufs bf, const Ctl* ctl, const double2* src_override,
-                                                    double2* dst_override, int LC) {
-  const int mloc = blockIdx.z, i = blockIdx.y, l0 = blockIdx.x * LC;
+template <typename T, int NTPC>
+__global__ void __launch_bounds__(TTH) nl_theta_fwd(Tables tb, Bufs bf, const Ctl* ctl, const double2* src_override,
+                                                    double2* dst_override) {
+  const int mloc = blockIdx.z, i = blockIdx.y, c0 = blockIdx.x * LC;
   bool skip;
   const double2* U = member_source(tb, bf, ctl, mloc, src_override, skip);
   if (skip) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   cpx<T>* buf = reinterpret_cast<cpx<T>*>(smraw);
-  const int NR = tb.NR, NT = tb.NT, NZ = tb.NZ, NTP = tb.NTP, NTNZ = tb.NTNZ;
+  __shared__ int colc[LC], coll[LC];
+  const int NR = tb.NR, NT = tb.NT, NZ = tb.NZ, NTNZ = tb.NTNZ;
+  const int NTP = NTPC > 0 ? NTPC : tb.NTP;
   const long long S = tb.S;
-  const int lc_n = min(LC, NZ - l0);
+  if (threadIdx.x < LC) {
+    int c = c0 + threadIdx.x;
+    colc[threadIdx.x] = c < 3 * NZ ? c / NZ : -1;
+    coll[threadIdx.x] = c % NZ;
+  }
+  __syncthreads();
   const cpx<T>* H = reinterpret_cast<const cpx<T>*>(bf.H) + (size_t)mloc * 3 * NR * NTP * NZ;
   double2* Nout = dst_override ? dst_override : bf.N + (size_t)mloc * 3 * S;
+  for (int idx = threadIdx.x; idx < NTP * LC; idx += TTH) {
+    int p = idx / LC, lc = idx % LC;
+    int c = colc[lc], l = coll[lc];
+    buf[idx] = (c >= 0 && l < NZ - 1) ? H[(((size_t)c * NR + i) * NTP + p) * NZ + l] : mk<T>(0, 0);
+  }
+  __syncthreads();
+  theta_fft<T, NTPC>(buf, tb, -1);
   // Wall derivative of u_z(0,0) for the mean forcing (pressGrad_k).
   double dwall = 0.0;
-  if (l0 == 0) {
+  if (c0 <= 2 * NZ && c0 + LC > 2 * NZ) {
     const double* Dw = tb.D + STEN * (NR - 1) + IW;
     for (int j = 0; j <= IW; j++) dwall += Dw[j] * U[2 * S + (size_t)(NR - 1 - IW + j) * NTNZ].x;
   }
-  for (int c = 0; c < 3; c++) {
-    const cpx<T>* Hc = H + ((size_t)c * NR + i) * NTP * NZ;
-    for (int idx = threadIdx.x; idx < NTP * LC; idx += blockDim.x) {
-      int p = idx / LC, lc = idx - p * LC;
-      int l = l0 + lc;
-      buf[idx] = (lc < lc_n && l < NZ - 1) ? Hc[(size_t)p * NZ + l] : mk<T>(0, 0);
-    }
-    __syncthreads();
-    fft_batch<T, -1, MAXR, true>(buf, tb.pt, LC, LC, 1, tw_t<T>(tb));
-    for (int idx = threadIdx.x; idx < NT * LC; idx += blockDim.x) {
-      int it = idx / LC, lc = idx - it * LC;
-      if (lc >= lc_n) continue;
-      int l = l0 + lc;
-      int p = it < NT / 2 ? it : NTP + it - NT;
-      cpx<T> b = buf[p * LC + lc];
-      double2 v = make_double2((double)b.x * tb.inv_norm, (double)b.y * tb.inv_norm);
-      if (it == NT / 2 || l == NZ - 1) v = make_double2(0.0, 0.0);
-      if (c == 2 && it == 0 && l == 0) v.x -= tb.two_re * dwall;
-      Nout[c * S + (size_t)i * NTNZ + (size_t)it * NZ + l] = v;
-    }
-    __syncthreads();
+  const T scale = (T)tb.inv_norm;
+  for (int idx = threadIdx.x; idx < NT * LC; idx += TTH) {
+    int it = idx / LC, lc = idx % LC;
+    int c = colc[lc], l = coll[lc];
+    if (c < 0) continue;
+    int p = it < NT / 2 ? it : NTP + it - NT;
+    cpx<T> b = buf[p * LC + lc];
+    double2 v;
+    if (sizeof(T) == 8) v = make_double2((double)b.x * tb.inv_norm, (double)b.y * tb.inv_norm);
+    else v = make_double2((double)(b.x * scale), (double)(b.y * scale));
+    if (it == NT / 2 || l == NZ - 1) v = make_double2(0.0, 0.0);
+    if (c == 2 && it == 0 && l == 0) v.x -= tb.two_re * dwall;
+    Nout[c * S + (size_t)i * NTNZ + (size_t)it * NZ + l] = v;
   }
 }
 
 // ---------------------------------------------------------------- launcher
-static int theta_chunk(int NZ) {
-  int nchunk = (NZ + 15) / 16;
-  return (NZ + nchunk - 1) / nchunk;
+template <typename T, int NTPC>
+static void launch_theta(const Tables& tb, const Bufs& bf, Ctl* dctl, const double2* src, const float2* src32,
+                         double2* dst, cudaStream_t st, int mask, int nm) {
+  size_t sm = sizeof(cpx<T>) * tb.NTP * LC;
+  if (mask & 1) {
+    dim3 g((9 * tb.NZ + LC - 1) / LC, tb.NR, nm);
+    nl_theta_inv<T, NTPC><<<g, TTH, sm, st>>>(tb, bf, dctl, src, src32);
+  }
+  if (mask & 4) {
+    dim3 g((3 * tb.NZ + LC - 1) / LC, tb.NR, nm);
+    nl_theta_fwd<T, NTPC><<<g, TTH, sm, st>>>(tb, bf, dctl, src, dst);
+  }
 }
 
+template <typename T, int NZRC, int RPB>
+static void launch_z(const Tables& tb, const Bufs& bf, Ctl* dctl, bool standalone, cudaStream_t st, int nm) {
+  size_t sm = sizeof(cpx<T>) * 6 * RPB * tb.NZR;
+  dim3 g((tb.NTP + RPB - 1) / RPB, tb.NR, nm);
+  nl_z<T, NZRC, RPB><<<g, ZTH, sm, st>>>(tb, bf, dctl, standalone ? 1 : 0);
+}
+
+#define NSP_NTP_LIST(X) X(12) X(24) X(48) X(72) X(96) X(144) X(192)
+#define NSP_NZR_LIST(X) X(24, 2) X(48, 2) X(96, 2) X(192, 2) X(384, 2) X(576, 1) X(768, 1)
+
 template <typename T>
-static void launch_nl_t(const Tables& tb, const Bufs& bf, Ctl* dctl, const double2* src, double2* dst, cudaStream_t st,
-                        int mask) {
-  int LC = theta_chunk(tb.NZ);
-  int nchunk = (tb.NZ + LC - 1) / LC;
+static void launch_nl_t(const Tables& tb, const Bufs& bf, Ctl* dctl, const double2* src, const float2* src32,
+                        double2* dst, cudaStream_t st, int mask) {
   int nm = src ? 1 : tb.nmem;
-  dim3 g1(nchunk, tb.NR, nm);
-  size_t sm1 = sizeof(cpx<T>) * tb.NTP * LC;
-  if (mask & 1) nl_theta_inv<T><<<g1, 256, sm1, st>>>(tb, bf, dctl, src, LC);
-  // z stage: two theta rows per block when it fits, else one.
-  int rpb = 2, thr = 256;
-  auto fits = [&](int r, int t) { return max_butterflies(tb.pz, 6 * r) <= MAXR * t; };
-  if (!fits(2, 256)) {
-    if (fits(2, 512) && sizeof(cpx<T>) * 12 * tb.NZR <= 96 * 1024) thr = 512;
-    else { rpb = 1; thr = fits(1, 256) ? 256 : 512; }
+  if (mask & 1) {
+    switch (tb.NTP) {
+#define NSP_CASE_T(n) \
+  case n: launch_theta<T, n>(tb, bf, dctl, src, src32, dst, st, 1, nm); break;
+      NSP_NTP_LIST(NSP_CASE_T)
+#undef NSP_CASE_T
+      default: launch_theta<T, 0>(tb, bf, dctl, src, src32, dst, st, 1, nm);
+    }
   }
-  size_t sm2 = sizeof(cpx<T>) * 6 * rpb * tb.NZR;
-  dim3 g2((tb.NTP + rpb - 1) / rpb, tb.NR, nm);
   if (mask & 2) {
-    if (rpb == 2) nl_z<T, 2><<<g2, thr, sm2, st>>>(tb, bf, dctl, src ? 1 : 0);
-    else nl_z<T, 1><<<g2, thr, sm2, st>>>(tb, bf, dctl, src ? 1 : 0);
+    switch (tb.NZR) {
+#define NSP_CASE_Z(n, r) \
+  case n: launch_z<T, n, r>(tb, bf, dctl, src != nullptr, st, nm); break;
+      NSP_NZR_LIST(NSP_CASE_Z)
+#undef NSP_CASE_Z
+      default: launch_z<T, 0, 1>(tb, bf, dctl, src != nullptr, st, nm);
+    }
   }
-  if (mask & 4) nl_theta_fwd<T><<<g1, 256, sm1, st>>>(tb, bf, dctl, src, dst, LC);
+  if (mask & 4) {
+    switch (tb.NTP) {
+#define NSP_CASE_T(n) \
+  case n: launch_theta<T, n>(tb, bf, dctl, src, src32, dst, st, 4, nm); break;
+      NSP_NTP_LIST(NSP_CASE_T)
+#undef NSP_CASE_T
+      default: launch_theta<T, 0>(tb, bf, dctl, src, src32, dst, st, 4, nm);
+    }
+  }
 }
 
 int kernels_per_nonlinear() { return 3; }
 
+template <typename T>
+static void configure_t() {
+  const int big = 200 * 1024;
+#define NSP_CFG_T(n)                                                                            \
+  cudaFuncSetAttribute(nl_theta_inv<T, n>, cudaFuncAttributeMaxDynamicSharedMemorySize, big); \
+  cudaFuncSetAttribute(nl_theta_fwd<T, n>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  NSP_NTP_LIST(NSP_CFG_T)
+  NSP_CFG_T(0)
+#undef NSP_CFG_T
+#define NSP_CFG_Z(n, r) cudaFuncSetAttribute(nl_z<T, n, r>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  NSP_NZR_LIST(NSP_CFG_Z)
+  NSP_CFG_Z(0, 1)
+#undef NSP_CFG_Z
+}
+
 void configure_transform_kernels() {
-  cudaFuncSetAttribute(nl_z<double, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  cudaFuncSetAttribute(nl_z<double, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  cudaFuncSetAttribute(nl_z<float, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  cudaFuncSetAttribute(nl_z<float, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  cudaFuncSetAttribute(nl_theta_inv<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  cudaFuncSetAttribute(nl_theta_inv<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  cudaFuncSetAttribute(nl_theta_fwd<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-  cudaFuncSetAttribute(nl_theta_fwd<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+  configure_t<double>();
+  configure_t<float>();
+}
+
+bool transform_supported(int NTP, int NZR) {
+  bool ct_t = false, ct_z = false;
+#define NSP_HAS_T(n) ct_t |= (NTP == n);
+#define NSP_HAS_Z(n, r) ct_z |= (NZR == n);
+  NSP_NTP_LIST(NSP_HAS_T)
+  NSP_NZR_LIST(NSP_HAS_Z)
+#undef NSP_HAS_T
+#undef NSP_HAS_Z
+  FftPlan pt, pz;
+  make_plan(NTP, pt);
+  make_plan(NZR, pz);
+  return (ct_t || max_butterflies(pt, LC) <= MAXR * TTH) && (ct_z || max_butterflies(pz, 6) <= MAXR * ZTH);
 }
 
 void launch_nonlinear(const Tables& tb, const Bufs& bf, Ctl* dctl, bool mixed, const double2* src, double2* dst,
-                      cudaStream_t st, int mask) {
-  if (mixed) launch_nl_t<float>(tb, bf, dctl, src, dst, st, mask);
-  else launch_nl_t<double>(tb, bf, dctl, src, dst, st, mask);
+                      cudaStream_t st, int mask, const float2* src32) {
+  if (mixed) launch_nl_t<float>(tb, bf, dctl, src, src32, dst, st, mask);
+  else launch_nl_t<double>(tb, bf, dctl, src, nullptr, dst, st, mask);
+}
+
+__global__ void to_f32_k(const double2* __restrict__ src, float2* __restrict__ dst, long long n) {
+  for (long long h = blockIdx.x * (long long)blockDim.x + threadIdx.x; h < n; h += (long long)gridDim.x * blockDim.x) {
+    double2 a = src[h];
+    dst[h] = make_float2((float)a.x, (float)a.y);
+  }
+}
+
+void launch_to_f32(const double2* src, float2* dst, long long n, cudaStream_t st) {
+  int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
+  to_f32_k<<<blocks, 256, 0, st>>>(src, dst, n);
 }
 
 }  // namespace nsp

@@ -24,6 +24,7 @@ EXPORTS = [
     "nsp_set_state_host", "nsp_get_state_host", "nsp_set_state_device", "nsp_get_state_device",
     "nsp_step", "nsp_nonlinear", "nsp_lusolve", "nsp_diag", "nsp_grid", "nsp_kernel_launches",
     "nsp_sync", "nsp_last_error", "nsp_destroy", "nsp_set_stream", "nsp_profile_stages",
+    "nsp_measure_fp64_peak",
 ]
 
 
@@ -80,6 +81,7 @@ def lib():
         L.nsp_sync.argtypes = [vp]
         L.nsp_set_stream.argtypes = [vp, vp]
         L.nsp_profile_stages.argtypes = [vp, ip, dp]
+        L.nsp_measure_fp64_peak.argtypes = [vp, dp]
         L.nsp_last_error.argtypes = [vp]
         L.nsp_last_error.restype = ctypes.c_char_p
         L.nsp_destroy.argtypes = [vp]
@@ -217,6 +219,12 @@ class Stepper:
         ms = np.zeros(5)
         self._check(lib().nsp_profile_stages(self._h, reps, _dp(ms)))
         return ms
+
+    def fp64_peak_tflops(self):
+        """Measured FP64 multiply-add throughput of the device (TFLOP/s)."""
+        t = ctypes.c_double()
+        self._check(lib().nsp_measure_fp64_peak(self._h, ctypes.byref(t)))
+        return t.value
 
     def sync(self):
         self._check(lib().nsp_sync(self._h))
