@@ -113,6 +113,23 @@ int nsp_step(nsp_ctx* ctx, int nsteps, int* iters_out);
 int nsp_nonlinear(nsp_ctx* ctx, int member, const void* ur, const void* ut, const void* uz,
                   void* nr, void* nt, void* nz);
 
+/* The nonlinear term of one member's field, computed without allocating any device
+ * memory (no counterpart in the reference).  For callers that cannot allocate while
+ * they run: hosts whose device-memory budget is fixed after start-up, applications
+ * whose own pool allocator owns the device memory, and loops that cannot afford
+ * cudaMalloc/cudaFree, which may synchronise the device.  u3 and n3 are device
+ * arrays of 3*NR*NT*NZ complex doubles, the components (r, theta, z) back to back.
+ * The transform intermediates live in a fixed 32 MiB __device__ array that every
+ * process loading this library holds on each GPU it uses; a member whose
+ * intermediates need more (9+3 complex arrays of NR*(3NT/2)*NZ in the working
+ * precision, plus an FP32 copy of the input in the mixed form) is rejected with
+ * NSP_ERR_ARG.  The first call on a device looks up the array's device address, so
+ * make that first call before any stream capture.  The array is shared by every
+ * call: calls that overlap on the GPU (other threads, other contexts on the same
+ * device) race on it.  Nothing in it needs to start at zero.  Synchronises the
+ * context's stream. */
+int nsp_nonlinear_static(nsp_ctx* ctx, int member, const void* u3, void* n3);
+
 /* One banded solve on one member's operators (LUsolve_u flag 0/1/2 and LUsolve_p,
  * mod_linear.cu:664-679): kind 0 = u+, 1 = u-, 2 = u_z, 3 = pressure.  rhs and sol
  * are device arrays of NR*NT*NZ complex doubles (rhs is not modified). */

@@ -642,6 +642,36 @@ int nsp_nonlinear(nsp_ctx* c, int m, const void* ur, const void* ut, const void*
   return NSP_OK;
 }
 
+int nsp_nonlinear_static(nsp_ctx* c, int m, const void* u3, void* n3) {
+  if (int rc = check_member(c, m)) return rc;
+  if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_nonlinear_static before nsp_setup");
+  if (!u3 || !n3) return fail(c, NSP_ERR_ARG, "null field pointer");
+  Group& g = c->groups[c->grp[m]];
+  const bool mixed = c->precision == NSP_MIXED;
+  const size_t csz = mixed ? sizeof(float2) : sizeof(double2);
+  auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
+  const size_t gsz = up((size_t)9 * g.tb.NR * g.tb.NTP * g.tb.NZ * csz);
+  const size_t hsz = up((size_t)3 * g.tb.NR * g.tb.NTP * g.tb.NZ * csz);
+  const size_t isz = mixed ? up((size_t)3 * g.tb.S * sizeof(float2)) : 0;
+  const size_t need = gsz + hsz + isz;
+  if (need > noalloc_scratch_bytes())
+    return fail(c, NSP_ERR_ARG, "nsp_nonlinear_static: member %d needs %zu bytes of scratch, the fixed limit is %zu",
+                m, need, noalloc_scratch_bytes());
+  CK(cudaSetDevice(c->device));
+  void* base = nullptr;
+  CK(noalloc_scratch(c->device, &base));
+  unsigned char* s = (unsigned char*)base;
+  Bufs b = g.bf;
+  b.G = s;
+  b.H = s + gsz;
+  float2* in32 = mixed ? (float2*)(s + gsz + hsz) : nullptr;
+  if (mixed) launch_to_f32((const double2*)u3, in32, 3LL * g.tb.S, c->st);
+  launch_nonlinear(g.tb, b, c->dctl, mixed, (const double2*)u3, (double2*)n3, c->st, 7, in32);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(c->st));
+  return NSP_OK;
+}
+
 int nsp_lusolve(nsp_ctx* c, int m, int kind, const void* rhs, void* sol) {
   if (int rc = check_member(c, m)) return rc;
   if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_lusolve before nsp_setup");

@@ -93,6 +93,9 @@ void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st)
 void launch_converge(Ctl* dctl, int nmem, unsigned long long cond_handle, int use_cond, cudaStream_t st);
 void launch_lusolve(const Tables& tb, int kind, const double2* rhs, double2* sol, cudaStream_t st);
 void launch_fp64_peak(double* out, int blocks, int threads, int iters, cudaStream_t st);
+// Fixed device scratch of the allocation-free entry point (nsp_noalloc.cu).
+size_t noalloc_scratch_bytes();
+cudaError_t noalloc_scratch(int device, void** ptr);
 // FP32 copy of nmem x 3 x S complex values (the mixed form's transform input).
 void launch_to_f32(const double2* src, float2* dst, long long n, cudaStream_t st);
 int kernels_per_nonlinear();

@@ -24,7 +24,7 @@ EXPORTS = [
     "nsp_set_state_host", "nsp_get_state_host", "nsp_set_state_device", "nsp_get_state_device",
     "nsp_step", "nsp_nonlinear", "nsp_lusolve", "nsp_diag", "nsp_grid", "nsp_kernel_launches",
     "nsp_sync", "nsp_last_error", "nsp_destroy", "nsp_set_stream", "nsp_profile_stages",
-    "nsp_measure_fp64_peak",
+    "nsp_measure_fp64_peak", "nsp_nonlinear_static",
 ]
 
 
@@ -82,6 +82,7 @@ def lib():
         L.nsp_set_stream.argtypes = [vp, vp]
         L.nsp_profile_stages.argtypes = [vp, ip, dp]
         L.nsp_measure_fp64_peak.argtypes = [vp, dp]
+        L.nsp_nonlinear_static.argtypes = [vp, ip, vp, vp]
         L.nsp_last_error.argtypes = [vp]
         L.nsp_last_error.restype = ctypes.c_char_p
         L.nsp_destroy.argtypes = [vp]
@@ -195,6 +196,10 @@ class Stepper:
 
     def nonlinear(self, m, u_dev, n_dev):
         self._check(lib().nsp_nonlinear(self._h, m, *[_ptr(a) for a in u_dev], *[_ptr(a) for a in n_dev]))
+
+    def nonlinear_static(self, m, u3_dev, n3_dev):
+        """Nonlinear term without device allocation; u3/n3 hold (r, theta, z) back to back."""
+        self._check(lib().nsp_nonlinear_static(self._h, m, _ptr(u3_dev), _ptr(n3_dev)))
 
     def lusolve(self, m, kind, rhs_dev, sol_dev):
         self._check(lib().nsp_lusolve(self._h, m, kind, _ptr(rhs_dev), _ptr(sol_dev)))
