@@ -91,7 +91,10 @@ int nsp_save_state(nsp_ctx* ctx, int member, const char* file_r, const char* fil
 
 /* State transfer.  Host pointers: interleaved complex double arrays of NR*NT*NZ
  * values.  Device pointers: same layout in device memory on the context's device
- * (the caller-owned vfield of main.cu:30-33). */
+ * (the caller-owned vfield of main.cu:30-33).  The host variants also accept
+ * member = NSP_ALL_MEMBERS: each pointer then holds that component of every member,
+ * back to back in member order (one synchronisation for the whole ensemble). */
+#define NSP_ALL_MEMBERS (-1)
 int nsp_set_state_host(nsp_ctx* ctx, int member, const double* ur, const double* ut, const double* uz);
 int nsp_get_state_host(nsp_ctx* ctx, int member, double* ur, double* ut, double* uz);
 int nsp_set_state_device(nsp_ctx* ctx, int member, const void* ur, const void* ut, const void* uz);

@@ -524,22 +524,39 @@ int nsp_save_state(nsp_ctx* c, int m, const char* fr, const char* ft, const char
   return NSP_OK;
 }
 
+// Host transfers of one member, or of all members (member == NSP_ALL_MEMBERS) from/to
+// arrays holding every member's component back to back in member order; one
+// synchronisation per call.
 int nsp_set_state_host(nsp_ctx* c, int m, const double* ur, const double* ut, const double* uz) {
-  if (int rc = check_member(c, m)) return rc;
+  if (!c) return NSP_ERR_ARG;
+  if (m != NSP_ALL_MEMBERS)
+    if (int rc = check_member(c, m)) return rc;
   if (!ur || !ut || !uz) return fail(c, NSP_ERR_ARG, "null state pointer");
-  size_t bytes = sizeof(double2) * (size_t)c->groups[c->grp[m]].tb.S;
   const double* src[3] = {ur, ut, uz};
-  for (int k = 0; k < 3; k++) CK(cudaMemcpyAsync(state_ptr(c, m, k), src[k], bytes, cudaMemcpyHostToDevice, c->st));
+  size_t off = 0;
+  for (int mm = (m < 0 ? 0 : m); mm < (m < 0 ? c->nmem : m + 1); mm++) {
+    size_t n = 2 * (size_t)c->groups[c->grp[mm]].tb.S;
+    for (int k = 0; k < 3; k++)
+      CK(cudaMemcpyAsync(state_ptr(c, mm, k), src[k] + off, n * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    off += n;
+  }
   CK(cudaStreamSynchronize(c->st));
   return NSP_OK;
 }
 
 int nsp_get_state_host(nsp_ctx* c, int m, double* ur, double* ut, double* uz) {
-  if (int rc = check_member(c, m)) return rc;
+  if (!c) return NSP_ERR_ARG;
+  if (m != NSP_ALL_MEMBERS)
+    if (int rc = check_member(c, m)) return rc;
   if (!ur || !ut || !uz) return fail(c, NSP_ERR_ARG, "null state pointer");
-  size_t bytes = sizeof(double2) * (size_t)c->groups[c->grp[m]].tb.S;
   double* dst[3] = {ur, ut, uz};
-  for (int k = 0; k < 3; k++) CK(cudaMemcpyAsync(dst[k], state_ptr(c, m, k), bytes, cudaMemcpyDeviceToHost, c->st));
+  size_t off = 0;
+  for (int mm = (m < 0 ? 0 : m); mm < (m < 0 ? c->nmem : m + 1); mm++) {
+    size_t n = 2 * (size_t)c->groups[c->grp[mm]].tb.S;
+    for (int k = 0; k < 3; k++)
+      CK(cudaMemcpyAsync(dst[k] + off, state_ptr(c, mm, k), n * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    off += n;
+  }
   CK(cudaStreamSynchronize(c->st));
   return NSP_OK;
 }

@@ -50,7 +50,7 @@ struct Tables {
   int lin_variant;     // block shape of the linear pass (autotuned at setup)
 };
 
-constexpr int LIN_VARIANTS = 4;
+constexpr int LIN_VARIANTS = 8;
 int linear_default_variant(int NR);
 bool linear_variant_fits(int v, int NR);
 
@@ -58,7 +58,7 @@ bool linear_variant_fits(int v, int NR);
 struct Bufs {
   double2* U[2];       // [nmem][3][S]: state / corrector iterate, roles swap each step (parity)
   float2* U32[2];      // mixed form only: FP32 copies of U[0], U[1] read by the transforms
-  double2* RHSW;       // [nmem][3][S]: N(u^n) in +/- form (rhsw of mod_integrate.cu:100-107)
+  double2* RHSW;       // [nmem][3][S]: (1-d_im) N(u^n) + u^n/dt + (1-d_im)/Re L u^n, +/- form
   double2* N;          // [nmem][3][S]: nonlinear term output
   void* G;             // [nmem][9][NR][NTP][NZ] complex T: theta-inverse of u, dr u, i m u / r
   void* H;             // [nmem][3][NR][NTP][NZ] complex T: z-forward of the nonlinear product

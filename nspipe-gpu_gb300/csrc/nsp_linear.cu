@@ -38,13 +38,15 @@ __device__ __forceinline__ void solve_line(double2* X, int ld, const double* __r
     X[i * ld] = x;
     xm3 = xm2; xm2 = xm1; xm1 = x;
   }
+  // Backward sweep: the farther neighbours are subtracted first, so only one
+  // multiply-add and the pivot multiply wait on the row just finished.
   double2 xp1 = c2(0, 0), xp2 = c2(0, 0), xp3 = c2(0, 0);
   for (int i = NR - 1; i >= 0; i--) {
     const double* fr = f + i * rs;
     double2 x = X[i * ld];
-    if (i + 1 < NR) { double u = __ldg(fr + 4 * NTNZ); x.x -= u * xp1.x; x.y -= u * xp1.y; }
-    if (i + 2 < NR) { double u = __ldg(fr + 5 * NTNZ); x.x -= u * xp2.x; x.y -= u * xp2.y; }
     if (i + 3 < NR) { double u = __ldg(fr + 6 * NTNZ); x.x -= u * xp3.x; x.y -= u * xp3.y; }
+    if (i + 2 < NR) { double u = __ldg(fr + 5 * NTNZ); x.x -= u * xp2.x; x.y -= u * xp2.y; }
+    if (i + 1 < NR) { double u = __ldg(fr + 4 * NTNZ); x.x -= u * xp1.x; x.y -= u * xp1.y; }
     double ui = __ldg(fr + 3 * NTNZ);
     x.x *= ui;
     x.y *= ui;
@@ -79,66 +81,87 @@ __global__ void __launch_bounds__(NTH) linear_k(Tables tb, Bufs bf, Ctl* ctl) {
   const int tid = threadIdx.x, nth = blockDim.x;
   if (tid == 0) bad = 0;
 
-  // A. u^n -> +/- (uw), N -> +/-; predictor stores rhsw, corrector blends d_im N + (1-d_im) rhsw.
-  for (int p = tid; p < LN; p += nth) {
-    int i = p / LM, mm = p - i * LM, k = k0 + mm;
-    if (k >= NTNZ) {
-      for (int c = 0; c < 3; c++) { W[c * LN + p] = c2(0, 0); R[c * LN + p] = c2(0, 0); }
-      continue;
-    }
-    size_t h = (size_t)i * NTNZ + k;
-    double2 ur = Un[h], ut = Un[S + h], uz = Un[2 * S + h];
-    W[p] = c2(ur.x - ut.y, ur.y + ut.x);
-    W[LN + p] = c2(ur.x + ut.y, ur.y - ut.x);
-    W[2 * LN + p] = uz;
-    double2 nr = Nn[h], nt = Nn[S + h], nz = Nn[2 * S + h];
-    double2 np = c2(nr.x - nt.y, nr.y + nt.x), nm = c2(nr.x + nt.y, nr.y - nt.x);
-    if (pred) {
-      Rw[h] = np; Rw[S + h] = nm; Rw[2 * S + h] = nz;
-    } else {
-      double2 w0 = Rw[h], w1 = Rw[S + h], w2 = Rw[2 * S + h];
-      np = c2(tb.d_im * np.x + tb.one_m_dim * w0.x, tb.d_im * np.y + tb.one_m_dim * w0.y);
-      nm = c2(tb.d_im * nm.x + tb.one_m_dim * w1.x, tb.d_im * nm.y + tb.one_m_dim * w1.y);
-      nz = c2(tb.d_im * nz.x + tb.one_m_dim * w2.x, tb.d_im * nz.y + tb.one_m_dim * w2.y);
-    }
-    R[p] = np; R[LN + p] = nm; R[2 * LN + p] = nz;
-  }
-  __syncthreads();
-
-  // B. rhs += u/dt + (1-d_im)/Re (L_r - k_z^2 - m^2/r^2 [-1/r^2 -+ 2m/r^2]) u, then +/- -> r/theta.
-  for (int p = tid; p < LN; p += nth) {
-    int i = p / LM, mm = p - i * LM, k = k0 + mm;
-    if (k >= NTNZ) continue;
-    int it = k / NZ, l = k - it * NZ, m = it < NT / 2 ? it : it - NT;
-    double kt = tb.kts * (double)m, kz = tb.kzs * (double)l;
-    int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
-    double ir2 = tb.rinv2[i];
-    double base = -kz * kz - kt * kt * ir2;
-    double pm = -ir2 - 2.0 * kt * ir2, mm2 = -ir2 + 2.0 * kt * ir2;
-    double2 out[3];
-#pragma unroll
-    for (int c = 0; c < 3; c++) {
-      int tab = abs((abs(m) % 2) - (c < 2 ? 1 : 0));
-      const double* Lr = tb.Luc + tab * STEN * NR + STEN * i + i0;  // (1-d_im)/Re * L_r
-      const double2* Wc = W + c * LN + mm;
-      double2 rr = R[c * LN + p];
-      double sx = rr.x, sy = rr.y;
-      for (int j = 0; j < len; j++) {
-        double de = __ldg(Lr + j);
-        double2 a = Wc[(left + j) * LM];
-        sx += de * a.x;
-        sy += de * a.y;
+  // The explicit part of the right-hand side, e = u^n/dt + (1-d_im)/Re L+- u^n
+  // (addLaplacian, mod_linear.cu:12-51), is the same in the predictor and in every
+  // corrector of a step.  The predictor computes it once and stores
+  // rhsw' = (1-d_im) N(u^n)+- + e; a corrector's right-hand side is then
+  // d_im N(u_i)+- + rhsw' (addRHS_k + addLaplacian), with no stencil and no read of u^n.
+  if (pred) {
+    // A. u^n -> +/- (uw) into W, N(u^n) -> +/- into R.
+    for (int p = tid; p < LN; p += nth) {
+      int i = p / LM, mm = p - i * LM, k = k0 + mm;
+      if (k >= NTNZ) {
+        for (int c = 0; c < 3; c++) { W[c * LN + p] = c2(0, 0); R[c * LN + p] = c2(0, 0); }
+        continue;
       }
-      double2 aux = Wc[i * LM];
-      double de = base + (c == 0 ? pm : (c == 1 ? mm2 : 0.0));
-      double dd = tb.c_ex * de + tb.inv_dt;  // diagonal: (1-d_im)/Re (-k_z^2 - m^2/r^2 ...) + 1/dt
-      sx += dd * aux.x;
-      sy += dd * aux.y;
-      out[c] = c2(sx, sy);
+      size_t h = (size_t)i * NTNZ + k;
+      double2 ur = Un[h], ut = Un[S + h], uz = Un[2 * S + h];
+      W[p] = c2(ur.x - ut.y, ur.y + ut.x);
+      W[LN + p] = c2(ur.x + ut.y, ur.y - ut.x);
+      W[2 * LN + p] = uz;
+      double2 nr = Nn[h], nt = Nn[S + h], nz = Nn[2 * S + h];
+      R[p] = c2(nr.x - nt.y, nr.y + nt.x);
+      R[LN + p] = c2(nr.x + nt.y, nr.y - nt.x);
+      R[2 * LN + p] = nz;
     }
-    R[p] = c2(0.5 * (out[0].x + out[1].x), 0.5 * (out[0].y + out[1].y));
-    R[LN + p] = c2(0.5 * (out[0].y - out[1].y), -0.5 * (out[0].x - out[1].x));
-    R[2 * LN + p] = out[2];
+    __syncthreads();
+    // B. e = u/dt + (1-d_im)/Re (L_r - k_z^2 - m^2/r^2 [-1/r^2 -+ 2m/r^2]) u; rhs = N + e;
+    //    rhsw' = (1-d_im) N + e; rhs +/- -> r/theta.
+    for (int p = tid; p < LN; p += nth) {
+      int i = p / LM, mm = p - i * LM, k = k0 + mm;
+      if (k >= NTNZ) continue;
+      int it = k / NZ, l = k - it * NZ, m = it < NT / 2 ? it : it - NT;
+      double kt = tb.kts * (double)m, kz = tb.kzs * (double)l;
+      int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
+      double ir2 = tb.rinv2[i];
+      double base = -kz * kz - kt * kt * ir2;
+      double pm = -ir2 - 2.0 * kt * ir2, mm2 = -ir2 + 2.0 * kt * ir2;
+      size_t h = (size_t)i * NTNZ + k;
+      double2 out[3];
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        int tab = abs((abs(m) % 2) - (c < 2 ? 1 : 0));
+        const double* Lr = tb.Luc + tab * STEN * NR + STEN * i + i0;  // (1-d_im)/Re * L_r
+        const double2* Wc = W + c * LN + mm;
+        double sx = 0.0, sy = 0.0;
+        for (int j = 0; j < len; j++) {
+          double de = __ldg(Lr + j);
+          double2 a = Wc[(left + j) * LM];
+          sx += de * a.x;
+          sy += de * a.y;
+        }
+        double2 aux = Wc[i * LM];
+        double de = base + (c == 0 ? pm : (c == 1 ? mm2 : 0.0));
+        double dd = tb.c_ex * de + tb.inv_dt;  // diagonal: (1-d_im)/Re (-k_z^2 - m^2/r^2 ...) + 1/dt
+        sx += dd * aux.x;
+        sy += dd * aux.y;
+        double2 n = R[c * LN + p];
+        out[c] = c2(n.x + sx, n.y + sy);
+        Rw[c * S + h] = c2(tb.one_m_dim * n.x + sx, tb.one_m_dim * n.y + sy);
+      }
+      R[p] = c2(0.5 * (out[0].x + out[1].x), 0.5 * (out[0].y + out[1].y));
+      R[LN + p] = c2(0.5 * (out[0].y - out[1].y), -0.5 * (out[0].x - out[1].x));
+      R[2 * LN + p] = out[2];
+    }
+  } else {
+    // A+B. rhs = d_im N(u_i)+- + rhsw', then +/- -> r/theta.
+    for (int p = tid; p < LN; p += nth) {
+      int i = p / LM, mm = p - i * LM, k = k0 + mm;
+      if (k >= NTNZ) {
+        for (int c = 0; c < 3; c++) R[c * LN + p] = c2(0, 0);
+        continue;
+      }
+      size_t h = (size_t)i * NTNZ + k;
+      double2 nr = Nn[h], nt = Nn[S + h], nz = Nn[2 * S + h];
+      double2 w0 = Rw[h], w1 = Rw[S + h], w2 = Rw[2 * S + h];
+      double2 np = c2(nr.x - nt.y, nr.y + nt.x), nm = c2(nr.x + nt.y, nr.y - nt.x);
+      np = c2(tb.d_im * np.x + w0.x, tb.d_im * np.y + w0.y);
+      nm = c2(tb.d_im * nm.x + w1.x, tb.d_im * nm.y + w1.y);
+      nz = c2(tb.d_im * nz.x + w2.x, tb.d_im * nz.y + w2.y);
+      R[p] = c2(0.5 * (np.x + nm.x), 0.5 * (np.y + nm.y));
+      R[LN + p] = c2(0.5 * (np.y - nm.y), -0.5 * (np.x - nm.x));
+      R[2 * LN + p] = nz;
+    }
   }
   __syncthreads();
 
@@ -159,11 +182,11 @@ __global__ void __launch_bounds__(NTH) linear_k(Tables tb, Bufs bf, Ctl* ctl) {
         sx += de * a.x;
         sy += de * a.y;
       }
-      double ri = tb.rinv[i];
+      double ri = tb.rinv[i], kti = kt * ri;
       double2 rr = R[p], rt = R[LN + p], rz = R[2 * LN + p];
       sx += rr.x * ri; sy += rr.y * ri;
-      sx += -kt * rt.y * ri; sy += kt * rt.x * ri;
-      sx += -kz * rz.y; sy += kz * rz.x;
+      sx -= kti * rt.y; sy += kti * rt.x;
+      sx -= kz * rz.y; sy += kz * rz.x;
       d = c2(sx, sy);
     }
     P[p] = d;
@@ -192,12 +215,12 @@ __global__ void __launch_bounds__(NTH) linear_k(Tables tb, Bufs bf, Ctl* ctl) {
         sx += de * a.x;
         sy += de * a.y;
       }
-      double ri = tb.rinv[i];
+      double kti = kt * tb.rinv[i];
       double2 pp = P[p], rr = R[p], rt = R[LN + p];
       rz = R[2 * LN + p];
       rr.x -= sx; rr.y -= sy;
-      rt.x -= -kt * pp.y * ri; rt.y -= kt * pp.x * ri;
-      rz.x -= -kz * pp.y; rz.y -= kz * pp.x;
+      rt.x += kti * pp.y; rt.y -= kti * pp.x;
+      rz.x += kz * pp.y; rz.y -= kz * pp.x;
       up = c2(rr.x - rt.y, rr.y + rt.x);
       um = c2(rr.x + rt.y, rr.y - rt.x);
     }
@@ -391,7 +414,8 @@ __global__ void lusolve_k(Tables tb, int kind, const double2* rhs, double2* sol)
 // Block shapes of the linear pass (modes per block, threads): the candidates of the
 // setup-time autotuner.  Shared memory per block is 6 radial lines per mode.
 struct LinShape { int LM, NTH; };
-static const LinShape kLinShapes[LIN_VARIANTS] = {{16, 256}, {8, 128}, {8, 256}, {4, 128}};
+static const LinShape kLinShapes[LIN_VARIANTS] = {{16, 256}, {8, 128}, {8, 256}, {4, 128},
+                                                  {12, 192}, {12, 256}, {24, 384}, {32, 512}};
 
 int linear_default_variant(int NR) { return NR <= 64 ? 0 : 2; }
 
@@ -405,6 +429,10 @@ void configure_linear_kernels() {
   cudaFuncSetAttribute(linear_k<8, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(linear_k<8, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   cudaFuncSetAttribute(linear_k<4, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(linear_k<12, 192>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(linear_k<12, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(linear_k<24, 384>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(linear_k<32, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
 }
 
 void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st) {
@@ -416,7 +444,11 @@ void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st)
     case 0: linear_k<16, 256><<<grid, 256, smem, st>>>(tb, bf, dctl); break;
     case 1: linear_k<8, 128><<<grid, 128, smem, st>>>(tb, bf, dctl); break;
     case 2: linear_k<8, 256><<<grid, 256, smem, st>>>(tb, bf, dctl); break;
-    default: linear_k<4, 128><<<grid, 128, smem, st>>>(tb, bf, dctl); break;
+    case 3: linear_k<4, 128><<<grid, 128, smem, st>>>(tb, bf, dctl); break;
+    case 4: linear_k<12, 192><<<grid, 192, smem, st>>>(tb, bf, dctl); break;
+    case 5: linear_k<12, 256><<<grid, 256, smem, st>>>(tb, bf, dctl); break;
+    case 6: linear_k<24, 384><<<grid, 384, smem, st>>>(tb, bf, dctl); break;
+    default: linear_k<32, 512><<<grid, 512, smem, st>>>(tb, bf, dctl); break;
   }
 }
 

@@ -163,9 +163,31 @@ class Stepper:
                 raise ValueError("state shape %s != %s" % (a.shape, self.shape(m)))
         self._check(lib().nsp_set_state_host(self._h, m, _dp(u[0]), _dp(u[1]), _dp(u[2])))
 
-    def get_state(self, m):
-        u = [np.zeros(self.shape(m), np.complex128) for _ in range(3)]
+    def get_state(self, m, out=None):
+        u = out if out is not None else [np.zeros(self.shape(m), np.complex128) for _ in range(3)]
+        for a in u:
+            if a.dtype != np.complex128 or not a.flags["C_CONTIGUOUS"] or a.size != int(np.prod(self.shape(m))):
+                raise ValueError("output must be C-contiguous complex128 of the member's shape")
         self._check(lib().nsp_get_state_host(self._h, m, _dp(u[0]), _dp(u[1]), _dp(u[2])))
+        return u
+
+    def _all_size(self):
+        return sum(int(np.prod(self.shape(m))) for m in range(self.n))
+
+    def set_states_all(self, u_all):
+        """All members at once: u_all[c] holds component c of every member back to back."""
+        u_all = [np.ascontiguousarray(a, np.complex128) for a in u_all]
+        for a in u_all:
+            if a.size != self._all_size():
+                raise ValueError("expected %d values per component" % self._all_size())
+        self._check(lib().nsp_set_state_host(self._h, -1, _dp(u_all[0]), _dp(u_all[1]), _dp(u_all[2])))
+
+    def get_states_all(self, out=None):
+        u = out if out is not None else [np.zeros(self._all_size(), np.complex128) for _ in range(3)]
+        for a in u:
+            if a.dtype != np.complex128 or not a.flags["C_CONTIGUOUS"] or a.size != self._all_size():
+                raise ValueError("output must be C-contiguous complex128 with every member")
+        self._check(lib().nsp_get_state_host(self._h, -1, _dp(u[0]), _dp(u[1]), _dp(u[2])))
         return u
 
     def set_state_device(self, m, ur, ut, uz):
