@@ -25,33 +25,77 @@ namespace nsp {
 
 __device__ __forceinline__ double2 c2(double x, double y) { return make_double2(x, y); }
 
+// One forward-substitution row: x -= L(i-3) x_{i-3} + L(i-2) x_{i-2} + L(i-1) x_{i-1},
+// in the reference's column order.  Factors of columns outside the band are stored
+// as 0 (and the carried x start at 0), so edge rows need no branches.
+__device__ __forceinline__ void fwd_row(double2& x, const double* l, double2& xm1, double2& xm2, double2& xm3) {
+  x.x -= l[0] * xm3.x; x.y -= l[0] * xm3.y;
+  x.x -= l[1] * xm2.x; x.y -= l[1] * xm2.y;
+  x.x -= l[2] * xm1.x; x.y -= l[2] * xm1.y;
+  xm3 = xm2; xm2 = xm1; xm1 = x;
+}
+// One backward row, farther neighbours first so that only one multiply-add and the
+// pivot multiply wait on the row just finished: x = (x - U3 x3 - U2 x2 - U1 x1) / U_ii.
+__device__ __forceinline__ void bwd_row(double2& x, const double* u, double2& xp1, double2& xp2, double2& xp3) {
+  x.x -= u[0] * xp3.x; x.y -= u[0] * xp3.y;
+  x.x -= u[1] * xp2.x; x.y -= u[1] * xp2.y;
+  x.x -= u[2] * xp1.x; x.y -= u[2] * xp1.y;
+  x.x *= u[3]; x.y *= u[3];
+  xp3 = xp2; xp2 = xp1; xp1 = x;
+}
+
 // Forward + backward substitution of one mode line held in X[i*ld] (i = 0..NR-1).
+// Factor rows are fetched four at a time so that their L2 latencies overlap.
 __device__ __forceinline__ void solve_line(double2* X, int ld, const double* __restrict__ f, int NTNZ, int NR) {
   const size_t rs = (size_t)NFAC * NTNZ;  // row stride of the factor table
   double2 xm1 = c2(0, 0), xm2 = c2(0, 0), xm3 = c2(0, 0);
-  for (int i = 0; i < NR; i++) {
-    const double* fr = f + i * rs;
-    double2 x = X[i * ld];
-    if (i >= 3) { double l = __ldg(fr); x.x -= l * xm3.x; x.y -= l * xm3.y; }
-    if (i >= 2) { double l = __ldg(fr + NTNZ); x.x -= l * xm2.x; x.y -= l * xm2.y; }
-    if (i >= 1) { double l = __ldg(fr + 2 * NTNZ); x.x -= l * xm1.x; x.y -= l * xm1.y; }
-    X[i * ld] = x;
-    xm3 = xm2; xm2 = xm1; xm1 = x;
+  int i = 0;
+  for (; i + 4 <= NR; i += 4) {
+    double l[4][3];
+    double2 b[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const double* fr = f + (i + r) * rs;
+      l[r][0] = __ldg(fr); l[r][1] = __ldg(fr + NTNZ); l[r][2] = __ldg(fr + 2 * NTNZ);
+      b[r] = X[(i + r) * ld];
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      fwd_row(b[r], l[r], xm1, xm2, xm3);
+      X[(i + r) * ld] = b[r];
+    }
   }
-  // Backward sweep: the farther neighbours are subtracted first, so only one
-  // multiply-add and the pivot multiply wait on the row just finished.
-  double2 xp1 = c2(0, 0), xp2 = c2(0, 0), xp3 = c2(0, 0);
-  for (int i = NR - 1; i >= 0; i--) {
+  for (; i < NR; i++) {
     const double* fr = f + i * rs;
+    double l[3] = {__ldg(fr), __ldg(fr + NTNZ), __ldg(fr + 2 * NTNZ)};
     double2 x = X[i * ld];
-    if (i + 3 < NR) { double u = __ldg(fr + 6 * NTNZ); x.x -= u * xp3.x; x.y -= u * xp3.y; }
-    if (i + 2 < NR) { double u = __ldg(fr + 5 * NTNZ); x.x -= u * xp2.x; x.y -= u * xp2.y; }
-    if (i + 1 < NR) { double u = __ldg(fr + 4 * NTNZ); x.x -= u * xp1.x; x.y -= u * xp1.y; }
-    double ui = __ldg(fr + 3 * NTNZ);
-    x.x *= ui;
-    x.y *= ui;
+    fwd_row(x, l, xm1, xm2, xm3);
     X[i * ld] = x;
-    xp3 = xp2; xp2 = xp1; xp1 = x;
+  }
+  double2 xp1 = c2(0, 0), xp2 = c2(0, 0), xp3 = c2(0, 0);
+  i = NR - 1;
+  for (; i >= 3; i -= 4) {
+    double u[4][4];
+    double2 b[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const double* fr = f + (i - r) * rs;
+      u[r][0] = __ldg(fr + 6 * NTNZ); u[r][1] = __ldg(fr + 5 * NTNZ);
+      u[r][2] = __ldg(fr + 4 * NTNZ); u[r][3] = __ldg(fr + 3 * NTNZ);
+      b[r] = X[(i - r) * ld];
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      bwd_row(b[r], u[r], xp1, xp2, xp3);
+      X[(i - r) * ld] = b[r];
+    }
+  }
+  for (; i >= 0; i--) {
+    const double* fr = f + i * rs;
+    double u[4] = {__ldg(fr + 6 * NTNZ), __ldg(fr + 5 * NTNZ), __ldg(fr + 4 * NTNZ), __ldg(fr + 3 * NTNZ)};
+    double2 x = X[i * ld];
+    bwd_row(x, u, xp1, xp2, xp3);
+    X[i * ld] = x;
   }
 }
 
