@@ -442,7 +442,7 @@ int nsp_setup(nsp_ctx* c) {
     std::vector<float> D32(o.D.size());
     for (int i = 0; i < p.NR; i++) { rinv[i] = 1.0 / o.r[i]; rinv2[i] = 1.0 / (o.r[i] * o.r[i]); }
     const double c_ex = (1.0 - p.d_im) / p.Re;
-    for (size_t e = 0; e < o.Lu.size(); e++) Luc[e] = c_ex * o.Lu[e];
+    for (size_t e = 0; e < o.Lu.size(); e++) Luc[e] = 0.5 * (c_ex * o.Lu[e]);
     for (size_t e = 0; e < o.D.size(); e++) D32[e] = (float)o.D[e];
     int rc;
     if ((rc = upload(c, &tb.r, o.r)) || (rc = upload(c, &tb.rinv, rinv)) || (rc = upload(c, &tb.rinv2, rinv2)) ||

@@ -39,7 +39,7 @@ struct Tables {
   const double* D;     // [2][NR][7]: first derivative, parity tables (0 even-extended, 1 odd)
   const float* D32;    // the same in FP32 (mixed-form transforms)
   const double* Lu;    // [2][NR][7]: radial Laplacian rows with identity wall row
-  const double* Luc;   // (1-d_im)/Re * Lu (explicit part of the Laplacian, pre-scaled)
+  const double* Luc;   // (1-d_im)/(2 Re) * Lu (explicit part of the Laplacian, pre-scaled)
   const double* fac;   // [4][NR][7][NTNZ]: banded LU factors of u+, u-, u_z, p
   const double2* V;    // [3][NR][NTNZ]: influence-matrix correction profiles (+, -, z)
   const double2* tw_t; // [NTP] exp(-2 pi i e/NTP), FP64
@@ -58,7 +58,7 @@ bool linear_variant_fits(int v, int NR);
 struct Bufs {
   double2* U[2];       // [nmem][3][S]: state / corrector iterate, roles swap each step (parity)
   float2* U32[2];      // mixed form only: FP32 copies of U[0], U[1] read by the transforms
-  double2* RHSW;       // [nmem][3][S]: (1-d_im) N(u^n) + u^n/dt + (1-d_im)/Re L u^n, +/- form
+  double2* RHSW;       // [nmem][3][S]: [(1-d_im) N(u^n) + u^n/dt + (1-d_im)/Re L u^n] / 2, r/theta form
   double2* N;          // [nmem][3][S]: nonlinear term output
   void* G;             // [nmem][9][NR][NTP][NZ] complex T: theta-inverse of u, dr u, i m u / r
   void* H;             // [nmem][3][NR][NTP][NZ] complex T: z-forward of the nonlinear product

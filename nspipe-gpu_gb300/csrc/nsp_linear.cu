@@ -14,8 +14,9 @@
 // The radial lines of the block's modes are staged in shared memory as
 // [component][r][mode]; pointwise and stencil phases use all threads over
 // (r, mode), the banded solves one thread per (component, mode) sweeping r with
-// the precomputed factors (read coalesced across modes).  u^n in +/- form (uw)
-// is recomputed from the state instead of stored.
+// the precomputed factors (read coalesced across modes).  The explicit
+// Laplacian of u^n is applied straight from the state in global memory (no uw
+// array, no shared-memory staging), so a block holds 4 radial lines per mode.
 #include <cstdio>
 
 #include "nsp_internal.h"
@@ -99,8 +100,10 @@ __device__ __forceinline__ void solve_line(double2* X, int ld, const double* __r
   }
 }
 
+// At least 1024 threads per SM resident (4 radial lines of 48 points x 16 modes
+// is 49 KB of shared memory, so four 256-thread blocks fit).
 template <int LM, int NTH>
-__global__ void __launch_bounds__(NTH) linear_k(Tables tb, Bufs bf, Ctl* ctl) {
+__global__ void __launch_bounds__(NTH, (1024 / NTH) < 2 ? 2 : (1024 / NTH)) linear_k(Tables tb, Bufs bf, Ctl* ctl) {
   const int mloc = blockIdx.y, gm = tb.mem0 + mloc;
   const int ph = ctl->phase[gm];
   if (ph < 0) return;
@@ -111,84 +114,91 @@ __global__ void __launch_bounds__(NTH) linear_k(Tables tb, Bufs bf, Ctl* ctl) {
   const int k0 = blockIdx.x * LM;
   const int LN = NR * LM;
   extern __shared__ double2 sm[];
-  double2* W = sm;           // [3][NR][LM] u^n in +/- form
-  double2* R = sm + 3 * LN;  // [3][NR][LM] right-hand side, then the new velocity
-  double2* P = W;            // divergence / pressure (W is dead by then)
+  double2* R = sm;           // [3][NR][LM] right-hand side, then the new velocity
+  double2* P = sm + 3 * LN;  // [NR][LM] divergence, then the pressure
   __shared__ double2 dvs[LM];
-  __shared__ double wnum[NTH / 32], wden[NTH / 32];
+  __shared__ unsigned long long wnum[NTH / 32], wden[NTH / 32];
+  __shared__ double skt[LM], skz[LM];  // k_theta, k_z of the block's modes
+  __shared__ int spar[LM];             // |m| mod 2 (selects the parity tables)
   __shared__ int bad;
-  const double2* Un = bf.U[par] + (size_t)mloc * 3 * S;
-  double2* Ui = bf.U[par ^ 1] + (size_t)mloc * 3 * S;
-  float2* Ui32 = bf.U32[par ^ 1] ? bf.U32[par ^ 1] + (size_t)mloc * 3 * S : nullptr;  // mixed form
+  // (selects instead of indexing the parameter arrays by a run-time value, which
+  // would copy them to local memory)
+  const double2* Un = (par ? bf.U[1] : bf.U[0]) + (size_t)mloc * 3 * S;
+  double2* Ui = (par ? bf.U[0] : bf.U[1]) + (size_t)mloc * 3 * S;
+  float2* U32i = par ? bf.U32[0] : bf.U32[1];
+  float2* Ui32 = U32i ? U32i + (size_t)mloc * 3 * S : nullptr;  // mixed form
   const double2* Nn = bf.N + (size_t)mloc * 3 * S;
   double2* Rw = bf.RHSW + (size_t)mloc * 3 * S;
   const int tid = threadIdx.x, nth = blockDim.x;
   if (tid == 0) bad = 0;
+  if (tid < LM) {  // wavenumbers once per block instead of per point (the FP64 pipe is the bound)
+    int k = k0 + tid, it = k / NZ, l = k - it * NZ, m = it < NT / 2 ? it : it - NT;
+    skt[tid] = tb.kts * (double)m;
+    skz[tid] = tb.kzs * (double)l;
+    spar[tid] = abs(m) % 2;
+  }
+  __syncthreads();
 
+  // Every line from the right-hand side to the Helmholtz solutions is carried at
+  // half scale (exact: a power of two through linear operations), so the +/- <->
+  // r/theta conversions need no multiply by 1/2.
+  //
   // The explicit part of the right-hand side, e = u^n/dt + (1-d_im)/Re L+- u^n
   // (addLaplacian, mod_linear.cu:12-51), is the same in the predictor and in every
   // corrector of a step.  The predictor computes it once and stores
-  // rhsw' = (1-d_im) N(u^n)+- + e; a corrector's right-hand side is then
-  // d_im N(u_i)+- + rhsw' (addRHS_k + addLaplacian), with no stencil and no read of u^n.
+  // rhsw' = (1-d_im) N(u^n) + e, in r/theta form and at half scale; a corrector's
+  // right-hand side is then d_im N(u_i) + rhsw' (addRHS_k + addLaplacian), with no
+  // stencil, no +/- conversion and no read of u^n.
   if (pred) {
-    // A. u^n -> +/- (uw) into W, N(u^n) -> +/- into R.
+    // e = u^n/dt + (1-d_im)/Re (L_r - k_z^2 - m^2/r^2 [-1/r^2 -+ 2m/r^2]) u^n on the +/- lines
+    // (addLaplacian), evaluated in r/theta form: with dd+- the two diagonals,
+    // s = (dd+ + dd-)/2 and d = (dd+ - dd-)/2,
+    //   e_r = L u_r + s u_r + i d u_t,   e_theta = L u_t + s u_t - i d u_r.
+    // Luc holds the stencil pre-scaled by 1/2, so e comes out at half scale; u^n is
+    // read straight from global memory (the stencil's rows are served by L1).
+    // Then, at half scale: rhs = N + e, rhsw' = (1-d_im) N + e.
+    const double hc = 0.5 * tb.c_ex, hidt = 0.5 * tb.inv_dt, hw = 0.5 * tb.one_m_dim;
     for (int p = tid; p < LN; p += nth) {
       int i = p / LM, mm = p - i * LM, k = k0 + mm;
       if (k >= NTNZ) {
-        for (int c = 0; c < 3; c++) { W[c * LN + p] = c2(0, 0); R[c * LN + p] = c2(0, 0); }
+        for (int c = 0; c < 3; c++) R[c * LN + p] = c2(0, 0);
         continue;
       }
-      size_t h = (size_t)i * NTNZ + k;
-      double2 ur = Un[h], ut = Un[S + h], uz = Un[2 * S + h];
-      W[p] = c2(ur.x - ut.y, ur.y + ut.x);
-      W[LN + p] = c2(ur.x + ut.y, ur.y - ut.x);
-      W[2 * LN + p] = uz;
-      double2 nr = Nn[h], nt = Nn[S + h], nz = Nn[2 * S + h];
-      R[p] = c2(nr.x - nt.y, nr.y + nt.x);
-      R[LN + p] = c2(nr.x + nt.y, nr.y - nt.x);
-      R[2 * LN + p] = nz;
-    }
-    __syncthreads();
-    // B. e = u/dt + (1-d_im)/Re (L_r - k_z^2 - m^2/r^2 [-1/r^2 -+ 2m/r^2]) u; rhs = N + e;
-    //    rhsw' = (1-d_im) N + e; rhs +/- -> r/theta.
-    for (int p = tid; p < LN; p += nth) {
-      int i = p / LM, mm = p - i * LM, k = k0 + mm;
-      if (k >= NTNZ) continue;
-      int it = k / NZ, l = k - it * NZ, m = it < NT / 2 ? it : it - NT;
-      double kt = tb.kts * (double)m, kz = tb.kzs * (double)l;
+      double kt = skt[mm], kz = skz[mm];
+      int par_m = spar[mm];
       int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
       double ir2 = tb.rinv2[i];
       double base = -kz * kz - kt * kt * ir2;
-      double pm = -ir2 - 2.0 * kt * ir2, mm2 = -ir2 + 2.0 * kt * ir2;
-      size_t h = (size_t)i * NTNZ + k;
-      double2 out[3];
-#pragma unroll
-      for (int c = 0; c < 3; c++) {
-        int tab = abs((abs(m) % 2) - (c < 2 ? 1 : 0));
-        const double* Lr = tb.Luc + tab * STEN * NR + STEN * i + i0;  // (1-d_im)/Re * L_r
-        const double2* Wc = W + c * LN + mm;
-        double sx = 0.0, sy = 0.0;
-        for (int j = 0; j < len; j++) {
-          double de = __ldg(Lr + j);
-          double2 a = Wc[(left + j) * LM];
-          sx += de * a.x;
-          sy += de * a.y;
-        }
-        double2 aux = Wc[i * LM];
-        double de = base + (c == 0 ? pm : (c == 1 ? mm2 : 0.0));
-        double dd = tb.c_ex * de + tb.inv_dt;  // diagonal: (1-d_im)/Re (-k_z^2 - m^2/r^2 ...) + 1/dt
-        sx += dd * aux.x;
-        sy += dd * aux.y;
-        double2 n = R[c * LN + p];
-        out[c] = c2(n.x + sx, n.y + sy);
-        Rw[c * S + h] = c2(tb.one_m_dim * n.x + sx, tb.one_m_dim * n.y + sy);
+      double hs = hc * (base - ir2) + hidt;  // s/2
+      double hd = -hc * (2.0 * kt * ir2);    // d/2
+      double hz = hc * base + hidt;          // diagonal of the u_z line / 2
+      const double* Lo = tb.Luc + (1 - par_m) * STEN * NR + STEN * i + i0;  // u_r, u_theta (odd flag)
+      const double* Le = tb.Luc + par_m * STEN * NR + STEN * i + i0;        // u_z
+      double2 lr = c2(0, 0), lt = c2(0, 0), lz = c2(0, 0);
+      for (int j = 0; j < len; j++) {
+        double a = __ldg(Lo + j), b = __ldg(Le + j);
+        size_t hj = (size_t)(left + j) * NTNZ + k;
+        double2 vr = Un[hj], vt = Un[S + hj], vz = Un[2 * S + hj];
+        lr.x += a * vr.x; lr.y += a * vr.y;
+        lt.x += a * vt.x; lt.y += a * vt.y;
+        lz.x += b * vz.x; lz.y += b * vz.y;
       }
-      R[p] = c2(0.5 * (out[0].x + out[1].x), 0.5 * (out[0].y + out[1].y));
-      R[LN + p] = c2(0.5 * (out[0].y - out[1].y), -0.5 * (out[0].x - out[1].x));
-      R[2 * LN + p] = out[2];
+      size_t h = (size_t)i * NTNZ + k;
+      double2 ur = Un[h], ut = Un[S + h], uz = Un[2 * S + h];
+      double2 er = c2(lr.x + hs * ur.x - hd * ut.y, lr.y + hs * ur.y + hd * ut.x);
+      double2 et = c2(lt.x + hs * ut.x + hd * ur.y, lt.y + hs * ut.y - hd * ur.x);
+      double2 ez = c2(lz.x + hz * uz.x, lz.y + hz * uz.y);
+      double2 nr = Nn[h], nt = Nn[S + h], nz = Nn[2 * S + h];
+      R[p] = c2(0.5 * nr.x + er.x, 0.5 * nr.y + er.y);
+      R[LN + p] = c2(0.5 * nt.x + et.x, 0.5 * nt.y + et.y);
+      R[2 * LN + p] = c2(0.5 * nz.x + ez.x, 0.5 * nz.y + ez.y);
+      Rw[h] = c2(hw * nr.x + er.x, hw * nr.y + er.y);
+      Rw[S + h] = c2(hw * nt.x + et.x, hw * nt.y + et.y);
+      Rw[2 * S + h] = c2(hw * nz.x + ez.x, hw * nz.y + ez.y);
     }
   } else {
-    // A+B. rhs = d_im N(u_i)+- + rhsw', then +/- -> r/theta.
+    // A+B. rhs/2 = (d_im/2) N(u_i) + rhsw'/2, straight in r/theta form.
+    const double hd = 0.5 * tb.d_im;
     for (int p = tid; p < LN; p += nth) {
       int i = p / LM, mm = p - i * LM, k = k0 + mm;
       if (k >= NTNZ) {
@@ -196,15 +206,11 @@ __global__ void __launch_bounds__(NTH) linear_k(Tables tb, Bufs bf, Ctl* ctl) {
         continue;
       }
       size_t h = (size_t)i * NTNZ + k;
-      double2 nr = Nn[h], nt = Nn[S + h], nz = Nn[2 * S + h];
-      double2 w0 = Rw[h], w1 = Rw[S + h], w2 = Rw[2 * S + h];
-      double2 np = c2(nr.x - nt.y, nr.y + nt.x), nm = c2(nr.x + nt.y, nr.y - nt.x);
-      np = c2(tb.d_im * np.x + w0.x, tb.d_im * np.y + w0.y);
-      nm = c2(tb.d_im * nm.x + w1.x, tb.d_im * nm.y + w1.y);
-      nz = c2(tb.d_im * nz.x + w2.x, tb.d_im * nz.y + w2.y);
-      R[p] = c2(0.5 * (np.x + nm.x), 0.5 * (np.y + nm.y));
-      R[LN + p] = c2(0.5 * (np.y - nm.y), -0.5 * (np.x - nm.x));
-      R[2 * LN + p] = nz;
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        double2 n = Nn[c * S + h], w = Rw[c * S + h];
+        R[c * LN + p] = c2(hd * n.x + w.x, hd * n.y + w.y);
+      }
     }
   }
   __syncthreads();
@@ -214,10 +220,9 @@ __global__ void __launch_bounds__(NTH) linear_k(Tables tb, Bufs bf, Ctl* ctl) {
     int i = p / LM, mm = p - i * LM, k = k0 + mm;
     double2 d = c2(0, 0);
     if (k < NTNZ && i < NR - 1) {
-      int it = k / NZ, l = k - it * NZ, m = it < NT / 2 ? it : it - NT;
-      double kt = tb.kts * (double)m, kz = tb.kzs * (double)l;
+      double kt = skt[mm], kz = skz[mm];
       int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
-      int tab = abs((abs(m) % 2) - 1);
+      int tab = 1 - spar[mm];
       const double* Dr = tb.D + tab * STEN * NR + STEN * i + i0;
       double sx = 0.0, sy = 0.0;
       for (int j = 0; j < len; j++) {
@@ -247,10 +252,9 @@ __global__ void __launch_bounds__(NTH) linear_k(Tables tb, Bufs bf, Ctl* ctl) {
     if (k >= NTNZ) continue;
     double2 up = c2(0, 0), um = c2(0, 0), rz = c2(0, 0);
     if (i < NR - 1) {
-      int it = k / NZ, l = k - it * NZ, m = it < NT / 2 ? it : it - NT;
-      double kt = tb.kts * (double)m, kz = tb.kzs * (double)l;
+      double kt = skt[mm], kz = skz[mm];
       int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
-      int tab = abs(m) % 2;
+      int tab = spar[mm];
       const double* Dr = tb.D + tab * STEN * NR + STEN * i + i0;
       double sx = 0.0, sy = 0.0;
       for (int j = 0; j < len; j++) {
@@ -279,14 +283,13 @@ __global__ void __launch_bounds__(NTH) linear_k(Tables tb, Bufs bf, Ctl* ctl) {
   }
   __syncthreads();
 
-  // G1. wall divergence of the solution (in r/theta form) per mode.
+  // G1. wall divergence of the (half-scale) solution, in r/theta form, per mode.
   if (tid < LM) {
     int mm = tid, k = k0 + mm;
     double2 dv = c2(0, 0);
     if (k < NTNZ) {
-      int it = k / NZ, l = k - it * NZ, m = it < NT / 2 ? it : it - NT;
-      double kt = tb.kts * (double)m, kz = tb.kzs * (double)l;
-      int tab = abs((abs(m) % 2) - 1);
+      double kt = skt[mm], kz = skz[mm];
+      int tab = 1 - spar[mm];
       const double* Dw = tb.D + tab * STEN * NR + STEN * (NR - 1) + IW;
       double sx = 0.0, sy = 0.0;
       double2 urw = c2(0, 0), utw = c2(0, 0);
@@ -309,7 +312,7 @@ __global__ void __launch_bounds__(NTH) linear_k(Tables tb, Bufs bf, Ctl* ctl) {
   }
   __syncthreads();
 
-  // G2. u += (-div_wall) V, back to r/theta, mode (0,0) constraints.
+  // G2. u += (-div_wall) V (both at half scale), back to full-scale r/theta, mode (0,0) constraints.
   for (int p = tid; p < LN; p += nth) {
     int i = p / LM, mm = p - i * LM, k = k0 + mm;
     if (k >= NTNZ) continue;
@@ -320,8 +323,9 @@ __global__ void __launch_bounds__(NTH) linear_k(Tables tb, Bufs bf, Ctl* ctl) {
     up.x += dv.x * v0.x - dv.y * v0.y; up.y += dv.x * v0.y + dv.y * v0.x;
     um.x += dv.x * v1.x - dv.y * v1.y; um.y += dv.x * v1.y + dv.y * v1.x;
     uz.x += dv.x * v2.x - dv.y * v2.y; uz.y += dv.x * v2.y + dv.y * v2.x;
-    double2 ur = c2(0.5 * (up.x + um.x), 0.5 * (up.y + um.y));
-    double2 ut = c2(0.5 * (up.y - um.y), -0.5 * (up.x - um.x));
+    double2 ur = c2(up.x + um.x, up.y + um.y);
+    double2 ut = c2(up.y - um.y, -(up.x - um.x));
+    uz = c2(uz.x + uz.x, uz.y + uz.y);
     if (k == 0) { ur = c2(0, 0); ut.y = 0.0; uz.y = 0.0; }
     R[p] = ur; R[LN + p] = ut; R[2 * LN + p] = uz;
   }
@@ -337,44 +341,45 @@ __global__ void __launch_bounds__(NTH) linear_k(Tables tb, Bufs bf, Ctl* ctl) {
   __syncthreads();
 
   // I. store the new iterate; corrector: convergence measure against the previous one.
-  double lnum = 0.0, lden = 0.0;
+  // The maxima of squared magnitudes (>= +0, or NaN) are taken on their bit patterns
+  // as unsigned integers, which order like the values, and the finiteness test reads
+  // the exponent field: both on the integer pipe.
+  unsigned long long lnum = 0ull, lden = 0ull;
   bool nonfin = false;
   for (int p = tid; p < LN; p += nth) {
     int i = p / LM, mm = p - i * LM, k = k0 + mm;
     if (k >= NTNZ) continue;
     size_t h = (size_t)i * NTNZ + k;
-    double n1 = 0.0, d1 = 0.0;
 #pragma unroll
     for (int c = 0; c < 3; c++) {
       double2 v = R[c * LN + p];
       if (!pred) {
         double2 o = Ui[c * S + h];
         double ex = o.x - v.x, ey = o.y - v.y;
-        n1 = fmax(n1, ex * ex + ey * ey);
-        d1 = fmax(d1, o.x * o.x + o.y * o.y);
+        lnum = max(lnum, (unsigned long long)__double_as_longlong(ex * ex + ey * ey));
+        lden = max(lden, (unsigned long long)__double_as_longlong(o.x * o.x + o.y * o.y));
       }
-      nonfin |= !(isfinite(v.x) && isfinite(v.y));
+      const unsigned EX = 0x7FF00000u;
+      nonfin |= ((unsigned)__double2hiint(v.x) & EX) == EX || ((unsigned)__double2hiint(v.y) & EX) == EX;
       Ui[c * S + h] = v;
       if (Ui32) Ui32[c * S + h] = make_float2((float)v.x, (float)v.y);
     }
-    lnum = fmax(lnum, n1);
-    lden = fmax(lden, d1);
   }
   if (nonfin) bad = 1;
   if (!pred) {
     for (int o = 16; o > 0; o >>= 1) {
-      lnum = fmax(lnum, __shfl_xor_sync(0xffffffffu, lnum, o));
-      lden = fmax(lden, __shfl_xor_sync(0xffffffffu, lden, o));
+      lnum = max(lnum, __shfl_xor_sync(0xffffffffu, lnum, o));
+      lden = max(lden, __shfl_xor_sync(0xffffffffu, lden, o));
     }
     if ((tid & 31) == 0) { wnum[tid >> 5] = lnum; wden[tid >> 5] = lden; }
   }
   __syncthreads();
   if (tid == 0) {
     if (!pred) {
-      double a = 0.0, b = 0.0;
-      for (int w = 0; w < nth / 32; w++) { a = fmax(a, wnum[w]); b = fmax(b, wden[w]); }
-      atomicMax(ctl->num + gm, (unsigned long long)__double_as_longlong(a));
-      atomicMax(ctl->den + gm, (unsigned long long)__double_as_longlong(b));
+      unsigned long long a = 0ull, b = 0ull;
+      for (int w = 0; w < nth / 32; w++) { a = max(a, wnum[w]); b = max(b, wden[w]); }
+      atomicMax(ctl->num + gm, a);
+      atomicMax(ctl->den + gm, b);
     }
     if (bad) atomicOr(ctl->status + gm, NSP_ERR_NONFINITE);
   }
@@ -456,7 +461,7 @@ __global__ void lusolve_k(Tables tb, int kind, const double2* rhs, double2* sol)
 }
 
 // Block shapes of the linear pass (modes per block, threads): the candidates of the
-// setup-time autotuner.  Shared memory per block is 6 radial lines per mode.
+// setup-time autotuner.  Shared memory per block is 4 radial lines per mode.
 struct LinShape { int LM, NTH; };
 static const LinShape kLinShapes[LIN_VARIANTS] = {{16, 256}, {8, 128}, {8, 256}, {4, 128},
                                                   {12, 192}, {12, 256}, {24, 384}, {32, 512}};
@@ -464,7 +469,7 @@ static const LinShape kLinShapes[LIN_VARIANTS] = {{16, 256}, {8, 128}, {8, 256},
 int linear_default_variant(int NR) { return NR <= 64 ? 0 : 2; }
 
 bool linear_variant_fits(int v, int NR) {
-  return v >= 0 && v < LIN_VARIANTS && sizeof(double2) * 6 * (size_t)NR * kLinShapes[v].LM <= 200 * 1024;
+  return v >= 0 && v < LIN_VARIANTS && sizeof(double2) * 4 * (size_t)NR * kLinShapes[v].LM <= 200 * 1024;
 }
 
 void configure_linear_kernels() {
@@ -483,7 +488,7 @@ void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st)
   int v = linear_variant_fits(tb.lin_variant, tb.NR) ? tb.lin_variant : linear_default_variant(tb.NR);
   const LinShape s = kLinShapes[v];
   dim3 grid((tb.NTNZ + s.LM - 1) / s.LM, tb.nmem);
-  size_t smem = sizeof(double2) * 6 * (size_t)tb.NR * s.LM;
+  size_t smem = sizeof(double2) * 4 * (size_t)tb.NR * s.LM;
   switch (v) {
     case 0: linear_k<16, 256><<<grid, 256, smem, st>>>(tb, bf, dctl); break;
     case 1: linear_k<8, 128><<<grid, 128, smem, st>>>(tb, bf, dctl); break;
