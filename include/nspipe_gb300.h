@@ -37,6 +37,8 @@ extern "C" {
 #define NSP_ERR_NONFINITE 4  /* a member's field became NaN/Inf during nsp_step    */
 #define NSP_ERR_STATE 5      /* call out of order (e.g. nsp_step before nsp_setup) */
 #define NSP_ERR_NOMEM 6      /* device allocation failed                           */
+#define NSP_ERR_DEVICE 7     /* a bounded device-side wait ran out (a tensor-core
+                                tile pipeline did not complete); results invalid   */
 
 #define NSP_FP64 0  /* plain form: every operation in FP64 (matches the reference)         */
 #define NSP_MIXED 1 /* transforms + nonlinear product in FP32; solves, BCs, state in FP64 */
@@ -146,6 +148,13 @@ int nsp_grid(nsp_ctx* ctx, int member, double* r, double* rdr);
 
 /* Number of kernel launches issued by the last nsp_step call (all graph nodes run). */
 long long nsp_kernel_launches(nsp_ctx* ctx);
+
+/* Introspection (no reference counterpart): writes a JSON object describing the
+ * context's execution choices -- precision, whether the step is a CUDA graph, and
+ * per member group its shape, member count, the autotuned linear-pass block
+ * (modes, threads) and the theta-transform path ("fft-fp64", "fft-fp32" or
+ * "tcgen05-3xtf32") -- into buf (NUL-terminated).  NSP_ERR_ARG if cap is too small. */
+int nsp_describe(nsp_ctx* ctx, char* buf, int cap);
 
 /* Makes the context launch its work on `stream` (a cudaStream_t of the context's
  * device); NULL restores the context's own stream.  The reference runs on the

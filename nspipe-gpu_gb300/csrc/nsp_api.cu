@@ -210,6 +210,18 @@ void tune_store(const std::map<std::string, int>& m) {
   fclose(f);
 }
 
+// A kernel whose bounded wait ran out sets Ctl::fault (and abandons its work).
+int check_fault(nsp_ctx* c) {
+  int fault = 0;
+  CK(cudaMemcpyAsync(&fault, &c->dctl->fault, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (fault) {
+    CK(cudaMemsetAsync(&c->dctl->fault, 0, sizeof(int), c->st));
+    return fail(c, NSP_ERR_DEVICE, "a device-side wait ran out; the call's results are invalid");
+  }
+  return NSP_OK;
+}
+
 int reset_control(nsp_ctx* c) {
   const int nm = c->nmem;
   std::vector<int> zeros(nm, 0);
@@ -466,12 +478,26 @@ int nsp_setup(nsp_ctx* c) {
     tb.Qdes = p.Qdes;
     tb.Qc = o.Qc;
     tb.inv_norm = 1.0 / ((double)tb.NTP * (double)tb.NZR);
+    // Mixed form: theta transforms as tensor-core DFT GEMMs where the length has a
+    // compiled tile shape (NSP_THETA_TC=0 keeps the FFT kernels).
+    int dev_sms = 0;
+    CK(cudaDeviceGetAttribute(&dev_sms, cudaDevAttrMultiProcessorCount, c->device));
+    tb.nsm = dev_sms;
+    tb.tc_theta = 0;
+    const char* te = getenv("NSP_THETA_TC");
+    if (c->precision == NSP_MIXED && theta_tc_supported(tb.NT, tb.NTP) && !(te && te[0] == '0')) {
+      if ((rc = upload(c, &tb.dft_inv, theta_dft_image(tb.NT, tb.NTP, true, 1.0))) ||
+          (rc = upload(c, &tb.dft_fwd, theta_dft_image(tb.NT, tb.NTP, false, tb.inv_norm))))
+        return rc;
+      tb.tc_theta = 1;
+    }
     // Release the large host tables; keep grid data for diagnostics.
     std::vector<double>().swap(o.fac);
     std::vector<double2>().swap(o.V);
   }
   configure_transform_kernels();
   configure_linear_kernels();
+  configure_theta_tc_kernels();
   CK(cudaGetLastError());
   if (int rc = autotune(c)) return rc;
   // NSP_GRAPH=0 selects the host-driven corrector loop (same kernels, one D2H flag
@@ -632,6 +658,7 @@ int nsp_step(nsp_ctx* c, int nsteps, int* iters_out) {
     done += chunk;
   }
   c->launches_last = launches;
+  if (int rc = check_fault(c)) return rc;
   std::vector<int> status(nm);
   CK(cudaMemcpy(status.data(), c->hctl.status, sizeof(int) * nm, cudaMemcpyDeviceToHost));
   for (int m = 0; m < nm; m++)
@@ -656,7 +683,7 @@ int nsp_nonlinear(nsp_ctx* c, int m, const void* ur, const void* ut, const void*
   CK(cudaGetLastError());
   for (int k = 0; k < 3; k++) CK(cudaMemcpyAsync(dst[k], out + k * S, bytes, cudaMemcpyDeviceToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
-  return NSP_OK;
+  return check_fault(c);
 }
 
 int nsp_nonlinear_static(nsp_ctx* c, int m, const void* u3, void* n3) {
@@ -741,6 +768,31 @@ int nsp_grid(nsp_ctx* c, int m, double* r, double* rdr) {
 }
 
 long long nsp_kernel_launches(nsp_ctx* c) { return c ? c->launches_last : 0; }
+
+int nsp_describe(nsp_ctx* c, char* buf, int cap) {
+  if (!c || !buf || cap <= 0) return NSP_ERR_ARG;
+  std::string s = "{\"precision\": \"";
+  s += c->precision == NSP_MIXED ? "mixed" : "fp64";
+  s += "\", \"graph\": ";
+  s += c->use_graph ? "true" : "false";
+  s += ", \"groups\": [";
+  for (size_t k = 0; k < c->groups.size(); k++) {
+    const Tables& tb = c->groups[k].tb;
+    int v = linear_variant_fits(tb.lin_variant, tb.NR) ? tb.lin_variant : linear_default_variant(tb.NR);
+    int LM = 0, NTH = 0;
+    linear_shape(v, &LM, &NTH);
+    char g[256];
+    snprintf(g, sizeof(g),
+             "%s{\"shape\": [%d, %d, %d], \"members\": %d, \"linear_block\": [%d, %d], \"theta\": \"%s\"}",
+             k ? ", " : "", tb.NR, tb.NT, tb.NZ, tb.nmem, LM, NTH,
+             c->precision != NSP_MIXED ? "fft-fp64" : (tb.tc_theta ? "tcgen05-3xtf32" : "fft-fp32"));
+    s += g;
+  }
+  s += "]}";
+  if ((int)s.size() + 1 > cap) return fail(c, NSP_ERR_ARG, "describe: buffer of %d bytes too small", cap);
+  memcpy(buf, s.c_str(), s.size() + 1);
+  return NSP_OK;
+}
 
 int nsp_set_stream(nsp_ctx* c, void* stream) {
   if (!c) return NSP_ERR_ARG;

@@ -48,11 +48,16 @@ struct Tables {
   const float2* tw_z32;
   FftPlan pt, pz;
   int lin_variant;     // block shape of the linear pass (autotuned at setup)
+  const float* dft_inv; // mixed form, tensor-core theta transforms: DFT-matrix operand images
+  const float* dft_fwd; //   ([hi | lo] x N x K core matrices, nsp_theta_tc.cu)
+  int tc_theta;        // 1: the mixed form's theta transforms run as tcgen05 GEMMs
+  int nsm;             // SM count (persistent grids)
 };
 
 constexpr int LIN_VARIANTS = 8;
 int linear_default_variant(int NR);
 bool linear_variant_fits(int v, int NR);
+void linear_shape(int v, int* LM, int* NTH);  // modes per block, threads of a variant
 
 // Batched per-group member buffers.
 struct Bufs {
@@ -81,6 +86,7 @@ struct Ctl {
   double* err;
   int* hist;           // [cap][nmem]: iterations of each step of the call
   int hist_cap;
+  int fault;           // nonzero: a device-side wait ran out and a kernel abandoned its work
 };
 
 // Kernel launchers (nsp_transform.cu, nsp_linear.cu).
@@ -99,6 +105,13 @@ cudaError_t noalloc_scratch(int device, void** ptr);
 // FP32 copy of nmem x 3 x S complex values (the mixed form's transform input).
 void launch_to_f32(const double2* src, float2* dst, long long n, cudaStream_t st);
 int kernels_per_nonlinear();
+// Tensor-core theta transforms (nsp_theta_tc.cu).
+bool theta_tc_supported(int NT, int NTP);
+std::vector<float> theta_dft_image(int NT, int NTP, bool inverse, double scale);
+void configure_theta_tc_kernels();
+// dir 0: inverse (u, d_r u, i m u / r -> G); dir 1: forward (H -> N).
+void launch_theta_tc(const Tables& tb, const Bufs& bf, Ctl* dctl, int dir, const double2* src, const float2* src32,
+                     double2* dst, cudaStream_t st);
 
 // Host-side operator construction (nsp_setup.cpp).
 struct HostOps {

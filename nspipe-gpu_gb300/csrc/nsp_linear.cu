@@ -468,6 +468,11 @@ static const LinShape kLinShapes[LIN_VARIANTS] = {{16, 256}, {8, 128}, {8, 256},
 
 int linear_default_variant(int NR) { return NR <= 64 ? 0 : 2; }
 
+void linear_shape(int v, int* LM, int* NTH) {
+  *LM = kLinShapes[v].LM;
+  *NTH = kLinShapes[v].NTH;
+}
+
 bool linear_variant_fits(int v, int NR) {
   return v >= 0 && v < LIN_VARIANTS && sizeof(double2) * 4 * (size_t)NR * kLinShapes[v].LM <= 200 * 1024;
 }

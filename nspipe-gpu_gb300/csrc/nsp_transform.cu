@@ -29,6 +29,7 @@
 
 #include "nsp_fft.cuh"
 #include "nsp_internal.h"
+#include "nsp_state.cuh"
 
 namespace nsp {
 
@@ -43,45 +44,6 @@ template <> __device__ __forceinline__ const float2* tw_t<float>(const Tables& t
 template <typename T> __device__ __forceinline__ const typename vec2<T>::type* tw_z(const Tables& tb);
 template <> __device__ __forceinline__ const double2* tw_z<double>(const Tables& tb) { return tb.tw_z; }
 template <> __device__ __forceinline__ const float2* tw_z<float>(const Tables& tb) { return tb.tw_z32; }
-
-// Source field of a member: the state in the predictor phase, the iterate in corrector phases.
-__device__ __forceinline__ const double2* member_source(const Tables& tb, const Bufs& bf, const Ctl* ctl, int mloc,
-                                                        const double2* src_override, bool& skip) {
-  skip = false;
-  if (src_override) return src_override;
-  int ph = ctl->phase[tb.mem0 + mloc];
-  if (ph < 0) { skip = true; return nullptr; }
-  int which = (ph == 0) ? ctl->parity : (ctl->parity ^ 1);
-  return bf.U[which] + (size_t)mloc * 3 * tb.S;
-}
-
-// Transform input in the working precision: the FP64 state, or its FP32 mirror.
-template <typename T> struct StateIn;
-template <> struct StateIn<double> {
-  const double2* p;
-  __device__ __forceinline__ cpx<double> ld(size_t h) const { double2 a = p[h]; return mk<double>(a.x, a.y); }
-};
-template <> struct StateIn<float> {
-  const float2* p;
-  __device__ __forceinline__ cpx<float> ld(size_t h) const { float2 a = __ldg(p + h); return mk<float>(a.x, a.y); }
-};
-template <typename T> __device__ __forceinline__ const T* dtab(const Tables& tb);
-template <> __device__ __forceinline__ const double* dtab<double>(const Tables& tb) { return tb.D; }
-template <> __device__ __forceinline__ const float* dtab<float>(const Tables& tb) { return tb.D32; }
-
-template <typename T>
-__device__ __forceinline__ StateIn<T> member_input(const Tables& tb, const Bufs& bf, const Ctl* ctl, int mloc,
-                                                  const double2* src, const float2* src32) {
-  StateIn<T> s;
-  int which = 0;
-  if (!src) {
-    int ph = ctl->phase[tb.mem0 + mloc];
-    which = (ph == 0) ? ctl->parity : (ctl->parity ^ 1);
-  }
-  if constexpr (sizeof(T) == 8) s.p = src ? src : bf.U[which] + (size_t)mloc * 3 * tb.S;
-  else s.p = src ? src32 : bf.U32[which] + (size_t)mloc * 3 * tb.S;
-  return s;
-}
 
 template <typename T, int NTPC>
 __device__ __forceinline__ void theta_fft(cpx<T>* buf, const Tables& tb, int sign) {
@@ -332,7 +294,10 @@ template <typename T>
 static void launch_nl_t(const Tables& tb, const Bufs& bf, Ctl* dctl, const double2* src, const float2* src32,
                         double2* dst, cudaStream_t st, int mask) {
   int nm = src ? 1 : tb.nmem;
-  if (mask & 1) {
+  const bool tc = sizeof(T) == 4 && tb.tc_theta;  // mixed form: theta transforms on the tensor cores
+  if ((mask & 1) && tc) {
+    launch_theta_tc(tb, bf, dctl, 0, src, src32, dst, st);
+  } else if (mask & 1) {
     switch (tb.NTP) {
 #define NSP_CASE_T(n) \
   case n: launch_theta<T, n>(tb, bf, dctl, src, src32, dst, st, 1, nm); break;
@@ -350,7 +315,9 @@ static void launch_nl_t(const Tables& tb, const Bufs& bf, Ctl* dctl, const doubl
       default: launch_z<T, 0, 1>(tb, bf, dctl, src != nullptr, st, nm);
     }
   }
-  if (mask & 4) {
+  if ((mask & 4) && tc) {
+    launch_theta_tc(tb, bf, dctl, 1, src, src32, dst, st);
+  } else if (mask & 4) {
     switch (tb.NTP) {
 #define NSP_CASE_T(n) \
   case n: launch_theta<T, n>(tb, bf, dctl, src, src32, dst, st, 4, nm); break;

@@ -7,6 +7,7 @@ reference's raw format, and the per-step entry points.  All numerics run in the
 CUDA library; if it is missing this module raises instead of falling back.
 """
 import ctypes
+import json
 import os
 
 import numpy as np
@@ -16,7 +17,7 @@ from .initfield import PI2, radial_grid, read_state, seeded_field, write_state  
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(os.path.dirname(_HERE), "libnspipe_gb300.so")
 
-NSP_OK, NSP_ERR_ARG, NSP_ERR_CUDA, NSP_ERR_IO, NSP_ERR_NONFINITE, NSP_ERR_STATE, NSP_ERR_NOMEM = range(7)
+NSP_OK, NSP_ERR_ARG, NSP_ERR_CUDA, NSP_ERR_IO, NSP_ERR_NONFINITE, NSP_ERR_STATE, NSP_ERR_NOMEM, NSP_ERR_DEVICE = range(8)
 NSP_FP64, NSP_MIXED = 0, 1
 
 EXPORTS = [
@@ -24,7 +25,7 @@ EXPORTS = [
     "nsp_set_state_host", "nsp_get_state_host", "nsp_set_state_device", "nsp_get_state_device",
     "nsp_step", "nsp_nonlinear", "nsp_lusolve", "nsp_diag", "nsp_grid", "nsp_kernel_launches",
     "nsp_sync", "nsp_last_error", "nsp_destroy", "nsp_set_stream", "nsp_profile_stages",
-    "nsp_measure_fp64_peak", "nsp_nonlinear_static",
+    "nsp_measure_fp64_peak", "nsp_nonlinear_static", "nsp_describe",
 ]
 
 
@@ -83,6 +84,7 @@ def lib():
         L.nsp_profile_stages.argtypes = [vp, ip, dp]
         L.nsp_measure_fp64_peak.argtypes = [vp, dp]
         L.nsp_nonlinear_static.argtypes = [vp, ip, vp, vp]
+        L.nsp_describe.argtypes = [vp, ctypes.c_char_p, ip]
         L.nsp_last_error.argtypes = [vp]
         L.nsp_last_error.restype = ctypes.c_char_p
         L.nsp_destroy.argtypes = [vp]
@@ -215,6 +217,12 @@ class Stepper:
 
     def kernel_launches(self):
         return lib().nsp_kernel_launches(self._h)
+
+    def describe(self):
+        """Execution choices of the context (precision, graph, per-group block shape, theta path)."""
+        buf = ctypes.create_string_buffer(4096)
+        self._check(lib().nsp_describe(self._h, buf, len(buf)))
+        return json.loads(buf.value.decode())
 
     def nonlinear(self, m, u_dev, n_dev):
         self._check(lib().nsp_nonlinear(self._h, m, *[_ptr(a) for a in u_dev], *[_ptr(a) for a in n_dev]))

@@ -1,0 +1,102 @@
+"""Tensor-core theta transforms of the mixed form (tcgen05 kind::tf32, 3xTF32 split,
+accumulators in TMEM): path selection, agreement with the FP32 FFT kernels and
+with the FP64 oracle, and the mixed-form accuracy gate after 50 and 100 steps
+against the reference build's golden fixture (velocity relative L2 <= 1e-6,
+mean profile <= 1e-4) and after 500 steps against the plain FP64 form.
+"""
+import numpy as np
+import pytest
+
+from conftest import rel
+from test_gpu_parity import CFG, dev, golden, init, nsp, orc, stepper  # noqa: F401  (fixtures)
+
+pytestmark = pytest.mark.gpu
+
+
+def test_theta_path_selection(nsp, monkeypatch):
+    monkeypatch.delenv("NSP_THETA_TC", raising=False)
+    st = stepper(nsp, "c0", nsp.NSP_MIXED)
+    d = st.describe()
+    assert d["precision"] == "mixed"
+    assert d["groups"][0]["theta"] == "tcgen05-3xtf32"
+    st.close()
+    st = stepper(nsp, "c0", nsp.NSP_FP64)
+    assert st.describe()["groups"][0]["theta"] == "fft-fp64"
+    st.close()
+    # lengths without a compiled tile shape keep the FFT kernels
+    st = stepper(nsp, "s2", nsp.NSP_MIXED)
+    assert st.describe()["groups"][0]["theta"] == "fft-fp32"
+    st.close()
+
+
+def test_theta_tc_matches_fft_and_oracle(nsp, orc, monkeypatch):
+    import torch
+    o = orc("c0")
+    u0 = init(nsp, "c0")
+    ref = o.nonlinear(u0)
+    out = {}
+    for mode, path in (("1", "tcgen05-3xtf32"), ("0", "fft-fp32")):
+        monkeypatch.setenv("NSP_THETA_TC", mode)
+        st = stepper(nsp, "c0", nsp.NSP_MIXED)
+        assert st.describe()["groups"][0]["theta"] == path
+        n = [torch.zeros(o.shape, dtype=torch.complex128, device="cuda") for _ in range(3)]
+        st.nonlinear(0, [dev(a) for a in u0], n)
+        out[mode] = [x.cpu().numpy() for x in n]
+        st.close()
+    for c in range(3):
+        assert rel(out["1"][c], ref[c]) < 2e-6, c
+        assert rel(out["1"][c], out["0"][c]) < 2e-6, c
+
+
+def test_theta_tc_ensemble_matches_single_members(nsp):
+    """The persistent tile loop spreads an ensemble's tiles over the CTAs; each
+    member still gets bit-for-bit the result of stepping it alone."""
+    M, nsteps = 3, 3
+    fields = [init(nsp, "c0", m) for m in range(M)]
+    st = stepper(nsp, "c0", nsp.NSP_MIXED, members=M)
+    for m in range(M):
+        st.set_state(m, fields[m])
+    st.step(nsteps)
+    ens = [np.stack(st.get_state(m)) for m in range(M)]
+    st.close()
+    for m in range(M):
+        one = stepper(nsp, "c0", nsp.NSP_MIXED)
+        one.set_state(0, fields[m])
+        one.step(nsteps)
+        assert np.array_equal(np.stack(one.get_state(0)), ens[m]), m
+        one.close()
+
+
+def _low(u, NT):
+    m_slots = [0, 1, 2, 3, 4, NT - 4, NT - 3, NT - 2, NT - 1]
+    return np.stack([a[:, m_slots, :6] for a in u])
+
+
+def test_mixed_gate_vs_reference_build_c0(nsp):
+    g = golden("c0")
+    NT = CFG["c0"][1]
+    st = stepper(nsp, "c0", nsp.NSP_MIXED)
+    assert st.describe()["groups"][0]["theta"] == "tcgen05-3xtf32"
+    st.set_state(0, init(nsp, "c0"))
+    done = 0
+    for s in (50, 100):
+        st.step(s - done)
+        done = s
+        u = st.get_state(0)
+        assert rel(_low(u, NT), g["low_%d" % s]) < 1e-6, s
+        assert rel(u[2][:, 0, 0], g["mean_%d" % s]) < 1e-4, s
+        norms = np.array([np.linalg.norm(a) for a in u])
+        assert np.all(np.abs(norms - g["norm_%d" % s]) <= 1e-6 * g["norm_%d" % s]), s
+    st.close()
+
+
+def test_mixed_500_steps_vs_fp64_form(nsp):
+    u0 = init(nsp, "c0")
+    res = {}
+    for prec in (nsp.NSP_FP64, nsp.NSP_MIXED):
+        st = stepper(nsp, "c0", prec)
+        st.set_state(0, u0)
+        st.step(500)
+        res[prec] = np.stack(st.get_state(0))
+        st.close()
+    assert rel(res[nsp.NSP_MIXED], res[nsp.NSP_FP64]) < 1e-6
