@@ -14,7 +14,8 @@
 
 namespace nsp {
 
-template <typename T> struct cpx { T x, y; };
+// Aligned to its full size so that loads and stores of a complex value are single vector accesses.
+template <typename T> struct alignas(2 * sizeof(T)) cpx { T x, y; };
 template <typename T> struct vec2;
 template <> struct vec2<double> { using type = double2; };
 template <> struct vec2<float> { using type = float2; };

@@ -25,7 +25,9 @@
 // back in FP64).  Transform lengths used by the supported configurations are
 // compile-time template arguments (all index arithmetic by constants); other
 // 2^a 3^b lengths use the run-time FFT.
+#include <cmath>
 #include <cstdio>
+#include <cstdlib>
 
 #include "nsp_fft.cuh"
 #include "nsp_internal.h"
@@ -214,6 +216,198 @@ __global__ void __launch_bounds__(ZTH) nl_z(Tables tb, Bufs bf, const Ctl* ctl, 
   }
 }
 
+// ---------------------------------------------------------------- z stage, two-pass
+// The same z stage with each length-NZR transform split as NZR = N1 x N2 ("four-step"):
+//   X[N2 k1 + k2] = sum_n1 w_N1^(n1 k1) [ w_NZR^(n1 k2) sum_n2 x[n1 + N1 n2] w_N2^(n2 k2) ],
+// pass A: one thread per (transform, n1) runs the N2-point DFT in registers and
+// applies the twiddle; pass B: one thread per (transform, k2) runs the N1-point DFT.
+// Between the passes a padded [k2][n1] transpose buffer keeps shared memory free of
+// bank conflicts; pass A of the inverse gathers the Hermitian spectra straight from
+// G.  Two shared-memory round trips per transform instead of one per radix stage.
+
+// exp(-2 pi i e / 96): every register sub-transform length used (4 .. 32) divides 96.
+__constant__ float2 c_w96f[96];
+__constant__ double2 c_w96d[96];
+template <typename T> __device__ __forceinline__ cpx<T> w96(int e);
+template <> __device__ __forceinline__ cpx<float> w96<float>(int e) { float2 w = c_w96f[e]; return mk<float>(w.x, w.y); }
+template <> __device__ __forceinline__ cpx<double> w96<double>(int e) { double2 w = c_w96d[e]; return mk<double>(w.x, w.y); }
+
+// In-register Stockham FFT of length N | 96 (every index a compile-time constant
+// once unrolled, so the array stays in registers); natural order in and out.
+template <typename T, int SIGN, int N, int S = 0, int NS = 1>
+__device__ __forceinline__ void reg_fft(cpx<T>* v) {
+  if constexpr (S < ct_nstages(N)) {
+    constexpr int P = ct_radix(N, S), NB = N / P;
+    static_assert(96 % (NS * P) == 0, "sub-transform length must divide 96");
+    cpx<T> o[N];
+#pragma unroll
+    for (int j = 0; j < NB; j++) {
+      const int k = j % NS;
+      cpx<T> x[P];
+#pragma unroll
+      for (int q = 0; q < P; q++) x[q] = v[j + q * NB];
+      if (NS > 1 && k > 0) {
+#pragma unroll
+        for (int q = 1; q < P; q++) {
+          const cpx<T> w = w96<T>((q * k * (96 / (NS * P))) % 96);
+          x[q] = cmulv(x[q], mk<T>(w.x, SIGN > 0 ? -w.y : w.y));
+        }
+      }
+      dft<T, SIGN, P>(x);
+#pragma unroll
+      for (int q = 0; q < P; q++) o[(j / NS) * NS * P + k + q * NS] = x[q];
+    }
+#pragma unroll
+    for (int n = 0; n < N; n++) v[n] = o[n];
+    reg_fft<T, SIGN, N, S + 1, NS * P>(v);
+  }
+}
+
+// Spectrum value n (0 <= n < NZR) of a packed pair of fields, Hermitian-extended:
+// Ga / Gb are the fields' columns (d_z fields read the u columns and multiply by i k_z).
+template <typename T>
+__device__ __forceinline__ cpx<T> z_pair_spec(const cpx<T>* Ga, const cpx<T>* Gb, bool dza, bool dzb, int n, int NZ,
+                                              int NZR, T kzs) {
+  int qq;
+  bool cj = false;
+  if (n < NZ) qq = n;
+  else if (n > NZR - NZ) { qq = NZR - n; cj = true; }
+  else return mk<T>(0, 0);
+  cpx<T> a = Ga[qq], b = Gb[qq];
+  const T kz = kzs * (T)qq;
+  if (dza) a = mk<T>(-kz * a.y, kz * a.x);
+  if (dzb) b = mk<T>(-kz * b.y, kz * b.x);
+  if (qq == 0) { a.y = (T)0; b.y = (T)0; }  // C2R ignores Im of the k_z = 0 coefficient
+  if (cj) { a.y = -a.y; b.y = -b.y; }
+  return mk<T>(a.x - b.y, a.y + b.x);
+}
+
+template <typename T, int NZRC, int N1, int N2, int R>
+__global__ void __launch_bounds__(ZTH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl, int standalone) {
+  static_assert(N1 * N2 == NZRC && R % 2 == 0, "z split");
+  constexpr int YP = N1 + 1;          // padded transpose row
+  constexpr int YT = N2 * YP;         // one transform in the transpose buffer
+  constexpr int PS = NZRC + 4;        // padded physical field row
+  constexpr int NF = R + R / 2;       // forward transforms: (N_r, N_t) per row, (N_z, N_z) per row pair
+  const int mloc = blockIdx.z, i = blockIdx.y, j0 = blockIdx.x * R;
+  if (!standalone && ctl->phase[tb.mem0 + mloc] < 0) return;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  cpx<T>* Y = reinterpret_cast<cpx<T>*>(smraw);  // [R*6][N2][N1+1]
+  T* Ph = reinterpret_cast<T*>(Y + R * 6 * YT);  // [R][12][PS] physical fields, then products
+  const int NR = tb.NR, NZ = tb.NZ, NTP = tb.NTP;
+  const cpx<T>* G = reinterpret_cast<const cpx<T>*>(bf.G) + (size_t)mloc * 9 * NR * NTP * NZ;
+  cpx<T>* H = reinterpret_cast<cpx<T>*>(bf.H) + (size_t)mloc * 3 * NR * NTP * NZ;
+  const T kzs = (T)tb.kzs;
+  const auto* twz = tw_z<T>(tb);  // exp(-2 pi i e / NZR)
+  const size_t fstride = (size_t)NR * NTP * NZ;
+
+  // 1. inverse, pass A (spectra gathered from G)
+  for (int task = threadIdx.x; task < R * 6 * N1; task += ZTH) {
+    const int n1 = task % N1, t = (task / N1) % 6, r = task / (6 * N1), j = j0 + r;
+    cpx<T> x[N2];
+    const cpx<T>* Gi = G + ((size_t)i * NTP + (j < NTP ? j : 0)) * NZ;
+    const int fa = 2 * t, fb = 2 * t + 1;  // d_z u_c (fields 9-11) comes from the u_c columns
+    const cpx<T>* Ga = Gi + (size_t)(fa < 9 ? fa : fa - 9) * fstride;
+    const cpx<T>* Gb = Gi + (size_t)(fb < 9 ? fb : fb - 9) * fstride;
+#pragma unroll
+    for (int n2 = 0; n2 < N2; n2++)
+      x[n2] = j < NTP ? z_pair_spec<T>(Ga, Gb, fa >= 9, fb >= 9, n1 + N1 * n2, NZ, NZRC, kzs) : mk<T>(0, 0);
+    reg_fft<T, +1, N2>(x);
+    cpx<T>* Yt = Y + (r * 6 + t) * YT + n1;
+#pragma unroll
+    for (int k2 = 0; k2 < N2; k2++) {
+      cpx<T> v = x[k2];
+      if (k2 > 0) {
+        const auto w = __ldg(twz + n1 * k2);
+        v = cmulv(v, mk<T>(w.x, -w.y));
+      }
+      Yt[k2 * YP] = v;
+    }
+  }
+  __syncthreads();
+  // 2. inverse, pass B -> physical point z = N2 k1 + k2 of fields (2t, 2t+1)
+  for (int task = threadIdx.x; task < R * 6 * N2; task += ZTH) {
+    const int k2 = task % N2, t = (task / N2) % 6, r = task / (6 * N2);
+    cpx<T> y[N1];
+    const cpx<T>* Yt = Y + (r * 6 + t) * YT + k2 * YP;
+#pragma unroll
+    for (int n1 = 0; n1 < N1; n1++) y[n1] = Yt[n1];
+    reg_fft<T, +1, N1>(y);
+    T* pa = Ph + (r * 12 + 2 * t) * PS + k2;
+#pragma unroll
+    for (int k1 = 0; k1 < N1; k1++) {
+      pa[N2 * k1] = y[k1].x;
+      pa[PS + N2 * k1] = y[k1].y;
+    }
+  }
+  __syncthreads();
+  // 3. -(u.grad)u (calcNonlinear_k, mod_io_nonlinear.cu:142-170), in place in fields 0-2.
+  // Field order: u_r,u_t,u_z, dr u_r,dr u_t,dr u_z, dt u_r,dt u_t,dt u_z, dz u_r,dz u_t,dz u_z.
+  const T rinv = (T)tb.rinv[i];
+  for (int task = threadIdx.x; task < R * NZRC; task += ZTH) {
+    const int z = task % NZRC, r = task / NZRC;
+    T* p = Ph + r * 12 * PS + z;
+    const T ur = p[0], ut = p[PS], uz = p[2 * PS];
+    const T drr = p[3 * PS], drt = p[4 * PS], drz = p[5 * PS];
+    const T dtr = p[6 * PS], dtt = p[7 * PS], dtz = p[8 * PS];
+    const T dzr = p[9 * PS], dzt = p[10 * PS], dzz = p[11 * PS];
+    const T utr = ut * rinv;
+    p[0] = -(ur * drr + ut * dtr + uz * dzr - ut * utr);
+    p[PS] = -(ur * drt + ut * dtt + uz * dzt + ur * utr);
+    p[2 * PS] = -(ur * drz + ut * dtz + uz * dzz);
+  }
+  __syncthreads();
+  // 4. forward, pass A: transform t < R packs (N_r, N_t) of row t; t >= R packs N_z of rows 2(t-R), 2(t-R)+1.
+  for (int task = threadIdx.x; task < NF * N1; task += ZTH) {
+    const int n1 = task % N1, t = task / N1;
+    const T* pa;
+    const T* pb;
+    if (t < R) { pa = Ph + t * 12 * PS; pb = pa + PS; }
+    else { pa = Ph + (2 * (t - R) * 12 + 2) * PS; pb = pa + 12 * PS; }
+    cpx<T> x[N2];
+#pragma unroll
+    for (int n2 = 0; n2 < N2; n2++) x[n2] = mk<T>(pa[n1 + N1 * n2], pb[n1 + N1 * n2]);
+    reg_fft<T, -1, N2>(x);
+    cpx<T>* Yt = Y + t * YT + n1;
+#pragma unroll
+    for (int k2 = 0; k2 < N2; k2++) {
+      cpx<T> v = x[k2];
+      if (k2 > 0) {
+        const auto w = __ldg(twz + n1 * k2);
+        v = cmulv(v, mk<T>(w.x, w.y));
+      }
+      Yt[k2 * YP] = v;
+    }
+  }
+  __syncthreads();
+  // 5. forward, pass B -> spectrum X[N2 k1 + k2] (natural order, over the physical buffer)
+  cpx<T>* Xs = reinterpret_cast<cpx<T>*>(Ph);
+  for (int task = threadIdx.x; task < NF * N2; task += ZTH) {
+    const int k2 = task % N2, t = task / N2;
+    cpx<T> y[N1];
+    const cpx<T>* Yt = Y + t * YT + k2 * YP;
+#pragma unroll
+    for (int n1 = 0; n1 < N1; n1++) y[n1] = Yt[n1];
+    reg_fft<T, -1, N1>(y);
+#pragma unroll
+    for (int k1 = 0; k1 < N1; k1++) Xs[t * NZRC + N2 * k1 + k2] = y[k1];
+  }
+  __syncthreads();
+  // 6. unpack x = a + i b: A_q = (X_q + conj X_-q)/2, B_q = (X_q - conj X_-q)/(2i); keep q < NZ-1.
+  const int NQ = NZ - 1;
+  for (int task = threadIdx.x; task < R * 3 * NQ; task += ZTH) {
+    const int q = task % NQ, c = (task / NQ) % 3, r = task / (3 * NQ), j = j0 + r;
+    if (j >= NTP) continue;
+    const int slot = c < 2 ? r : R + r / 2;
+    const bool takeB = c < 2 ? (c == 1) : (r & 1);
+    const cpx<T>* X = Xs + slot * NZRC;
+    const cpx<T> xq = X[q], xm = X[(NZRC - q) % NZRC];
+    const cpx<T> v = takeB ? mk<T>((T)0.5 * (xq.y + xm.y), (T)-0.5 * (xq.x - xm.x))
+                           : mk<T>((T)0.5 * (xq.x + xm.x), (T)0.5 * (xq.y - xm.y));
+    H[(((size_t)c * NR + i) * NTP + j) * NZ + q] = v;
+  }
+}
+
 // ---------------------------------------------------------------- theta forward
 template <typename T, int NTPC>
 __global__ void __launch_bounds__(TTH) nl_theta_fwd(Tables tb, Bufs bf, const Ctl* ctl, const double2* src_override,
@@ -287,8 +481,25 @@ static void launch_z(const Tables& tb, const Bufs& bf, Ctl* dctl, bool standalon
   nl_z<T, NZRC, RPB><<<g, ZTH, sm, st>>>(tb, bf, dctl, standalone ? 1 : 0);
 }
 
+static bool z2_enabled();
+
+template <typename T, int NZRC, int N1, int N2, int R>
+static constexpr size_t z2_smem() {
+  return sizeof(cpx<T>) * R * 6 * N2 * (N1 + 1) + sizeof(T) * R * 12 * (NZRC + 4);
+}
+
+template <typename T, int NZRC, int N1, int N2, int R>
+static void launch_z2(const Tables& tb, const Bufs& bf, Ctl* dctl, bool standalone, cudaStream_t st, int nm) {
+  dim3 g((tb.NTP + R - 1) / R, tb.NR, nm);
+  nl_z2<T, NZRC, N1, N2, R><<<g, ZTH, z2_smem<T, NZRC, N1, N2, R>(), st>>>(tb, bf, dctl, standalone ? 1 : 0);
+}
+
 #define NSP_NTP_LIST(X) X(12) X(24) X(48) X(72) X(96) X(144) X(192)
 #define NSP_NZR_LIST(X) X(24, 2) X(48, 2) X(96, 2) X(192, 2) X(384, 2) X(576, 1) X(768, 1)
+// Two-pass z stage: (NZR, N1, N2, rows per block) for FP32 and FP64.
+#define NSP_Z2_LIST_F(X) X(24, 4, 6, 2) X(48, 8, 6, 2) X(96, 8, 12, 2) X(192, 16, 12, 2) X(384, 16, 24, 2) \
+  X(576, 24, 24, 2) X(768, 32, 24, 2)
+#define NSP_Z2_LIST_D(X) X(24, 4, 6, 2) X(48, 8, 6, 2) X(96, 8, 12, 2) X(192, 16, 12, 2) X(384, 16, 24, 2)
 
 template <typename T>
 static void launch_nl_t(const Tables& tb, const Bufs& bf, Ctl* dctl, const double2* src, const float2* src32,
@@ -307,12 +518,25 @@ static void launch_nl_t(const Tables& tb, const Bufs& bf, Ctl* dctl, const doubl
     }
   }
   if (mask & 2) {
-    switch (tb.NZR) {
+    bool done = false;
+    if (z2_enabled()) {
+      if constexpr (sizeof(T) == 4) {
+#define NSP_CASE_Z2(n, a, b, r) \
+  if (!done && tb.NZR == n) { launch_z2<T, n, a, b, r>(tb, bf, dctl, src != nullptr, st, nm); done = true; }
+        NSP_Z2_LIST_F(NSP_CASE_Z2)
+      } else {
+        NSP_Z2_LIST_D(NSP_CASE_Z2)
+#undef NSP_CASE_Z2
+      }
+    }
+    if (!done) {
+      switch (tb.NZR) {
 #define NSP_CASE_Z(n, r) \
   case n: launch_z<T, n, r>(tb, bf, dctl, src != nullptr, st, nm); break;
-      NSP_NZR_LIST(NSP_CASE_Z)
+        NSP_NZR_LIST(NSP_CASE_Z)
 #undef NSP_CASE_Z
-      default: launch_z<T, 0, 1>(tb, bf, dctl, src != nullptr, st, nm);
+        default: launch_z<T, 0, 1>(tb, bf, dctl, src != nullptr, st, nm);
+      }
     }
   }
   if ((mask & 4) && tc) {
@@ -345,9 +569,35 @@ static void configure_t() {
 #undef NSP_CFG_Z
 }
 
+// NSP_Z2=0 keeps the radix-stage z kernels (for comparisons).
+static bool g_z2 = true;
+static bool z2_enabled() { return g_z2; }
+
 void configure_transform_kernels() {
   configure_t<double>();
   configure_t<float>();
+#define NSP_CFG_Z2F(n, a, b, r)                                                          \
+  cudaFuncSetAttribute(nl_z2<float, n, a, b, r>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                       (int)z2_smem<float, n, a, b, r>());
+#define NSP_CFG_Z2D(n, a, b, r)                                                            \
+  cudaFuncSetAttribute(nl_z2<double, n, a, b, r>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                       (int)z2_smem<double, n, a, b, r>());
+  NSP_Z2_LIST_F(NSP_CFG_Z2F)
+  NSP_Z2_LIST_D(NSP_CFG_Z2D)
+#undef NSP_CFG_Z2F
+#undef NSP_CFG_Z2D
+  // Twiddles of the register sub-transforms, exp(-2 pi i e / 96), from long double.
+  float2 wf[96];
+  double2 wd[96];
+  for (int e = 0; e < 96; e++) {
+    const long double a = -6.283185307179586476925286766559L * (long double)e / 96.0L;
+    wd[e] = make_double2((double)cosl(a), (double)sinl(a));
+    wf[e] = make_float2((float)cosl(a), (float)sinl(a));
+  }
+  cudaMemcpyToSymbol(c_w96f, wf, sizeof(wf));
+  cudaMemcpyToSymbol(c_w96d, wd, sizeof(wd));
+  const char* e = getenv("NSP_Z2");
+  g_z2 = !(e && e[0] == '0');
 }
 
 bool transform_supported(int NTP, int NZR) {
