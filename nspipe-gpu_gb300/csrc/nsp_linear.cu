@@ -26,34 +26,45 @@ namespace nsp {
 
 __device__ __forceinline__ double2 c2(double x, double y) { return make_double2(x, y); }
 
+// x -= l * y for a complex line value (both parts) or one real part of it.
+__device__ __forceinline__ void fms(double2& x, double l, const double2& y) { x.x -= l * y.x; x.y -= l * y.y; }
+__device__ __forceinline__ void fms(double& x, double l, const double& y) { x -= l * y; }
+__device__ __forceinline__ void scale(double2& x, double u) { x.x *= u; x.y *= u; }
+__device__ __forceinline__ void scale(double& x, double u) { x *= u; }
+
 // One forward-substitution row: x -= L(i-3) x_{i-3} + L(i-2) x_{i-2} + L(i-1) x_{i-1},
 // in the reference's column order.  Factors of columns outside the band are stored
 // as 0 (and the carried x start at 0), so edge rows need no branches.
-__device__ __forceinline__ void fwd_row(double2& x, const double* l, double2& xm1, double2& xm2, double2& xm3) {
-  x.x -= l[0] * xm3.x; x.y -= l[0] * xm3.y;
-  x.x -= l[1] * xm2.x; x.y -= l[1] * xm2.y;
-  x.x -= l[2] * xm1.x; x.y -= l[2] * xm1.y;
+template <typename V>
+__device__ __forceinline__ void fwd_row(V& x, const double* l, V& xm1, V& xm2, V& xm3) {
+  fms(x, l[0], xm3);
+  fms(x, l[1], xm2);
+  fms(x, l[2], xm1);
   xm3 = xm2; xm2 = xm1; xm1 = x;
 }
 // One backward row, farther neighbours first so that only one multiply-add and the
 // pivot multiply wait on the row just finished: x = (x - U3 x3 - U2 x2 - U1 x1) / U_ii.
-__device__ __forceinline__ void bwd_row(double2& x, const double* u, double2& xp1, double2& xp2, double2& xp3) {
-  x.x -= u[0] * xp3.x; x.y -= u[0] * xp3.y;
-  x.x -= u[1] * xp2.x; x.y -= u[1] * xp2.y;
-  x.x -= u[2] * xp1.x; x.y -= u[2] * xp1.y;
-  x.x *= u[3]; x.y *= u[3];
+template <typename V>
+__device__ __forceinline__ void bwd_row(V& x, const double* u, V& xp1, V& xp2, V& xp3) {
+  fms(x, u[0], xp3);
+  fms(x, u[1], xp2);
+  fms(x, u[2], xp1);
+  scale(x, u[3]);
   xp3 = xp2; xp2 = xp1; xp1 = x;
 }
 
-// Forward + backward substitution of one mode line held in X[i*ld] (i = 0..NR-1).
-// Factor rows are fetched four at a time so that their L2 latencies overlap.
-__device__ __forceinline__ void solve_line(double2* X, int ld, const double* __restrict__ f, int NTNZ, int NR) {
+// Forward + backward substitution of one mode line held in X[i*ld] (i = 0..NR-1):
+// V = double2 solves the complex line, V = double one of its parts (the factors are
+// real, so the real and imaginary parts are independent solves and two threads can
+// share a line).  Factor rows are fetched four at a time so that their L2 latencies overlap.
+template <typename V>
+__device__ __forceinline__ void solve_line(V* X, int ld, const double* __restrict__ f, int NTNZ, int NR) {
   const size_t rs = (size_t)NFAC * NTNZ;  // row stride of the factor table
-  double2 xm1 = c2(0, 0), xm2 = c2(0, 0), xm3 = c2(0, 0);
+  V xm1{}, xm2{}, xm3{};
   int i = 0;
   for (; i + 4 <= NR; i += 4) {
     double l[4][3];
-    double2 b[4];
+    V b[4];
 #pragma unroll
     for (int r = 0; r < 4; r++) {
       const double* fr = f + (i + r) * rs;
@@ -69,15 +80,15 @@ __device__ __forceinline__ void solve_line(double2* X, int ld, const double* __r
   for (; i < NR; i++) {
     const double* fr = f + i * rs;
     double l[3] = {__ldg(fr), __ldg(fr + NTNZ), __ldg(fr + 2 * NTNZ)};
-    double2 x = X[i * ld];
+    V x = X[i * ld];
     fwd_row(x, l, xm1, xm2, xm3);
     X[i * ld] = x;
   }
-  double2 xp1 = c2(0, 0), xp2 = c2(0, 0), xp3 = c2(0, 0);
+  V xp1{}, xp2{}, xp3{};
   i = NR - 1;
   for (; i >= 3; i -= 4) {
     double u[4][4];
-    double2 b[4];
+    V b[4];
 #pragma unroll
     for (int r = 0; r < 4; r++) {
       const double* fr = f + (i - r) * rs;
@@ -94,7 +105,7 @@ __device__ __forceinline__ void solve_line(double2* X, int ld, const double* __r
   for (; i >= 0; i--) {
     const double* fr = f + i * rs;
     double u[4] = {__ldg(fr + 6 * NTNZ), __ldg(fr + 5 * NTNZ), __ldg(fr + 4 * NTNZ), __ldg(fr + 3 * NTNZ)};
-    double2 x = X[i * ld];
+    V x = X[i * ld];
     bwd_row(x, u, xp1, xp2, xp3);
     X[i * ld] = x;
   }
@@ -243,7 +254,13 @@ __global__ void __launch_bounds__(NTH, (1024 / NTH) < 2 ? 2 : (1024 / NTH)) line
   __syncthreads();
 
   // D. pressure Poisson solve, one thread per mode.
-  if (tid < LM && k0 + tid < NTNZ) solve_line(P + tid, LM, tb.fac + 3 * (size_t)NR * NFAC * NTNZ + k0 + tid, NTNZ, NR);
+  // (two threads per mode line: real and imaginary parts; every lane of the warp busy)
+  if (tid < 2 * LM) {
+    const int mm = tid >> 1, part = tid & 1;
+    if (k0 + mm < NTNZ)
+      solve_line(reinterpret_cast<double*>(P + mm) + part, 2 * LM, tb.fac + 3 * (size_t)NR * NFAC * NTNZ + k0 + mm,
+                 NTNZ, NR);
+  }
   __syncthreads();
 
   // E. rhs -= grad p, r/theta -> +/-, wall rows = 0.
@@ -256,17 +273,16 @@ __global__ void __launch_bounds__(NTH, (1024 / NTH) < 2 ? 2 : (1024 / NTH)) line
       int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
       int tab = spar[mm];
       const double* Dr = tb.D + tab * STEN * NR + STEN * i + i0;
-      double sx = 0.0, sy = 0.0;
+      double2 rr = R[p];  // rr - d_r p, accumulated straight into the multiply-adds
       for (int j = 0; j < len; j++) {
         double de = __ldg(Dr + j);
         double2 a = P[(left + j) * LM + mm];
-        sx += de * a.x;
-        sy += de * a.y;
+        rr.x -= de * a.x;
+        rr.y -= de * a.y;
       }
       double kti = kt * tb.rinv[i];
-      double2 pp = P[p], rr = R[p], rt = R[LN + p];
+      double2 pp = P[p], rt = R[LN + p];
       rz = R[2 * LN + p];
-      rr.x -= sx; rr.y -= sy;
       rt.x += kti * pp.y; rt.y -= kti * pp.x;
       rz.x += kz * pp.y; rz.y -= kz * pp.x;
       up = c2(rr.x - rt.y, rr.y + rt.x);
@@ -277,9 +293,11 @@ __global__ void __launch_bounds__(NTH, (1024 / NTH) < 2 ? 2 : (1024 / NTH)) line
   __syncthreads();
 
   // F. Helmholtz solves for u+, u-, u_z.
-  if (tid < 3 * LM) {
-    int c = tid / LM, mm = tid - c * LM;
-    if (k0 + mm < NTNZ) solve_line(R + c * LN + mm, LM, tb.fac + (size_t)c * NR * NFAC * NTNZ + k0 + mm, NTNZ, NR);
+  if (tid < 6 * LM) {
+    const int c = tid / (2 * LM), rem = tid - c * 2 * LM, mm = rem >> 1, part = rem & 1;
+    if (k0 + mm < NTNZ)
+      solve_line(reinterpret_cast<double*>(R + c * LN + mm) + part, 2 * LM,
+                 tb.fac + (size_t)c * NR * NFAC * NTNZ + k0 + mm, NTNZ, NR);
   }
   __syncthreads();
 
