@@ -265,36 +265,38 @@ __device__ __forceinline__ void reg_fft(cpx<T>* v) {
 
 // Spectrum value n (0 <= n < NZR) of a packed pair of fields, Hermitian-extended:
 // Ga / Gb are the fields' columns (d_z fields read the u columns and multiply by i k_z).
-template <typename T>
-__device__ __forceinline__ cpx<T> z_pair_spec(const cpx<T>* Ga, const cpx<T>* Gb, bool dza, bool dzb, int n, int NZ,
-                                              int NZR, T kzs) {
-  int qq;
-  bool cj = false;
-  if (n < NZ) qq = n;
-  else if (n > NZR - NZ) { qq = NZR - n; cj = true; }
-  else return mk<T>(0, 0);
+// Branch-free: the load index is clamped and the value selected.
+template <typename T, int NZ, int NZR>
+__device__ __forceinline__ cpx<T> z_pair_spec(const cpx<T>* Ga, const cpx<T>* Gb, bool dza, bool dzb, int n, T kzs) {
+  const bool direct = n < NZ, mirror = n > NZR - NZ;
+  const int qq = direct ? n : (mirror ? NZR - n : 0);
   cpx<T> a = Ga[qq], b = Gb[qq];
   const T kz = kzs * (T)qq;
   if (dza) a = mk<T>(-kz * a.y, kz * a.x);
   if (dzb) b = mk<T>(-kz * b.y, kz * b.x);
-  if (qq == 0) { a.y = (T)0; b.y = (T)0; }  // C2R ignores Im of the k_z = 0 coefficient
-  if (cj) { a.y = -a.y; b.y = -b.y; }
-  return mk<T>(a.x - b.y, a.y + b.x);
+  // C2R ignores Im of the k_z = 0 coefficient; the mirrored half is the conjugate.
+  const T sy = (qq == 0) ? (T)0 : (mirror ? (T)-1 : (T)1);
+  a.y *= sy;
+  b.y *= sy;
+  const cpx<T> z = mk<T>(a.x - b.y, a.y + b.x);
+  return (direct || mirror) ? z : mk<T>(0, 0);
 }
 
 template <typename T, int NZRC, int N1, int N2, int R>
 __global__ void __launch_bounds__(ZTH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl, int standalone) {
-  static_assert(N1 * N2 == NZRC && R % 2 == 0, "z split");
+  static_assert(N1 * N2 == NZRC && R % 2 == 0 && NZRC % 3 == 0, "z split");
+  constexpr int NZ = NZRC / 3 + 1;    // NZR = 3 (NZ - 1) (3/2 rule)
+  constexpr int NQ = NZ - 1;          // retained z modes of the output
   constexpr int YP = N1 + 1;          // padded transpose row
   constexpr int YT = N2 * YP;         // one transform in the transpose buffer
-  constexpr int PS = NZRC + 4;        // padded physical field row
+  constexpr int PS = NZRC + 2;        // padded physical row (complex pairs)
   constexpr int NF = R + R / 2;       // forward transforms: (N_r, N_t) per row, (N_z, N_z) per row pair
-  const int mloc = blockIdx.z, i = blockIdx.y, j0 = blockIdx.x * R;
+  const int mloc = blockIdx.z, i = blockIdx.y, j0 = blockIdx.x * R;  // NTP % R == 0 (host check)
   if (!standalone && ctl->phase[tb.mem0 + mloc] < 0) return;
   extern __shared__ __align__(16) unsigned char smraw[];
   cpx<T>* Y = reinterpret_cast<cpx<T>*>(smraw);  // [R*6][N2][N1+1]
-  T* Ph = reinterpret_cast<T*>(Y + R * 6 * YT);  // [R][12][PS] physical fields, then products
-  const int NR = tb.NR, NZ = tb.NZ, NTP = tb.NTP;
+  cpx<T>* Ph = Y + R * 6 * YT;                   // [R][6][PS]: physical field pairs (2t, 2t+1), then products
+  const int NR = tb.NR, NTP = tb.NTP;
   const cpx<T>* G = reinterpret_cast<const cpx<T>*>(bf.G) + (size_t)mloc * 9 * NR * NTP * NZ;
   cpx<T>* H = reinterpret_cast<cpx<T>*>(bf.H) + (size_t)mloc * 3 * NR * NTP * NZ;
   const T kzs = (T)tb.kzs;
@@ -303,15 +305,14 @@ __global__ void __launch_bounds__(ZTH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl,
 
   // 1. inverse, pass A (spectra gathered from G)
   for (int task = threadIdx.x; task < R * 6 * N1; task += ZTH) {
-    const int n1 = task % N1, t = (task / N1) % 6, r = task / (6 * N1), j = j0 + r;
-    cpx<T> x[N2];
-    const cpx<T>* Gi = G + ((size_t)i * NTP + (j < NTP ? j : 0)) * NZ;
+    const int n1 = task % N1, t = (task / N1) % 6, r = task / (6 * N1);
+    const cpx<T>* Gi = G + ((size_t)i * NTP + j0 + r) * NZ;
     const int fa = 2 * t, fb = 2 * t + 1;  // d_z u_c (fields 9-11) comes from the u_c columns
     const cpx<T>* Ga = Gi + (size_t)(fa < 9 ? fa : fa - 9) * fstride;
     const cpx<T>* Gb = Gi + (size_t)(fb < 9 ? fb : fb - 9) * fstride;
+    cpx<T> x[N2];
 #pragma unroll
-    for (int n2 = 0; n2 < N2; n2++)
-      x[n2] = j < NTP ? z_pair_spec<T>(Ga, Gb, fa >= 9, fb >= 9, n1 + N1 * n2, NZ, NZRC, kzs) : mk<T>(0, 0);
+    for (int n2 = 0; n2 < N2; n2++) x[n2] = z_pair_spec<T, NZ, NZRC>(Ga, Gb, fa >= 9, fb >= 9, n1 + N1 * n2, kzs);
     reg_fft<T, +1, N2>(x);
     cpx<T>* Yt = Y + (r * 6 + t) * YT + n1;
 #pragma unroll
@@ -325,7 +326,7 @@ __global__ void __launch_bounds__(ZTH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl,
     }
   }
   __syncthreads();
-  // 2. inverse, pass B -> physical point z = N2 k1 + k2 of fields (2t, 2t+1)
+  // 2. inverse, pass B -> physical point z = N2 k1 + k2 of the pair (2t, 2t+1)
   for (int task = threadIdx.x; task < R * 6 * N2; task += ZTH) {
     const int k2 = task % N2, t = (task / N2) % 6, r = task / (6 * N2);
     cpx<T> y[N1];
@@ -333,40 +334,40 @@ __global__ void __launch_bounds__(ZTH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl,
 #pragma unroll
     for (int n1 = 0; n1 < N1; n1++) y[n1] = Yt[n1];
     reg_fft<T, +1, N1>(y);
-    T* pa = Ph + (r * 12 + 2 * t) * PS + k2;
+    cpx<T>* pz = Ph + (r * 6 + t) * PS + k2;
 #pragma unroll
-    for (int k1 = 0; k1 < N1; k1++) {
-      pa[N2 * k1] = y[k1].x;
-      pa[PS + N2 * k1] = y[k1].y;
-    }
+    for (int k1 = 0; k1 < N1; k1++) pz[N2 * k1] = y[k1];
   }
   __syncthreads();
-  // 3. -(u.grad)u (calcNonlinear_k, mod_io_nonlinear.cu:142-170), in place in fields 0-2.
-  // Field order: u_r,u_t,u_z, dr u_r,dr u_t,dr u_z, dt u_r,dt u_t,dt u_z, dz u_r,dz u_t,dz u_z.
+  // 3. -(u.grad)u (calcNonlinear_k, mod_io_nonlinear.cu:142-170).  Pairs: (u_r,u_t) (u_z,dr u_r)
+  // (dr u_t,dr u_z) (dt u_r,dt u_t) (dt u_z,dz u_r) (dz u_t,dz u_z).  Written back as
+  // pair 0 = (N_r, N_t), pair 1 .x = N_z.
   const T rinv = (T)tb.rinv[i];
   for (int task = threadIdx.x; task < R * NZRC; task += ZTH) {
     const int z = task % NZRC, r = task / NZRC;
-    T* p = Ph + r * 12 * PS + z;
-    const T ur = p[0], ut = p[PS], uz = p[2 * PS];
-    const T drr = p[3 * PS], drt = p[4 * PS], drz = p[5 * PS];
-    const T dtr = p[6 * PS], dtt = p[7 * PS], dtz = p[8 * PS];
-    const T dzr = p[9 * PS], dzt = p[10 * PS], dzz = p[11 * PS];
+    cpx<T>* p = Ph + r * 6 * PS + z;
+    const cpx<T> a0 = p[0], a1 = p[PS], a2 = p[2 * PS], a3 = p[3 * PS], a4 = p[4 * PS], a5 = p[5 * PS];
+    const T ur = a0.x, ut = a0.y, uz = a1.x;
+    const T drr = a1.y, drt = a2.x, drz = a2.y, dtr = a3.x, dtt = a3.y, dtz = a4.x, dzr = a4.y, dzt = a5.x, dzz = a5.y;
     const T utr = ut * rinv;
-    p[0] = -(ur * drr + ut * dtr + uz * dzr - ut * utr);
-    p[PS] = -(ur * drt + ut * dtt + uz * dzt + ur * utr);
-    p[2 * PS] = -(ur * drz + ut * dtz + uz * dzz);
+    p[0] = mk<T>(-(ur * drr + ut * dtr + uz * dzr - ut * utr), -(ur * drt + ut * dtt + uz * dzt + ur * utr));
+    p[PS].x = -(ur * drz + ut * dtz + uz * dzz);
   }
   __syncthreads();
-  // 4. forward, pass A: transform t < R packs (N_r, N_t) of row t; t >= R packs N_z of rows 2(t-R), 2(t-R)+1.
+  // 4. forward, pass A: transform t < R is (N_r, N_t) of row t; t >= R packs N_z of rows 2(t-R), 2(t-R)+1.
   for (int task = threadIdx.x; task < NF * N1; task += ZTH) {
     const int n1 = task % N1, t = task / N1;
-    const T* pa;
-    const T* pb;
-    if (t < R) { pa = Ph + t * 12 * PS; pb = pa + PS; }
-    else { pa = Ph + (2 * (t - R) * 12 + 2) * PS; pb = pa + 12 * PS; }
     cpx<T> x[N2];
+    if (t < R) {
+      const cpx<T>* pa = Ph + t * 6 * PS + n1;
 #pragma unroll
-    for (int n2 = 0; n2 < N2; n2++) x[n2] = mk<T>(pa[n1 + N1 * n2], pb[n1 + N1 * n2]);
+      for (int n2 = 0; n2 < N2; n2++) x[n2] = pa[N1 * n2];
+    } else {
+      const cpx<T>* pa = Ph + (2 * (t - R) * 6 + 1) * PS + n1;
+      const cpx<T>* pb = pa + 6 * PS;
+#pragma unroll
+      for (int n2 = 0; n2 < N2; n2++) x[n2] = mk<T>(pa[N1 * n2].x, pb[N1 * n2].x);
+    }
     reg_fft<T, -1, N2>(x);
     cpx<T>* Yt = Y + t * YT + n1;
 #pragma unroll
@@ -381,7 +382,7 @@ __global__ void __launch_bounds__(ZTH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl,
   }
   __syncthreads();
   // 5. forward, pass B -> spectrum X[N2 k1 + k2] (natural order, over the physical buffer)
-  cpx<T>* Xs = reinterpret_cast<cpx<T>*>(Ph);
+  cpx<T>* Xs = Ph;
   for (int task = threadIdx.x; task < NF * N2; task += ZTH) {
     const int k2 = task % N2, t = task / N2;
     cpx<T> y[N1];
@@ -394,10 +395,8 @@ __global__ void __launch_bounds__(ZTH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl,
   }
   __syncthreads();
   // 6. unpack x = a + i b: A_q = (X_q + conj X_-q)/2, B_q = (X_q - conj X_-q)/(2i); keep q < NZ-1.
-  const int NQ = NZ - 1;
   for (int task = threadIdx.x; task < R * 3 * NQ; task += ZTH) {
     const int q = task % NQ, c = (task / NQ) % 3, r = task / (3 * NQ), j = j0 + r;
-    if (j >= NTP) continue;
     const int slot = c < 2 ? r : R + r / 2;
     const bool takeB = c < 2 ? (c == 1) : (r & 1);
     const cpx<T>* X = Xs + slot * NZRC;
@@ -485,7 +484,7 @@ static bool z2_enabled();
 
 template <typename T, int NZRC, int N1, int N2, int R>
 static constexpr size_t z2_smem() {
-  return sizeof(cpx<T>) * R * 6 * N2 * (N1 + 1) + sizeof(T) * R * 12 * (NZRC + 4);
+  return sizeof(cpx<T>) * ((size_t)R * 6 * N2 * (N1 + 1) + (size_t)R * 6 * (NZRC + 2));
 }
 
 template <typename T, int NZRC, int N1, int N2, int R>
@@ -499,7 +498,6 @@ static void launch_z2(const Tables& tb, const Bufs& bf, Ctl* dctl, bool standalo
 // Two-pass z stage: (NZR, N1, N2, rows per block) for FP32 and FP64.
 #define NSP_Z2_LIST_F(X) X(24, 4, 6, 2) X(48, 8, 6, 2) X(96, 8, 12, 2) X(192, 16, 12, 2) X(384, 16, 24, 2) \
   X(576, 24, 24, 2) X(768, 32, 24, 2)
-#define NSP_Z2_LIST_D(X) X(24, 4, 6, 2) X(48, 8, 6, 2) X(96, 8, 12, 2) X(192, 16, 12, 2) X(384, 16, 24, 2)
 
 template <typename T>
 static void launch_nl_t(const Tables& tb, const Bufs& bf, Ctl* dctl, const double2* src, const float2* src32,
@@ -519,15 +517,15 @@ static void launch_nl_t(const Tables& tb, const Bufs& bf, Ctl* dctl, const doubl
   }
   if (mask & 2) {
     bool done = false;
-    if (z2_enabled()) {
-      if constexpr (sizeof(T) == 4) {
-#define NSP_CASE_Z2(n, a, b, r) \
-  if (!done && tb.NZR == n) { launch_z2<T, n, a, b, r>(tb, bf, dctl, src != nullptr, st, nm); done = true; }
-        NSP_Z2_LIST_F(NSP_CASE_Z2)
-      } else {
-        NSP_Z2_LIST_D(NSP_CASE_Z2)
+    // FP32 (mixed form) only: in FP64 the radix-stage kernel issues fewer FP64 instructions.
+    if (sizeof(T) == 4 && z2_enabled()) {
+#define NSP_CASE_Z2(n, a, b, r)                                             \
+  if (!done && tb.NZR == n && tb.NTP % r == 0) {                           \
+    launch_z2<T, n, a, b, r>(tb, bf, dctl, src != nullptr, st, nm);         \
+    done = true;                                                            \
+  }
+      NSP_Z2_LIST_F(NSP_CASE_Z2)
 #undef NSP_CASE_Z2
-      }
     }
     if (!done) {
       switch (tb.NZR) {
@@ -579,13 +577,8 @@ void configure_transform_kernels() {
 #define NSP_CFG_Z2F(n, a, b, r)                                                          \
   cudaFuncSetAttribute(nl_z2<float, n, a, b, r>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
                        (int)z2_smem<float, n, a, b, r>());
-#define NSP_CFG_Z2D(n, a, b, r)                                                            \
-  cudaFuncSetAttribute(nl_z2<double, n, a, b, r>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
-                       (int)z2_smem<double, n, a, b, r>());
   NSP_Z2_LIST_F(NSP_CFG_Z2F)
-  NSP_Z2_LIST_D(NSP_CFG_Z2D)
 #undef NSP_CFG_Z2F
-#undef NSP_CFG_Z2D
   // Twiddles of the register sub-transforms, exp(-2 pi i e / 96), from long double.
   float2 wf[96];
   double2 wd[96];
