@@ -233,6 +233,7 @@ def main():
         return ms / 1e3, iters, clk.summary()
 
     st = make(prec)
+    describe = st.describe()  # graph, autotuned linear-pass block, theta-transform path
     sec, iters, clocks = device_timed(st, args.steps, args.warmup)
     launches = st.kernel_launches()
     sec_max = max_over_ranks(sec)
@@ -322,7 +323,8 @@ def main():
             "data": "synthetic: seeded divergence-free perturbations of Hagen-Poiseuille flow",
             "config": {"workload": WORKLOAD, "members_per_gpu": M, "precision": args.precision,
                        "parallelism": "ensemble members sharded per GPU (dp%d), no collective" % world,
-                       "l2": "inputs larger than L2: %.2f GB of member state per GPU" % (M * 9 * S * 16 / 1e9)},
+                       "l2": "inputs larger than L2: %.2f GB of member state per GPU" % (M * 9 * S * 16 / 1e9),
+                       "execution": describe},
             "ns_per_step_dof": 1e9 * sec_max / args.steps / (M * world * DOF),
             "iters_mean": float(iters.mean()),
             "gpu_launches": int(launches),

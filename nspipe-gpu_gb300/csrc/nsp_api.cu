@@ -242,37 +242,44 @@ int autotune(nsp_ctx* c) {
   std::map<std::string, int> cache = tune_load();
   bool dirty = false;
   const int nm = c->nmem;
-  std::vector<int> ones(nm, 1);
-  CK(cudaMemcpyAsync(c->hctl.phase, ones.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, c->st));
+  std::vector<int> zeros(nm, 0), ones(nm, 1);
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
   for (auto& g : c->groups) {
     char key[128];
-    snprintf(key, sizeof key, "%dx%dx%d:m%d:p%d", g.tb.NR, g.tb.NT, g.tb.NZ, g.tb.nmem, c->precision);
+    snprintf(key, sizeof key, "v2:%dx%dx%d:m%d:p%d", g.tb.NR, g.tb.NT, g.tb.NZ, g.tb.nmem, c->precision);
     auto it = cache.find(key);
     if (it != cache.end() && linear_variant_fits(it->second, g.tb.NR)) {
       g.tb.lin_variant = it->second;
       continue;
     }
+    // A step is one predictor pass (phase 0) and usually one or two corrector passes
+    // (phase 1): each candidate is scored by predictor + corrector time.
     float best = 1e30f;
     for (int v = 0; v < LIN_VARIANTS; v++) {
       if (!linear_variant_fits(v, g.tb.NR)) continue;
       Tables tv = g.tb;
       tv.lin_variant = v;
-      launch_linear(tv, g.bf, c->dctl, c->st);
-      float t = 1e30f;
-      for (int r = 0; r < 3; r++) {
-        CK(cudaEventRecord(e0, c->st));
+      float score = 0.f;
+      for (int phase = 0; phase < 2; phase++) {
+        const std::vector<int>& ph = phase ? ones : zeros;
+        CK(cudaMemcpyAsync(c->hctl.phase, ph.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, c->st));
         launch_linear(tv, g.bf, c->dctl, c->st);
-        CK(cudaEventRecord(e1, c->st));
-        CK(cudaEventSynchronize(e1));
-        float ms = 0.f;
-        CK(cudaEventElapsedTime(&ms, e0, e1));
-        t = std::min(t, ms);
+        float t = 1e30f;
+        for (int r = 0; r < 3; r++) {
+          CK(cudaEventRecord(e0, c->st));
+          launch_linear(tv, g.bf, c->dctl, c->st);
+          CK(cudaEventRecord(e1, c->st));
+          CK(cudaEventSynchronize(e1));
+          float ms = 0.f;
+          CK(cudaEventElapsedTime(&ms, e0, e1));
+          t = std::min(t, ms);
+        }
+        score += t;
       }
       CK(cudaGetLastError());
-      if (t < best) { best = t; g.tb.lin_variant = v; }
+      if (score < best) { best = score; g.tb.lin_variant = v; }
     }
     cache[key] = g.tb.lin_variant;
     dirty = true;
@@ -806,8 +813,7 @@ int nsp_profile_stages(nsp_ctx* c, int reps, double* ms_out) {
   if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_profile_stages before nsp_setup");
   CK(cudaSetDevice(c->device));
   const int nm = c->nmem;
-  std::vector<int> ones(nm, 1);
-  CK(cudaMemcpyAsync(c->hctl.phase, ones.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, c->st));
+  std::vector<int> zeros(nm, 0), ones(nm, 1);
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));

@@ -54,7 +54,7 @@ struct Tables {
   int nsm;             // SM count (persistent grids)
 };
 
-constexpr int LIN_VARIANTS = 8;
+constexpr int LIN_VARIANTS = 11;
 int linear_default_variant(int NR);
 bool linear_variant_fits(int v, int NR);
 void linear_shape(int v, int* LM, int* NTH);  // modes per block, threads of a variant

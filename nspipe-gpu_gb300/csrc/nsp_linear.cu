@@ -112,9 +112,10 @@ __device__ __forceinline__ void solve_line(V* X, int ld, const double* __restric
 }
 
 // At least 1024 threads per SM resident (4 radial lines of 48 points x 16 modes
-// is 49 KB of shared memory, so four 256-thread blocks fit).
+// is 49 KB of shared memory, so four 256-thread blocks fit): 64 registers.
 template <int LM, int NTH>
-__global__ void __launch_bounds__(NTH, (1024 / NTH) < 2 ? 2 : (1024 / NTH)) linear_k(Tables tb, Bufs bf, Ctl* ctl) {
+__global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 : (1024 / NTH)))
+    linear_k(Tables tb, Bufs bf, Ctl* ctl) {
   const int mloc = blockIdx.y, gm = tb.mem0 + mloc;
   const int ph = ctl->phase[gm];
   if (ph < 0) return;
@@ -479,10 +480,18 @@ __global__ void lusolve_k(Tables tb, int kind, const double2* rhs, double2* sol)
 }
 
 // Block shapes of the linear pass (modes per block, threads): the candidates of the
-// setup-time autotuner.  Shared memory per block is 4 radial lines per mode.
+// setup-time autotuner.  Shared memory per block is 4 radial lines per mode.  Wide
+// blocks (32, 64 modes) give the solve phases one or more full warps on every SM
+// sub-partition; narrow ones more blocks per SM.
+#define NSP_LIN_SHAPES(X) \
+  X(0, 16, 256) X(1, 8, 128) X(2, 8, 256) X(3, 4, 128) X(4, 12, 192) X(5, 12, 256) X(6, 24, 384) X(7, 32, 512) \
+  X(8, 32, 256) X(9, 64, 512) X(10, 64, 1024)
 struct LinShape { int LM, NTH; };
-static const LinShape kLinShapes[LIN_VARIANTS] = {{16, 256}, {8, 128}, {8, 256}, {4, 128},
-                                                  {12, 192}, {12, 256}, {24, 384}, {32, 512}};
+static const LinShape kLinShapes[LIN_VARIANTS] = {
+#define NSP_LIN_ENTRY(v, lm, nth) {lm, nth},
+    NSP_LIN_SHAPES(NSP_LIN_ENTRY)
+#undef NSP_LIN_ENTRY
+};
 
 int linear_default_variant(int NR) { return NR <= 64 ? 0 : 2; }
 
@@ -497,14 +506,9 @@ bool linear_variant_fits(int v, int NR) {
 
 void configure_linear_kernels() {
   const int big = 200 * 1024;
-  cudaFuncSetAttribute(linear_k<16, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(linear_k<8, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(linear_k<8, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(linear_k<4, 128>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(linear_k<12, 192>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(linear_k<12, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(linear_k<24, 384>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-  cudaFuncSetAttribute(linear_k<32, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+#define NSP_LIN_CFG(v, lm, nth) cudaFuncSetAttribute(linear_k<lm, nth>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  NSP_LIN_SHAPES(NSP_LIN_CFG)
+#undef NSP_LIN_CFG
 }
 
 void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st) {
@@ -513,14 +517,11 @@ void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st)
   dim3 grid((tb.NTNZ + s.LM - 1) / s.LM, tb.nmem);
   size_t smem = sizeof(double2) * 4 * (size_t)tb.NR * s.LM;
   switch (v) {
-    case 0: linear_k<16, 256><<<grid, 256, smem, st>>>(tb, bf, dctl); break;
-    case 1: linear_k<8, 128><<<grid, 128, smem, st>>>(tb, bf, dctl); break;
-    case 2: linear_k<8, 256><<<grid, 256, smem, st>>>(tb, bf, dctl); break;
-    case 3: linear_k<4, 128><<<grid, 128, smem, st>>>(tb, bf, dctl); break;
-    case 4: linear_k<12, 192><<<grid, 192, smem, st>>>(tb, bf, dctl); break;
-    case 5: linear_k<12, 256><<<grid, 256, smem, st>>>(tb, bf, dctl); break;
-    case 6: linear_k<24, 384><<<grid, 384, smem, st>>>(tb, bf, dctl); break;
-    default: linear_k<32, 512><<<grid, 512, smem, st>>>(tb, bf, dctl); break;
+#define NSP_LIN_CASE(v, lm, nth) \
+  case v: linear_k<lm, nth><<<grid, nth, smem, st>>>(tb, bf, dctl); break;
+    NSP_LIN_SHAPES(NSP_LIN_CASE)
+#undef NSP_LIN_CASE
+    default: break;
   }
 }
 
