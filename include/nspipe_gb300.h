@@ -65,6 +65,10 @@ typedef struct nsp_diag_out {
   double last_err;    /* convergence measure of the last corrector iteration             */
   int last_iters;     /* corrector iterations of the last step                           */
   int status;         /* NSP_OK or NSP_ERR_NONFINITE                                     */
+  double re_tau;      /* friction Reynolds number Re * u_tau                             */
+  double div_max;     /* max |div u| over the interior rows (div_k, mod_radialFD.cu:67-96) */
+  double div_wall;    /* max |div u| on the wall row, the quantity the influence-matrix
+                         correction drives to zero (divWall_k, mod_radialFD.cu:34-63)     */
 } nsp_diag_out;
 
 typedef struct nsp_ctx nsp_ctx;
@@ -145,6 +149,11 @@ int nsp_diag(nsp_ctx* ctx, int member, nsp_diag_out* out);
 
 /* Radial grid r[NR] and quadrature weights rdr[NR] of a member (after nsp_setup). */
 int nsp_grid(nsp_ctx* ctx, int member, double* r, double* rdr);
+
+/* Mean axial velocity profile Re u_z(m=0, k_z=0)(r_i), i = 0..NR-1, of one member:
+ * the data row of wrt_mpr / wrt_mnp_k (mod_io_nonlinear.cu:119-129, 663-687)
+ * without the time stamp.  out holds NR doubles (host memory). */
+int nsp_mean_profile(nsp_ctx* ctx, int member, double* out);
 
 /* Number of kernel launches issued by the last nsp_step call (all graph nodes run). */
 long long nsp_kernel_launches(nsp_ctx* ctx);

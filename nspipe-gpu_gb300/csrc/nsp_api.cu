@@ -61,6 +61,7 @@ struct nsp_ctx {
   long long launches_last = 0;
   double2* scratch = nullptr;  // 2 x 3 x Smax, for nsp_nonlinear
   float2* scratch32 = nullptr; // 3 x Smax, FP32 input of nsp_nonlinear in the mixed form
+  unsigned long long* diagbuf = nullptr;  // 2 ordered-bit maxima of the divergence diagnostic
   long long Smax = 0;
   std::vector<void*> allocs;
   std::string err;
@@ -762,6 +763,34 @@ int nsp_diag(nsp_ctx* c, int m, nsp_diag_out* out) {
   out->last_err = err;
   out->last_iters = ite;
   out->status = (status & NSP_ERR_NONFINITE) ? NSP_ERR_NONFINITE : NSP_OK;
+  out->re_tau = g.p.Re * out->u_tau;
+  // Divergence of the state on the device.
+  if (!c->diagbuf) {
+    void* p = nullptr;
+    if (int rc = dalloc(c, &p, 2 * sizeof(unsigned long long))) return rc;
+    c->diagbuf = static_cast<unsigned long long*>(p);
+  }
+  CK(cudaMemsetAsync(c->diagbuf, 0, 2 * sizeof(unsigned long long), c->st));
+  launch_diag_div(g.tb, state_ptr(c, m, 0), c->diagbuf, c->st);
+  CK(cudaGetLastError());
+  unsigned long long bits[2];
+  CK(cudaMemcpyAsync(bits, c->diagbuf, sizeof bits, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  double dv[2];
+  memcpy(dv, bits, sizeof dv);
+  out->div_max = dv[0];
+  out->div_wall = dv[1];
+  return NSP_OK;
+}
+
+int nsp_mean_profile(nsp_ctx* c, int m, double* out) {
+  if (int rc = check_member(c, m)) return rc;
+  if (!out) return fail(c, NSP_ERR_ARG, "null output");
+  const Group& g = c->groups[c->grp[m]];
+  // Re u_z(0,0)(r_i): the first double of each radial row's (0,0) coefficient.
+  CK(cudaMemcpy2DAsync(out, sizeof(double), state_ptr(c, m, 2), sizeof(double2) * g.tb.NTNZ, sizeof(double), g.tb.NR,
+                       cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
   return NSP_OK;
 }
 

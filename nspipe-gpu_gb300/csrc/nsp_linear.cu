@@ -452,6 +452,51 @@ __global__ void converge_k(Ctl* ctl, cudaGraphConditionalHandle h, int use_cond)
   }
 }
 
+// Divergence diagnostic of one member's state (div_k / divWall_k, mod_radialFD.cu:34-96):
+// |d_r u_r + u_r/r + i m u_theta / r + i k_z u_z| per point, maximum over the interior
+// rows into out[0] and over the wall row into out[1] (ordered bits, atomicMax).
+__global__ void diag_div_k(Tables tb, const double2* __restrict__ U, unsigned long long* out) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int NR = tb.NR, NT = tb.NT, NZ = tb.NZ, NTNZ = tb.NTNZ;
+  const long long S = tb.S;
+  double mi = 0.0, mw = 0.0;
+  if (k < NTNZ) {
+    const int it = k / NZ, l = k - it * NZ, m = it < NT / 2 ? it : it - NT;
+    const double kt = tb.kts * (double)m, kz = tb.kzs * (double)l;
+    const int tab = abs((abs(m) % 2) - 1);
+    for (int i = 0; i < NR; i++) {
+      const int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
+      const double* Dr = tb.D + tab * STEN * NR + STEN * i + i0;
+      double sx = 0.0, sy = 0.0;
+      for (int j = 0; j < len; j++) {
+        const double2 a = U[(size_t)(left + j) * NTNZ + k];
+        sx += Dr[j] * a.x;
+        sy += Dr[j] * a.y;
+      }
+      const size_t h = (size_t)i * NTNZ + k;
+      const double ri = tb.rinv[i], kti = kt * ri;
+      const double2 ur = U[h], ut = U[S + h], uz = U[2 * S + h];
+      sx += ur.x * ri - kti * ut.y - kz * uz.y;
+      sy += ur.y * ri + kti * ut.x + kz * uz.x;
+      const double a = sqrt(sx * sx + sy * sy);
+      if (i < NR - 1) mi = fmax(mi, a);
+      else mw = fmax(mw, a);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mi = fmax(mi, __shfl_xor_sync(0xffffffffu, mi, o));
+    mw = fmax(mw, __shfl_xor_sync(0xffffffffu, mw, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(out, (unsigned long long)__double_as_longlong(mi));
+    atomicMax(out + 1, (unsigned long long)__double_as_longlong(mw));
+  }
+}
+
+void launch_diag_div(const Tables& tb, const double2* U, unsigned long long* out, cudaStream_t st) {
+  diag_div_k<<<(tb.NTNZ + 127) / 128, 128, 0, st>>>(tb, U, out);
+}
+
 // FP64 throughput probe: 8 independent multiply-add chains per thread, no memory
 // traffic; the measured denominator of the FP64 roofline.
 __global__ void fp64_peak_k(double* out, int iters, double a, double b) {

@@ -25,7 +25,7 @@ EXPORTS = [
     "nsp_set_state_host", "nsp_get_state_host", "nsp_set_state_device", "nsp_get_state_device",
     "nsp_step", "nsp_nonlinear", "nsp_lusolve", "nsp_diag", "nsp_grid", "nsp_kernel_launches",
     "nsp_sync", "nsp_last_error", "nsp_destroy", "nsp_set_stream", "nsp_profile_stages",
-    "nsp_measure_fp64_peak", "nsp_nonlinear_static", "nsp_describe",
+    "nsp_measure_fp64_peak", "nsp_nonlinear_static", "nsp_describe", "nsp_mean_profile",
 ]
 
 
@@ -43,6 +43,7 @@ class NspDiag(ctypes.Structure):
     _fields_ = [
         ("u_centre", ctypes.c_double), ("u_tau", ctypes.c_double), ("flux", ctypes.c_double),
         ("last_err", ctypes.c_double), ("last_iters", ctypes.c_int), ("status", ctypes.c_int),
+        ("re_tau", ctypes.c_double), ("div_max", ctypes.c_double), ("div_wall", ctypes.c_double),
     ]
 
 
@@ -85,6 +86,7 @@ def lib():
         L.nsp_measure_fp64_peak.argtypes = [vp, dp]
         L.nsp_nonlinear_static.argtypes = [vp, ip, vp, vp]
         L.nsp_describe.argtypes = [vp, ctypes.c_char_p, ip]
+        L.nsp_mean_profile.argtypes = [vp, ip, dp]
         L.nsp_last_error.argtypes = [vp]
         L.nsp_last_error.restype = ctypes.c_char_p
         L.nsp_destroy.argtypes = [vp]
@@ -238,6 +240,12 @@ class Stepper:
         d = NspDiag()
         self._check(lib().nsp_diag(self._h, m, ctypes.byref(d)))
         return d
+
+    def mean_profile(self, m=0):
+        """Re u_z(0,0)(r_i), i < NR (the data row of the reference's mean-profile file)."""
+        out = np.zeros(self.params[m].NR)
+        self._check(lib().nsp_mean_profile(self._h, m, _dp(out)))
+        return out
 
     def grid(self, m=0):
         NR = self.params[m].NR
