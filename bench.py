@@ -11,6 +11,7 @@ iterations to tol = 5e-8 as in the reference.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64]
     python bench.py --impl reference ...   # the reference nsPipe-CUDA build, same workload
+    python bench.py --workload uneven      # supplementary: 28 pipes of three resolutions, mixed
 
 Under torchrun each rank (one GPU) advances its own 64-member ensemble (weak
 scaling, no data-path collective); timing is bracketed by a barrier and
@@ -164,6 +165,77 @@ def run_reference(args):
     return 0
 
 
+# ------------------------------------------------------------------ uneven batch (supplementary line)
+UNEVEN = [  # (members, NR, NT, NZ, Re low, Re high): 32x64, 48x128, 96x192 modes
+    (16, 48, 32, 65, 2000.0, 2400.0),
+    (8, 64, 48, 129, 2400.0, 3000.0),
+    (4, 96, 96, 193, 3000.0, 4000.0),
+]
+UNEVEN_DT, UNEVEN_AMP = 0.006, 0.05  # dt = 0.003 R/U_b
+
+
+def run_uneven(args):
+    """Mixed-precision uneven batch: 28 pipes of three resolutions with Re spread
+    within each; member-steps/s and ns/(step.dof) over the whole batch, the plain
+    FP64 form on the same batch, and the execution choices (one group per shape,
+    one operator set per Re, groups as parallel graph branches)."""
+    import numpy as np
+    import torch
+    import nspipe_gb300 as nsp
+    torch.cuda.set_device(0)
+    prm, fields, dof = [], [], 0
+    k = 0
+    for n, nr, nt, nz, lo, hi in UNEVEN:
+        for i in range(n):
+            re = lo + (hi - lo) * i / max(1, n - 1)
+            prm.append(nsp.make_params(nr, nt, nz, re, UNEVEN_DT, 2.0 * PI2))
+            fields.append(nsp.seeded_field(nr, nt, nz, 2.0 * PI2, UNEVEN_AMP, 4000 + k))
+            dof += 3 * nr * nt * nz
+            k += 1
+
+    def timed(precision):
+        st = nsp.Stepper(prm, precision=precision)
+        for m, f in enumerate(fields):
+            st.set_state(m, f)
+        desc = st.describe()
+        stream = torch.cuda.Stream()
+        st.set_stream(stream.cuda_stream)
+        st.step(args.warmup, check=False)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with ClockSampler(0) as clk:
+            with torch.cuda.stream(stream):
+                e0.record(stream)
+                iters = st.step(args.steps, check=False)
+                e1.record(stream)
+            torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1e3
+        launches = st.kernel_launches()
+        finite = all(d.status == 0 for d in (st.diag(m) for m in range(len(prm))))
+        st.set_stream(0)
+        st.close()
+        return sec, iters, clk.summary(), desc, launches, finite
+
+    sec, iters, clocks, desc, launches, finite = timed(nsp.NSP_MIXED)
+    n = len(prm)
+    value = n * args.steps / sec
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": 1e3 * sec / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f64+f32", "data": "synthetic: seeded divergence-free perturbations of Hagen-Poiseuille flow",
+           "config": {"workload": "uneven batch: 16 pipes NR=48 x 32 x 64 modes (Re 2000-2400), 8 NR=64 x 48 x 128 "
+                                  "(Re 2400-3000), 4 NR=96 x 96 x 192 (Re 3000-4000); dt=0.003R/U_b, L=4piR, "
+                                  "amplitude 0.05", "members_per_gpu": n, "precision": "mixed", "execution": desc},
+           "ns_per_step_dof": 1e9 * sec / args.steps / dof, "iters_mean": float(iters.mean()),
+           "gpu_launches": int(launches), "clocks": clocks, "all_members_finite": finite}
+    if not args.no_fp64_compare:
+        sec64, it64, _, _, _, fin64 = timed(nsp.NSP_FP64)
+        out["fp64_form"] = {"value": n * args.steps / sec64, "unit": UNIT, "ms_per_step": 1e3 * sec64 / args.steps,
+                            "iters_mean": float(it64.mean()), "mixed_over_fp64": sec64 / sec,
+                            "all_members_finite": fin64}
+    print(json.dumps(out))
+    return 0
+
+
 # ------------------------------------------------------------------ our arm
 def main():
     ap = argparse.ArgumentParser()
@@ -175,11 +247,15 @@ def main():
     ap.add_argument("--members", type=int, default=MEMBERS)
     ap.add_argument("--no-fp64-compare", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", default="ensemble", choices=["ensemble", "uneven"],
+                    help="ensemble: the headline 64-member workload; uneven: the mixed three-resolution batch")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.workload == "uneven":
+        return run_uneven(args)
 
     import numpy as np
     import torch

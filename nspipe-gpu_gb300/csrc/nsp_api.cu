@@ -35,8 +35,10 @@ namespace {
 
 struct Group {
   nsp_params p;
-  std::vector<int> users;  // user member indices, in slot order
-  HostOps ops;
+  std::vector<int> users;   // user member indices, in slot order
+  std::vector<double> sets; // distinct Re of the group (operator parameter sets)
+  std::vector<int> mset;    // [slot] parameter set of each member
+  HostOps ops;              // shape data and set 0's operators (host copy)
   Tables tb{};
   Bufs bf{};
 };
@@ -62,6 +64,10 @@ struct nsp_ctx {
   double2* scratch = nullptr;  // 2 x 3 x Smax, for nsp_nonlinear
   float2* scratch32 = nullptr; // 3 x Smax, FP32 input of nsp_nonlinear in the mixed form
   unsigned long long* diagbuf = nullptr;  // 2 ordered-bit maxima of the divergence diagnostic
+  // Parallel branches of the step graph: one per member group beyond the first.
+  std::vector<cudaStream_t> side;
+  cudaEvent_t ev_fork = nullptr;
+  std::vector<cudaEvent_t> ev_join;
   long long Smax = 0;
   std::vector<void*> allocs;
   std::string err;
@@ -138,10 +144,25 @@ std::vector<float2> to_f32(const std::vector<double2>& v) {
   return o;
 }
 
-bool same_ops(const nsp_params& a, const nsp_params& b) {
-  return a.NR == b.NR && a.NT == b.NT && a.NZ == b.NZ && a.LT == b.LT && a.LZ == b.LZ && a.Re == b.Re &&
-         a.dt == b.dt && a.d_im == b.d_im && a.sten == b.sten && a.Qdes == b.Qdes && a.maxit == b.maxit &&
-         a.tol == b.tol;
+// Members sharing everything but Re share one group (one launch per stage);
+// their Re values become the group's operator parameter sets.
+bool same_shape(const nsp_params& a, const nsp_params& b) {
+  return a.NR == b.NR && a.NT == b.NT && a.NZ == b.NZ && a.LT == b.LT && a.LZ == b.LZ && a.dt == b.dt &&
+         a.d_im == b.d_im && a.sten == b.sten && a.Qdes == b.Qdes && a.maxit == b.maxit && a.tol == b.tol;
+}
+
+// Tables of one member's parameter set only (for single-member calls: nsp_nonlinear,
+// nsp_lusolve), as a one-set view of its group's tables.
+Tables member_view(const Group& g, int slot) {
+  Tables t = g.tb;
+  const int ps = g.mset[slot];
+  t.fac += (size_t)ps * 4 * t.NR * NFAC * t.NTNZ;
+  t.V += (size_t)ps * 3 * t.S;
+  t.Luc += (size_t)ps * 2 * STEN * t.NR;
+  t.uc += (size_t)ps * t.NR;
+  t.sscal += (size_t)4 * ps;
+  t.nsets = 1;
+  return t;
 }
 
 int check_params(nsp_ctx* c, const nsp_params& p, int idx) {
@@ -311,11 +332,32 @@ int build_graph(nsp_ctx* c) {
   cudaGraphNode_t node;
   CK(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp));
   cudaGraph_t body = cp.conditional.phGraph_out[0];
-  CK(cudaStreamBeginCaptureToGraph(c->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-  for (auto& gr : c->groups) {
-    launch_nonlinear(gr.tb, gr.bf, c->dctl, c->precision == NSP_MIXED, nullptr, nullptr, c->st);
-    launch_linear(gr.tb, gr.bf, c->dctl, c->st);
+  // Member groups (different shapes) are independent until the convergence
+  // bookkeeping: each group's four kernels form their own branch of the body graph
+  // so that groups run concurrently, then converge_k joins them.
+  const size_t ng = c->groups.size();
+  if (c->side.size() + 1 < ng) {
+    if (!c->ev_fork) CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+    while (c->side.size() + 1 < ng) {
+      cudaStream_t s2;
+      cudaEvent_t e2;
+      CK(cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&e2, cudaEventDisableTiming));
+      c->side.push_back(s2);
+      c->ev_join.push_back(e2);
+    }
   }
+  CK(cudaStreamBeginCaptureToGraph(c->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  if (ng > 1) CK(cudaEventRecord(c->ev_fork, c->st));
+  for (size_t k = 0; k < ng; k++) {
+    Group& gr = c->groups[k];
+    cudaStream_t sk = k == 0 ? c->st : c->side[k - 1];
+    if (k > 0) CK(cudaStreamWaitEvent(sk, c->ev_fork, 0));
+    launch_nonlinear(gr.tb, gr.bf, c->dctl, c->precision == NSP_MIXED, nullptr, nullptr, sk);
+    launch_linear(gr.tb, gr.bf, c->dctl, sk);
+    if (k > 0) CK(cudaEventRecord(c->ev_join[k - 1], sk));
+  }
+  for (size_t k = 1; k < ng; k++) CK(cudaStreamWaitEvent(c->st, c->ev_join[k - 1], 0));
   launch_converge(c->dctl, c->nmem, (unsigned long long)h, 1, c->st);
   cudaGraph_t cap = nullptr;
   CK(cudaStreamEndCapture(c->st, &cap));
@@ -361,16 +403,25 @@ int nsp_create(const nsp_params* members, int n_members, int precision, int devi
   for (int m = 0; m < n_members; m++) {
     int gi = -1;
     for (size_t g = 0; g < c->groups.size(); g++)
-      if (same_ops(c->groups[g].p, members[m])) { gi = (int)g; break; }
+      if (same_shape(c->groups[g].p, members[m])) { gi = (int)g; break; }
     if (gi < 0) {
       Group g;
       g.p = members[m];
       c->groups.push_back(g);
       gi = (int)c->groups.size() - 1;
     }
+    Group& gr = c->groups[gi];
     c->grp[m] = gi;
-    c->slot[m] = (int)c->groups[gi].users.size();
-    c->groups[gi].users.push_back(m);
+    c->slot[m] = (int)gr.users.size();
+    gr.users.push_back(m);
+    int ps = -1;
+    for (size_t k = 0; k < gr.sets.size(); k++)
+      if (gr.sets[k] == members[m].Re) { ps = (int)k; break; }
+    if (ps < 0) {
+      gr.sets.push_back(members[m].Re);
+      ps = (int)gr.sets.size() - 1;
+    }
+    gr.mset.push_back(ps);
   }
   c->internal.assign(n_members, 0);
   int base = 0;
@@ -454,22 +505,38 @@ int nsp_setup(nsp_ctx* c) {
     // maxit/tol are per context in the device control block: all groups must agree.
     if (g.p.maxit != c->hctl.maxit || g.p.tol != c->hctl.tol)
       return fail(c, NSP_ERR_ARG, "all members must share maxit and tol");
-    build_operators(g.p, g.ops);
     Tables& tb = g.tb;
     const nsp_params& p = g.p;
     HostOps& o = g.ops;
-    std::vector<double> rinv(p.NR), rinv2(p.NR), Luc(o.Lu.size());
+    // Operators of every parameter set (distinct Re), concatenated set-major.
+    const int nsets = (int)g.sets.size();
+    std::vector<double> fac_all, Luc_all, uc_all, sscal;
+    std::vector<double2> V_all;
+    for (int k = 0; k < nsets; k++) {
+      nsp_params pk = p;
+      pk.Re = g.sets[k];
+      HostOps ok;
+      build_operators(pk, ok);
+      const double c_ex = (1.0 - pk.d_im) / pk.Re;
+      fac_all.insert(fac_all.end(), ok.fac.begin(), ok.fac.end());
+      V_all.insert(V_all.end(), ok.V.begin(), ok.V.end());
+      uc_all.insert(uc_all.end(), ok.uc.begin(), ok.uc.end());
+      for (size_t e = 0; e < ok.Lu.size(); e++) Luc_all.push_back(0.5 * (c_ex * ok.Lu[e]));
+      sscal.insert(sscal.end(), {c_ex, 2.0 / pk.Re, ok.Qc, pk.Re});
+      if (k == 0) o = std::move(ok);
+    }
+    std::vector<double> rinv(p.NR), rinv2(p.NR);
     std::vector<float> D32(o.D.size());
     for (int i = 0; i < p.NR; i++) { rinv[i] = 1.0 / o.r[i]; rinv2[i] = 1.0 / (o.r[i] * o.r[i]); }
-    const double c_ex = (1.0 - p.d_im) / p.Re;
-    for (size_t e = 0; e < o.Lu.size(); e++) Luc[e] = 0.5 * (c_ex * o.Lu[e]);
     for (size_t e = 0; e < o.D.size(); e++) D32[e] = (float)o.D[e];
     int rc;
     if ((rc = upload(c, &tb.r, o.r)) || (rc = upload(c, &tb.rinv, rinv)) || (rc = upload(c, &tb.rinv2, rinv2)) ||
-        (rc = upload(c, &tb.rdr, o.rdr)) || (rc = upload(c, &tb.uc, o.uc)) || (rc = upload(c, &tb.D, o.D)) ||
-        (rc = upload(c, &tb.D32, D32)) || (rc = upload(c, &tb.Lu, o.Lu)) || (rc = upload(c, &tb.Luc, Luc)) ||
-        (rc = upload(c, &tb.fac, o.fac)) || (rc = upload(c, &tb.V, o.V)))
+        (rc = upload(c, &tb.rdr, o.rdr)) || (rc = upload(c, &tb.uc, uc_all)) || (rc = upload(c, &tb.D, o.D)) ||
+        (rc = upload(c, &tb.D32, D32)) || (rc = upload(c, &tb.Lu, o.Lu)) || (rc = upload(c, &tb.Luc, Luc_all)) ||
+        (rc = upload(c, &tb.fac, fac_all)) || (rc = upload(c, &tb.V, V_all)) || (rc = upload(c, &tb.sscal, sscal)) ||
+        (rc = upload(c, &tb.mset, g.mset)))
       return rc;
+    tb.nsets = nsets;
     std::vector<double2> wt = twiddles(tb.NTP), wz = twiddles(tb.NZR);
     if ((rc = upload(c, &tb.tw_t, wt)) || (rc = upload(c, &tb.tw_z, wz)) || (rc = upload(c, &tb.tw_t32, to_f32(wt))) ||
         (rc = upload(c, &tb.tw_z32, to_f32(wz))))
@@ -479,12 +546,12 @@ int nsp_setup(nsp_ctx* c) {
     tb.kts = PI2 / p.LT;
     tb.kzs = PI2 / p.LZ;
     tb.inv_dt = 1.0 / p.dt;
-    tb.c_ex = (1.0 - p.d_im) / p.Re;
+    tb.c_ex = sscal[0];  // set 0's scalars; kernels read each member's from sscal
     tb.d_im = p.d_im;
     tb.one_m_dim = 1.0 - p.d_im;
-    tb.two_re = 2.0 / p.Re;
+    tb.two_re = sscal[1];
     tb.Qdes = p.Qdes;
-    tb.Qc = o.Qc;
+    tb.Qc = sscal[2];
     tb.inv_norm = 1.0 / ((double)tb.NTP * (double)tb.NZR);
     // Mixed form: theta transforms as tensor-core DFT GEMMs where the length has a
     // compiled tile shape (NSP_THETA_TC=0 keeps the FFT kernels).
@@ -687,7 +754,8 @@ int nsp_nonlinear(nsp_ctx* c, int m, const void* ur, const void* ut, const void*
   for (int k = 0; k < 3; k++) CK(cudaMemcpyAsync(in + k * S, src[k], bytes, cudaMemcpyDeviceToDevice, c->st));
   const bool mixed = c->precision == NSP_MIXED;
   if (mixed) launch_to_f32(in, c->scratch32, 3LL * (long long)S, c->st);
-  launch_nonlinear(g.tb, g.bf, c->dctl, mixed, in, out, c->st, 7, mixed ? c->scratch32 : nullptr);
+  const Tables tv = member_view(g, c->slot[m]);  // the member's 2/Re for the wall forcing
+  launch_nonlinear(tv, g.bf, c->dctl, mixed, in, out, c->st, 7, mixed ? c->scratch32 : nullptr);
   CK(cudaGetLastError());
   for (int k = 0; k < 3; k++) CK(cudaMemcpyAsync(dst[k], out + k * S, bytes, cudaMemcpyDeviceToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
@@ -718,7 +786,8 @@ int nsp_nonlinear_static(nsp_ctx* c, int m, const void* u3, void* n3) {
   b.H = s + gsz;
   float2* in32 = mixed ? (float2*)(s + gsz + hsz) : nullptr;
   if (mixed) launch_to_f32((const double2*)u3, in32, 3LL * g.tb.S, c->st);
-  launch_nonlinear(g.tb, b, c->dctl, mixed, (const double2*)u3, (double2*)n3, c->st, 7, in32);
+  const Tables tv = member_view(g, c->slot[m]);
+  launch_nonlinear(tv, b, c->dctl, mixed, (const double2*)u3, (double2*)n3, c->st, 7, in32);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->st));
   return NSP_OK;
@@ -728,8 +797,8 @@ int nsp_lusolve(nsp_ctx* c, int m, int kind, const void* rhs, void* sol) {
   if (int rc = check_member(c, m)) return rc;
   if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_lusolve before nsp_setup");
   if (kind < 0 || kind > 3) return fail(c, NSP_ERR_ARG, "kind %d not in 0..3", kind);
-  Group& g = c->groups[c->grp[m]];
-  launch_lusolve(g.tb, kind, (const double2*)rhs, (double2*)sol, c->st);
+  const Tables tv = member_view(c->groups[c->grp[m]], c->slot[m]);
+  launch_lusolve(tv, kind, (const double2*)rhs, (double2*)sol, c->st);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->st));
   return NSP_OK;
@@ -758,12 +827,13 @@ int nsp_diag(nsp_ctx* c, int m, nsp_diag_out* out) {
   for (int i = 0; i < STEN; i++) du += uz[NR - STEN + i].x * o.D[(size_t)(NR - 1) * STEN + i];
   for (int i = 0; i < NR; i++) Q += o.rdr[i] * uz[i].x;
   out->u_centre = ucen;
-  out->u_tau = std::sqrt(std::fabs(du) / g.p.Re);
+  const double Re_m = c->prm[m].Re;
+  out->u_tau = std::sqrt(std::fabs(du) / Re_m);
   out->flux = Q;
   out->last_err = err;
   out->last_iters = ite;
   out->status = (status & NSP_ERR_NONFINITE) ? NSP_ERR_NONFINITE : NSP_OK;
-  out->re_tau = g.p.Re * out->u_tau;
+  out->re_tau = Re_m * out->u_tau;
   // Divergence of the state on the device.
   if (!c->diagbuf) {
     void* p = nullptr;
@@ -920,6 +990,9 @@ int nsp_destroy(nsp_ctx* c) {
   if (c->st) cudaStreamSynchronize(c->st);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
   for (void* p : c->allocs) cudaFree(p);
+  for (cudaStream_t s2 : c->side) cudaStreamDestroy(s2);
+  for (cudaEvent_t e2 : c->ev_join) cudaEventDestroy(e2);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->own_st) cudaStreamDestroy(c->own_st);
   delete c;
   return NSP_OK;

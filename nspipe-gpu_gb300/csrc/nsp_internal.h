@@ -22,8 +22,11 @@ struct FftPlan {
   int rad[MAXPLAN];
 };
 
-// Operator tables of one group of members sharing (NR, NT, NZ, LT, LZ, Re, dt, d_im).
-// All pointers are device memory; the struct is passed to kernels by value.
+// Operator tables of one group of members sharing (NR, NT, NZ, LT, LZ, dt, d_im):
+// one launch per stage covers the whole group.  Members may differ in Re; each
+// distinct Re is an operator parameter set, and the Re-dependent tables (fac, V,
+// Luc, uc, sscal) hold nsets consecutive sets.  All pointers are device memory;
+// the struct is passed to kernels by value.
 struct Tables {
   int NR, NT, NZ, NTP, NZP, NZR, NTNZ;
   long long S;         // NR*NT*NZ
@@ -48,11 +51,19 @@ struct Tables {
   const float2* tw_z32;
   FftPlan pt, pz;
   int lin_variant;     // block shape of the linear pass (autotuned at setup)
+  int nsets;           // operator parameter sets (distinct Re) of the group
+  const int* mset;     // [nmem] parameter set of each member
+  const double* sscal; // [nsets][4]: (1-d_im)/Re, 2/Re, Qc, Re
   const float* dft_inv; // mixed form, tensor-core theta transforms: DFT-matrix operand images
   const float* dft_fwd; //   ([hi | lo] x N x K core matrices, nsp_theta_tc.cu)
   int tc_theta;        // 1: the mixed form's theta transforms run as tcgen05 GEMMs
   int nsm;             // SM count (persistent grids)
 };
+
+#ifdef __CUDACC__
+// Operator parameter set of a member (0 when the group has a single Re).
+__device__ __forceinline__ int member_set(const Tables& tb, int mloc) { return tb.nsets > 1 ? tb.mset[mloc] : 0; }
+#endif
 
 constexpr int LIN_VARIANTS = 11;
 int linear_default_variant(int NR);

@@ -141,6 +141,14 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   float2* Ui32 = U32i ? U32i + (size_t)mloc * 3 * S : nullptr;  // mixed form
   const double2* Nn = bf.N + (size_t)mloc * 3 * S;
   double2* Rw = bf.RHSW + (size_t)mloc * 3 * S;
+  // The member's operator parameter set (its Re): LU factors, correction profiles,
+  // explicit Laplacian, flux profile and scalars.
+  const int ps = member_set(tb, mloc);
+  const double* fac = tb.fac + (size_t)ps * 4 * NR * NFAC * NTNZ;
+  const double2* Vp = tb.V + (size_t)ps * 3 * S;
+  const double* Luc = tb.Luc + (size_t)ps * 2 * STEN * NR;
+  const double* ucp = tb.uc + (size_t)ps * NR;
+  const double c_ex = tb.sscal[4 * ps], Qc = tb.sscal[4 * ps + 2];
   const int tid = threadIdx.x, nth = blockDim.x;
   if (tid == 0) bad = 0;
   if (tid < LM) {  // wavenumbers once per block instead of per point (the FP64 pipe is the bound)
@@ -169,7 +177,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     // Luc holds the stencil pre-scaled by 1/2, so e comes out at half scale; u^n is
     // read straight from global memory (the stencil's rows are served by L1).
     // Then, at half scale: rhs = N + e, rhsw' = (1-d_im) N + e.
-    const double hc = 0.5 * tb.c_ex, hidt = 0.5 * tb.inv_dt, hw = 0.5 * tb.one_m_dim;
+    const double hc = 0.5 * c_ex, hidt = 0.5 * tb.inv_dt, hw = 0.5 * tb.one_m_dim;
     for (int p = tid; p < LN; p += nth) {
       int i = p / LM, mm = p - i * LM, k = k0 + mm;
       if (k >= NTNZ) {
@@ -184,8 +192,8 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       double hs = hc * (base - ir2) + hidt;  // s/2
       double hd = -hc * (2.0 * kt * ir2);    // d/2
       double hz = hc * base + hidt;          // diagonal of the u_z line / 2
-      const double* Lo = tb.Luc + (1 - par_m) * STEN * NR + STEN * i + i0;  // u_r, u_theta (odd flag)
-      const double* Le = tb.Luc + par_m * STEN * NR + STEN * i + i0;        // u_z
+      const double* Lo = Luc + (1 - par_m) * STEN * NR + STEN * i + i0;  // u_r, u_theta (odd flag)
+      const double* Le = Luc + par_m * STEN * NR + STEN * i + i0;        // u_z
       double2 lr = c2(0, 0), lt = c2(0, 0), lz = c2(0, 0);
       for (int j = 0; j < len; j++) {
         double a = __ldg(Lo + j), b = __ldg(Le + j);
@@ -259,7 +267,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   if (tid < 2 * LM) {
     const int mm = tid >> 1, part = tid & 1;
     if (k0 + mm < NTNZ)
-      solve_line(reinterpret_cast<double*>(P + mm) + part, 2 * LM, tb.fac + 3 * (size_t)NR * NFAC * NTNZ + k0 + mm,
+      solve_line(reinterpret_cast<double*>(P + mm) + part, 2 * LM, fac + 3 * (size_t)NR * NFAC * NTNZ + k0 + mm,
                  NTNZ, NR);
   }
   __syncthreads();
@@ -298,7 +306,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     const int c = tid / (2 * LM), rem = tid - c * 2 * LM, mm = rem >> 1, part = rem & 1;
     if (k0 + mm < NTNZ)
       solve_line(reinterpret_cast<double*>(R + c * LN + mm) + part, 2 * LM,
-                 tb.fac + (size_t)c * NR * NFAC * NTNZ + k0 + mm, NTNZ, NR);
+                 fac + (size_t)c * NR * NFAC * NTNZ + k0 + mm, NTNZ, NR);
   }
   __syncthreads();
 
@@ -338,7 +346,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     double2 up = R[p], um = R[LN + p], uz = R[2 * LN + p];
     double2 dv = dvs[mm];
     size_t hv = (size_t)i * NTNZ + k;
-    double2 v0 = tb.V[hv], v1 = tb.V[S + hv], v2 = tb.V[2 * S + hv];
+    double2 v0 = Vp[hv], v1 = Vp[S + hv], v2 = Vp[2 * S + hv];
     up.x += dv.x * v0.x - dv.y * v0.y; up.y += dv.x * v0.y + dv.y * v0.x;
     um.x += dv.x * v1.x - dv.y * v1.y; um.y += dv.x * v1.y + dv.y * v1.x;
     uz.x += dv.x * v2.x - dv.y * v2.y; uz.y += dv.x * v2.y + dv.y * v2.x;
@@ -354,8 +362,8 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   if (k0 == 0 && tid == 0) {
     double Q = 0.0;
     for (int i = 0; i < NR; i++) Q += tb.rdr[i] * R[2 * LN + i * LM].x;
-    double corr = (tb.Qdes - Q) / tb.Qc;
-    for (int i = 0; i < NR; i++) R[2 * LN + i * LM].x += corr * tb.uc[i];
+    double corr = (tb.Qdes - Q) / Qc;
+    for (int i = 0; i < NR; i++) R[2 * LN + i * LM].x += corr * ucp[i];
   }
   __syncthreads();
 

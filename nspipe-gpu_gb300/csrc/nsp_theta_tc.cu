@@ -229,7 +229,7 @@ template <int NT, int NTP> struct FwdJob {
       const int it = part * (CPP / 2) + j;
       double2 o = make_double2((double)v[2 * j], (double)v[2 * j + 1]);
       if (it == NT / 2 || l == NZ - 1) o = make_double2(0.0, 0.0);  // padBackward_k's dropped modes
-      if (c == 2 && it == 0 && l == 0) o.x -= tb.two_re * dwall;
+      if (c == 2 && it == 0 && l == 0) o.x -= tb.sscal[4 * member_set(tb, mloc) + 1] * dwall;  // 2/Re
       Nout[(size_t)it * NZ] = o;
     }
   }

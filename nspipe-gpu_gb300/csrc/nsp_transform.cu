@@ -453,7 +453,7 @@ __global__ void __launch_bounds__(TTH) nl_theta_fwd(Tables tb, Bufs bf, const Ct
     if (sizeof(T) == 8) v = make_double2((double)b.x * tb.inv_norm, (double)b.y * tb.inv_norm);
     else v = make_double2((double)(b.x * scale), (double)(b.y * scale));
     if (it == NT / 2 || l == NZ - 1) v = make_double2(0.0, 0.0);
-    if (c == 2 && it == 0 && l == 0) v.x -= tb.two_re * dwall;
+    if (c == 2 && it == 0 && l == 0) v.x -= tb.sscal[4 * member_set(tb, mloc) + 1] * dwall;  // 2/Re
     Nout[c * S + (size_t)i * NTNZ + (size_t)it * NZ + l] = v;
   }
 }

@@ -1,0 +1,77 @@
+"""Uneven batches: members of several shapes and Reynolds numbers in one context.
+Members sharing a shape form one group (one launch per stage) whatever their Re;
+each distinct Re is an operator parameter set of the group; the groups run as
+parallel branches of the step graph.  Every member must match its own oracle."""
+import numpy as np
+import pytest
+
+from conftest import rel
+from test_gpu_parity import CFG, dev, init, nsp, orc  # noqa: F401  (fixtures)
+
+pytestmark = pytest.mark.gpu
+
+NAMES = ["s1", "s2", "s1", "s1", "s2"]
+SCALE = [1.0, 1.0, 1.2, 1.0, 1.3]  # Re multipliers: s1 has two sets (1.0 twice, 1.2), s2 two sets
+
+
+def batch(nsp, precision):
+    prm, states = [], []
+    for k, name in enumerate(NAMES):
+        NR, NT, NZ, LZ, Re, dt, _, _ = CFG[name]
+        prm.append(nsp.make_params(NR, NT, NZ, Re * SCALE[k], dt, LZ))
+        states.append(init(nsp, name, k))
+    st = nsp.Stepper(prm, precision=precision)
+    for m, u in enumerate(states):
+        st.set_state(m, u)
+    return st, states
+
+
+def member_oracle(name, k):
+    import oracle
+    NR, NT, NZ, LZ, Re, dt, _, _ = CFG[name]
+    return oracle.Oracle(NR, NT, NZ, Re=Re * SCALE[k], dt=dt, LZ=LZ)
+
+
+def test_uneven_groups_sets_and_parity(nsp):
+    st, states = batch(nsp, nsp.NSP_FP64)
+    d = st.describe()
+    assert [g["members"] for g in d["groups"]] == [3, 2]
+    its = st.step(3)
+    for m, name in enumerate(NAMES):
+        o = member_oracle(name, m)
+        uo, ito, _ = o.step([a.copy() for a in states[m]], 3)
+        assert rel(np.stack(st.get_state(m)), np.stack(uo)) < 1e-12, m
+        assert list(its[:, m]) == list(ito), m
+        o.close()
+    st.close()
+
+
+def test_uneven_single_member_calls_use_member_operators(nsp):
+    import torch
+    st, states = batch(nsp, nsp.NSP_FP64)
+    m, name = 2, "s1"  # second parameter set of the s1 group
+    o = member_oracle(name, m)
+    shape = o.shape
+    rng = np.random.default_rng(5)
+    b = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    sol = torch.zeros(shape, dtype=torch.complex128, device="cuda")
+    st.lusolve(m, 0, dev(b), sol)
+    assert rel(sol.cpu().numpy(), o.lusolve_u(b, 0)) < 1e-13
+    n = [torch.zeros(shape, dtype=torch.complex128, device="cuda") for _ in range(3)]
+    st.nonlinear(m, [dev(a) for a in states[m]], n)
+    ref = o.nonlinear(states[m])
+    for c in range(3):
+        assert rel(n[c].cpu().numpy(), ref[c]) < 1e-13, c
+    o.close()
+    st.close()
+
+
+def test_uneven_mixed_close_to_fp64(nsp):
+    res = {}
+    for prec in (nsp.NSP_FP64, nsp.NSP_MIXED):
+        st, _ = batch(nsp, prec)
+        st.step(5)
+        res[prec] = [np.stack(st.get_state(m)) for m in range(len(NAMES))]
+        st.close()
+    for m in range(len(NAMES)):
+        assert rel(res[nsp.NSP_MIXED][m], res[nsp.NSP_FP64][m]) < 1e-6, m
