@@ -217,19 +217,30 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       Rw[2 * S + h] = c2(hw * nz.x + ez.x, hw * nz.y + ez.y);
     }
   } else {
-    // A+B. rhs/2 = (d_im/2) N(u_i) + rhsw'/2, straight in r/theta form.
+    // A+B. rhs/2 = (d_im/2) N(u_i) + rhsw'/2, straight in r/theta form.  U points per
+    // thread have their loads issued together (measured best at 1 here: more spills).
     const double hd = 0.5 * tb.d_im;
-    for (int p = tid; p < LN; p += nth) {
-      int i = p / LM, mm = p - i * LM, k = k0 + mm;
-      if (k >= NTNZ) {
-        for (int c = 0; c < 3; c++) R[c * LN + p] = c2(0, 0);
-        continue;
-      }
-      size_t h = (size_t)i * NTNZ + k;
+    constexpr int U = 1;
+    for (int pb = tid; pb < LN; pb += U * nth) {
+      double2 n[U][3], w[U][3];
 #pragma unroll
-      for (int c = 0; c < 3; c++) {
-        double2 n = Nn[c * S + h], w = Rw[c * S + h];
-        R[c * LN + p] = c2(hd * n.x + w.x, hd * n.y + w.y);
+      for (int u = 0; u < U; u++) {
+        const int p = pb + u * nth, i = p / LM, k = k0 + p - i * LM;
+        const bool ok = p < LN && k < NTNZ;
+        const size_t h = ok ? (size_t)i * NTNZ + k : 0;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          n[u][c] = ok ? Nn[c * S + h] : c2(0, 0);
+          w[u][c] = ok ? Rw[c * S + h] : c2(0, 0);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; u++) {
+        const int p = pb + u * nth;
+        if (p < LN) {
+#pragma unroll
+          for (int c = 0; c < 3; c++) R[c * LN + p] = c2(hd * n[u][c].x + w[u][c].x, hd * n[u][c].y + w[u][c].y);
+        }
       }
     }
   }
@@ -373,23 +384,37 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   // the exponent field: both on the integer pipe.
   unsigned long long lnum = 0ull, lden = 0ull;
   bool nonfin = false;
-  for (int p = tid; p < LN; p += nth) {
-    int i = p / LM, mm = p - i * LM, k = k0 + mm;
-    if (k >= NTNZ) continue;
-    size_t h = (size_t)i * NTNZ + k;
+  constexpr int UI = 2;  // points per thread whose previous-iterate loads are issued together
+  for (int pb = tid; pb < LN; pb += UI * nth) {
+    double2 o[UI][3];
+    if (!pred) {
 #pragma unroll
-    for (int c = 0; c < 3; c++) {
-      double2 v = R[c * LN + p];
-      if (!pred) {
-        double2 o = Ui[c * S + h];
-        double ex = o.x - v.x, ey = o.y - v.y;
-        lnum = max(lnum, (unsigned long long)__double_as_longlong(ex * ex + ey * ey));
-        lden = max(lden, (unsigned long long)__double_as_longlong(o.x * o.x + o.y * o.y));
+      for (int u = 0; u < UI; u++) {
+        const int p = pb + u * nth, i = p / LM, k = k0 + p - i * LM;
+        const bool ok = p < LN && k < NTNZ;
+        const size_t h = ok ? (size_t)i * NTNZ + k : 0;
+#pragma unroll
+        for (int c = 0; c < 3; c++) o[u][c] = ok ? Ui[c * S + h] : c2(0, 0);
       }
-      const unsigned EX = 0x7FF00000u;
-      nonfin |= ((unsigned)__double2hiint(v.x) & EX) == EX || ((unsigned)__double2hiint(v.y) & EX) == EX;
-      Ui[c * S + h] = v;
-      if (Ui32) Ui32[c * S + h] = make_float2((float)v.x, (float)v.y);
+    }
+#pragma unroll
+    for (int u = 0; u < UI; u++) {
+      const int p = pb + u * nth, i = p / LM, k = k0 + p - i * LM;
+      if (p >= LN || k >= NTNZ) continue;
+      const size_t h = (size_t)i * NTNZ + k;
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        double2 v = R[c * LN + p];
+        if (!pred) {
+          const double ex = o[u][c].x - v.x, ey = o[u][c].y - v.y;
+          lnum = max(lnum, (unsigned long long)__double_as_longlong(ex * ex + ey * ey));
+          lden = max(lden, (unsigned long long)__double_as_longlong(o[u][c].x * o[u][c].x + o[u][c].y * o[u][c].y));
+        }
+        const unsigned EX = 0x7FF00000u;
+        nonfin |= ((unsigned)__double2hiint(v.x) & EX) == EX || ((unsigned)__double2hiint(v.y) & EX) == EX;
+        Ui[c * S + h] = v;
+        if (Ui32) Ui32[c * S + h] = make_float2((float)v.x, (float)v.y);
+      }
     }
   }
   if (nonfin) bad = 1;
