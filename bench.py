@@ -64,6 +64,16 @@ class ClockSampler:
                                          stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except OSError:
             self.proc = None
+        # Start timing only once nvidia-smi is sampling: its start-up (NVML
+        # initialisation on a fresh machine) must not overlap the timed steps.
+        t0 = time.time()
+        while self.proc and time.time() - t0 < 10.0:
+            try:
+                if os.path.getsize(self.path) > 0:
+                    break
+            except OSError:
+                pass
+            time.sleep(0.05)
         time.sleep(0.3)
         return self
 

@@ -25,7 +25,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I", o
 
 CU_UNITS = ["nsp_api.cu", "nsp_linear.cu", "nsp_transform.cu", "nsp_noalloc.cu", "nsp_theta_tc.cu"]
 CXX_UNITS = ["nsp_setup.cpp"]
-HEADERS = ["nsp_internal.h", "nsp_fft.cuh", os.path.join("..", "..", "include", "nspipe_gb300.h")]
+HEADERS = ["nsp_internal.h", "nsp_fft.cuh", "nsp_cvt.cuh", "nsp_state.cuh", "nsp_tc.cuh", os.path.join("..", "..", "include", "nspipe_gb300.h")]
 
 
 def _stale(obj, src):

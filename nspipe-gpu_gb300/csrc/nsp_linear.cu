@@ -19,6 +19,7 @@
 // array, no shared-memory staging), so a block holds 4 radial lines per mode.
 #include <cstdio>
 
+#include "nsp_cvt.cuh"
 #include "nsp_internal.h"
 
 namespace nsp {
@@ -413,7 +414,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
         const unsigned EX = 0x7FF00000u;
         nonfin |= ((unsigned)__double2hiint(v.x) & EX) == EX || ((unsigned)__double2hiint(v.y) & EX) == EX;
         Ui[c * S + h] = v;
-        if (Ui32) Ui32[c * S + h] = make_float2((float)v.x, (float)v.y);
+        if (Ui32) Ui32[c * S + h] = make_float2(f64_to_f32(v.x), f64_to_f32(v.y));  // integer-pipe rounding
       }
     }
   }

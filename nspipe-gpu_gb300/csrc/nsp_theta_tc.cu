@@ -35,6 +35,7 @@
 #include <cstring>
 #include <vector>
 
+#include "nsp_cvt.cuh"
 #include "nsp_fft.cuh"
 #include "nsp_internal.h"
 #include "nsp_state.cuh"
@@ -227,7 +228,7 @@ template <int NT, int NTP> struct FwdJob {
 #pragma unroll
     for (int j = 0; j < CPP / 2; j++) {
       const int it = part * (CPP / 2) + j;
-      double2 o = make_double2((double)v[2 * j], (double)v[2 * j + 1]);
+      double2 o = make_double2(f32_to_f64(v[2 * j]), f32_to_f64(v[2 * j + 1]));  // exact, integer pipe
       if (it == NT / 2 || l == NZ - 1) o = make_double2(0.0, 0.0);  // padBackward_k's dropped modes
       if (c == 2 && it == 0 && l == 0) o.x -= tb.sscal[4 * member_set(tb, mloc) + 1] * dwall;  // 2/Re
       Nout[(size_t)it * NZ] = o;

@@ -29,6 +29,7 @@
 #include <cstdio>
 #include <cstdlib>
 
+#include "nsp_cvt.cuh"
 #include "nsp_fft.cuh"
 #include "nsp_internal.h"
 #include "nsp_state.cuh"
@@ -451,7 +452,7 @@ __global__ void __launch_bounds__(TTH) nl_theta_fwd(Tables tb, Bufs bf, const Ct
     cpx<T> b = buf[p * LC + lc];
     double2 v;
     if (sizeof(T) == 8) v = make_double2((double)b.x * tb.inv_norm, (double)b.y * tb.inv_norm);
-    else v = make_double2((double)(b.x * scale), (double)(b.y * scale));
+    else v = make_double2(f32_to_f64(b.x * scale), f32_to_f64(b.y * scale));  // exact, integer pipe
     if (it == NT / 2 || l == NZ - 1) v = make_double2(0.0, 0.0);
     if (c == 2 && it == 0 && l == 0) v.x -= tb.sscal[4 * member_set(tb, mloc) + 1] * dwall;  // 2/Re
     Nout[c * S + (size_t)i * NTNZ + (size_t)it * NZ + l] = v;
@@ -616,7 +617,7 @@ void launch_nonlinear(const Tables& tb, const Bufs& bf, Ctl* dctl, bool mixed, c
 __global__ void to_f32_k(const double2* __restrict__ src, float2* __restrict__ dst, long long n) {
   for (long long h = blockIdx.x * (long long)blockDim.x + threadIdx.x; h < n; h += (long long)gridDim.x * blockDim.x) {
     double2 a = src[h];
-    dst[h] = make_float2((float)a.x, (float)a.y);
+    dst[h] = make_float2(f64_to_f32(a.x), f64_to_f32(a.y));
   }
 }
 
