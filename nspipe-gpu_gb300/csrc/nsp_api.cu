@@ -463,11 +463,14 @@ int nsp_create(const nsp_params* members, int n_members, int precision, int devi
     CK(cudaMemset(g.bf.N, 0, S3 * sizeof(double2)));
     CK(cudaMemset(g.bf.RHSW, 0, S3 * sizeof(double2)));
     g.bf.U32[0] = g.bf.U32[1] = nullptr;
+    g.bf.DR32[0] = g.bf.DR32[1] = nullptr;
     if (precision == NSP_MIXED) {
-      if ((rc = dalloc(c, &g.bf.U32[0], S3 * sizeof(float2)))) return rc;
-      if ((rc = dalloc(c, &g.bf.U32[1], S3 * sizeof(float2)))) return rc;
-      CK(cudaMemset(g.bf.U32[0], 0, S3 * sizeof(float2)));
-      CK(cudaMemset(g.bf.U32[1], 0, S3 * sizeof(float2)));
+      for (int k = 0; k < 2; k++) {
+        if ((rc = dalloc(c, &g.bf.U32[k], S3 * sizeof(float2)))) return rc;
+        if ((rc = dalloc(c, &g.bf.DR32[k], S3 * sizeof(float2)))) return rc;
+        CK(cudaMemset(g.bf.U32[k], 0, S3 * sizeof(float2)));
+        CK(cudaMemset(g.bf.DR32[k], 0, S3 * sizeof(float2)));
+      }
     }
     if (tb.S > c->Smax) c->Smax = tb.S;
   }
@@ -692,11 +695,11 @@ int nsp_step(nsp_ctx* c, int nsteps, int* iters_out) {
   long long launches = 0;
   const long long per_iter = 4LL * (long long)c->groups.size() + 1;
   std::vector<int> hist;
-  // Mixed form: the transforms read an FP32 mirror of the state, kept current by the
-  // linear pass; refresh it here because the state may have been set from outside.
+  // Mixed form: the transforms read an FP32 mirror of the state and its radial
+  // derivative, kept current by the linear pass; refresh them here because the
+  // state may have been set from outside.
   if (c->precision == NSP_MIXED && nsteps > 0)
-    for (auto& g : c->groups)
-      launch_to_f32(g.bf.U[c->parity], g.bf.U32[c->parity], (long long)g.tb.nmem * 3 * g.tb.S, c->st);
+    for (auto& g : c->groups) launch_mirror(g.tb, g.bf.U[c->parity], g.bf.U32[c->parity], g.bf.DR32[c->parity], c->st);
   for (int done = 0; done < nsteps;) {
     int chunk = std::min(cap, nsteps - done);
     CK(cudaMemsetAsync(&c->dctl->step, 0, sizeof(int), c->st));

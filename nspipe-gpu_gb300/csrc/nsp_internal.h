@@ -74,6 +74,8 @@ void linear_shape(int v, int* LM, int* NTH);  // modes per block, threads of a v
 struct Bufs {
   double2* U[2];       // [nmem][3][S]: state / corrector iterate, roles swap each step (parity)
   float2* U32[2];      // mixed form only: FP32 copies of U[0], U[1] read by the transforms
+  float2* DR32[2];     // mixed form only: d_r of U32[k] (7-point parity stencil, FP32), written
+                       // with U32 so that the theta-inverse reads it instead of re-gathering levels
   double2* RHSW;       // [nmem][3][S]: [(1-d_im) N(u^n) + u^n/dt + (1-d_im)/Re L u^n] / 2, r/theta form
   double2* N;          // [nmem][3][S]: nonlinear term output
   void* G;             // [nmem][9][NR][NTP][NZ] complex T: theta-inverse of u, dr u, i m u / r
@@ -117,6 +119,8 @@ size_t noalloc_scratch_bytes();
 cudaError_t noalloc_scratch(int device, void** ptr);
 // FP32 copy of nmem x 3 x S complex values (the mixed form's transform input).
 void launch_to_f32(const double2* src, float2* dst, long long n, cudaStream_t st);
+// The FP32 mirror and its radial derivative (DR32) of a group's state U (mixed form).
+void launch_mirror(const Tables& tb, const double2* U, float2* U32, float2* DR32, cudaStream_t st);
 int kernels_per_nonlinear();
 // Tensor-core theta transforms (nsp_theta_tc.cu).
 bool theta_tc_supported(int NT, int NTP);

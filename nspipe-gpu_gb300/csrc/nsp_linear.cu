@@ -20,7 +20,9 @@
 #include <cstdio>
 
 #include "nsp_cvt.cuh"
+#include "nsp_fft.cuh"
 #include "nsp_internal.h"
+#include "nsp_state.cuh"
 
 namespace nsp {
 
@@ -140,6 +142,8 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   double2* Ui = (par ? bf.U[0] : bf.U[1]) + (size_t)mloc * 3 * S;
   float2* U32i = par ? bf.U32[0] : bf.U32[1];
   float2* Ui32 = U32i ? U32i + (size_t)mloc * 3 * S : nullptr;  // mixed form
+  float2* DR32i = par ? bf.DR32[0] : bf.DR32[1];
+  float2* Udr32 = DR32i ? DR32i + (size_t)mloc * 3 * S : nullptr;  // mixed form: d_r of the FP32 mirror
   const double2* Nn = bf.N + (size_t)mloc * 3 * S;
   double2* Rw = bf.RHSW + (size_t)mloc * 3 * S;
   // The member's operator parameter set (its Re): LU factors, correction profiles,
@@ -414,7 +418,11 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
         const unsigned EX = 0x7FF00000u;
         nonfin |= ((unsigned)__double2hiint(v.x) & EX) == EX || ((unsigned)__double2hiint(v.y) & EX) == EX;
         Ui[c * S + h] = v;
-        if (Ui32) Ui32[c * S + h] = make_float2(f64_to_f32(v.x), f64_to_f32(v.y));  // integer-pipe rounding
+        if (Ui32) {
+          const float2 f = make_float2(f64_to_f32(v.x), f64_to_f32(v.y));  // integer-pipe rounding
+          Ui32[c * S + h] = f;
+          reinterpret_cast<float2*>(R + c * LN + p)[0] = f;  // FP32 copy for the d_r mirror below
+        }
       }
     }
   }
@@ -427,6 +435,23 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     if ((tid & 31) == 0) { wnum[tid >> 5] = lnum; wden[tid >> 5] = lden; }
   }
   __syncthreads();
+  // J. mixed form: d_r of the new FP32 mirror (the theta-inverse's d_r u fields), with
+  // the transform kernels' stencil, so that they read one value instead of 7 levels.
+  if (Udr32) {
+    const float2* F = reinterpret_cast<const float2*>(R);  // FP32 value of line entry e at F[2e]
+    for (int p = tid; p < LN; p += nth) {
+      const int i = p / LM, mm = p - i * LM, k = k0 + mm;
+      if (k >= NTNZ) continue;
+      const int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
+      const size_t h = (size_t)i * NTNZ + k;
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const int tab = abs(spar[mm] - (c < 2 ? 1 : 0));
+        const float* Dr = tb.D32 + tab * STEN * NR + STEN * i + i0;
+        Udr32[c * S + h] = dr32_line(Dr, left, len, [&](int row) { return F[2 * (c * LN + row * LM + mm)]; });
+      }
+    }
+  }
   if (tid == 0) {
     if (!pred) {
       unsigned long long a = 0ull, b = 0ull;

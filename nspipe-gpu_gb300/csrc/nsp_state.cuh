@@ -47,4 +47,29 @@ __device__ __forceinline__ StateIn<T> member_input(const Tables& tb, const Bufs&
   return s;
 }
 
+// FP32 radial-derivative mirror of the member's transform input (mixed form, member
+// state only; explicit fields have none and the kernels apply the stencil themselves).
+__device__ __forceinline__ const float2* member_dr32(const Tables& tb, const Bufs& bf, const Ctl* ctl, int mloc,
+                                                    const double2* src) {
+  if (src || !bf.DR32[0]) return nullptr;
+  const int ph = ctl->phase[tb.mem0 + mloc];
+  const int which = (ph == 0) ? ctl->parity : (ctl->parity ^ 1);
+  return (which ? bf.DR32[1] : bf.DR32[0]) + (size_t)mloc * 3 * tb.S;
+}
+
+// d_r of one FP32 line value at level i (derivr_k, mod_radialFD.cu:10-30): the
+// 7-point parity stencil in FP32, terms in row order.  Shared by the linear pass
+// (which writes the DR32 mirror) and the transform kernels, so both give the same bits.
+template <typename LOAD>
+__device__ __forceinline__ float2 dr32_line(const float* Dr, int left, int len, LOAD ld) {
+  float vx = 0.f, vy = 0.f;
+  for (int j = 0; j < len; j++) {
+    const float de = __ldg(Dr + j);
+    const float2 a = ld(left + j);
+    vx += de * a.x;
+    vy += de * a.y;
+  }
+  return make_float2(vx, vy);
+}
+
 }  // namespace nsp

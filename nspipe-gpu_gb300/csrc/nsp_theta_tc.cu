@@ -24,10 +24,11 @@
 // [128 lines][K], B = the DFT matrix [N][K], D = A B^T in 128 TMEM lanes x N
 // columns, one line per lane, so the epilogue's stores are coalesced along l.
 // Persistent CTAs (one per SM) copy the DFT image once with a bulk async copy and
-// pipeline over tiles: fill tile j (all warps, independent loads) -> fence -> one
-// thread issues 3 K/8 MMAs into TMEM accumulator j % 2 and commits to an mbarrier
-// -> drain tile j-1's accumulator to global memory while tile j is on the tensor
-// cores.  Every wait is bounded: a CTA whose wait runs out records a fault in the
+// pipeline over tiles: tile j's operands (loaded into registers during the previous
+// iteration) go to shared memory -> fence -> one thread issues 3 K/8 MMAs into TMEM
+// accumulator j % 2 and commits to an mbarrier -> tile j+1's global loads are
+// issued -> tile j-1's accumulator drains to global memory while tile j is on the
+// tensor cores and tile j+1's loads are in flight.  Every wait is bounded: a CTA whose wait runs out records a fault in the
 // control block, waits (bounded) for its MMAs and still frees its TMEM.
 #include <algorithm>
 #include <cmath>
@@ -90,23 +91,34 @@ template <int NT, int NTP> struct InvJob {
   // Warp w fills lines 8w..8w+7; lane = line (lane % 8) x mode quarter (lane / 8), so
   // a warp's 32 stores of one K index hit 32 different banks.  Every load of a
   // thread is independent of the others (one line, J modes, up to 7 levels).
-  __device__ static void fill(const Tables& tb, const Bufs& bf, const Ctl* ctl, int mloc, int t, const double2* src,
-                              const float2* src32, unsigned char* ah, unsigned char* al) {
-    constexpr uint32_t SBO = (K / 4) * 128;
+  struct Regs { float vx[J], vy[J]; };  // one thread's share of a tile (line col, J modes)
+
+  // Global -> registers; the loop issues this for the next tile before draining the
+  // previous one, so the loads are in flight during the epilogue.
+  __device__ static void load(const Tables& tb, const Bufs& bf, const Ctl* ctl, int mloc, int t, const double2* src,
+                              const float2* src32, Regs& rg) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int col = warp * 8 + (lane & 7), mq = lane >> 3;
     const int NR = tb.NR, NZ = tb.NZ, NTNZ = tb.NTNZ;
     const long long S = tb.S;
     const int g = t * TM + col;
-    float vx[J], vy[J];
+    float* vx = rg.vx;
+    float* vy = rg.vy;
 #pragma unroll
     for (int j = 0; j < J; j++) { vx[j] = 0.f; vy[j] = 0.f; }
     if (g < columns(tb)) {
       const StateIn<float> U = member_input<float>(tb, bf, ctl, mloc, src, src32);
+      const float2* DR = member_dr32(tb, bf, ctl, mloc, src);  // d_r mirror of the member state, if any
       const int i = g / (9 * NZ), rem = g - i * 9 * NZ, f = rem / NZ, l = rem - f * NZ;
       const int comp = f < 3 ? f : (f < 6 ? f - 3 : f - 6);
       const size_t base = (size_t)comp * S + l;
-      if (f < 3) {
+      if (f >= 3 && f < 6 && DR) {  // d_r u from the mirror the linear pass wrote
+#pragma unroll
+        for (int j = 0; j < J; j++) {
+          const float2 a = __ldg(DR + (size_t)i * NTNZ + base + (size_t)(mq + 4 * j) * NZ);
+          vx[j] = a.x; vy[j] = a.y;
+        }
+      } else if (f < 3) {
 #pragma unroll
         for (int j = 0; j < J; j++) {
           cpx<float> a = U.ld((size_t)i * NTNZ + base + (size_t)(mq + 4 * j) * NZ);
@@ -141,11 +153,18 @@ template <int NT, int NTP> struct InvJob {
         }
       }
     }
+  }
+
+  // Registers -> the tile's operand stage (TF32 hi/lo split, core-matrix layout).
+  __device__ static void store(const Regs& rg, unsigned char* ah, unsigned char* al) {
+    constexpr uint32_t SBO = (K / 4) * 128;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int col = warp * 8 + (lane & 7), mq = lane >> 3;
 #pragma unroll
     for (int j = 0; j < J; j++) {
       const int it = mq + 4 * j;
-      put_split(ah, al, tc::koff(col, it, SBO), vx[j]);
-      put_split(ah, al, tc::koff(col, NT + it, SBO), vy[j]);
+      put_split(ah, al, tc::koff(col, it, SBO), rg.vx[j]);
+      put_split(ah, al, tc::koff(col, NT + it, SBO), rg.vy[j]);
     }
   }
 
@@ -177,13 +196,14 @@ template <int NT, int NTP> struct FwdJob {
   __device__ static int columns(const Tables& tb) { return 3 * tb.NR * tb.NZ; }
   __device__ static const float* image(const Tables& tb) { return tb.dft_fwd; }
 
-  __device__ static void fill(const Tables& tb, const Bufs& bf, const Ctl*, int mloc, int t, const double2*,
-                              const float2*, unsigned char* ah, unsigned char* al) {
-    constexpr uint32_t SBO = (K / 4) * 128;
+  struct Regs { cpx<float> h[J]; };
+
+  __device__ static void load(const Tables& tb, const Bufs& bf, const Ctl*, int mloc, int t, const double2*,
+                              const float2*, Regs& rg) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int col = warp * 8 + (lane & 7), pq = lane >> 3;
     const int NR = tb.NR, NZ = tb.NZ, g = t * TM + col;
-    cpx<float> h[J];
+    cpx<float>* h = rg.h;
 #pragma unroll
     for (int j = 0; j < J; j++) h[j] = mk<float>(0.f, 0.f);
     if (g < columns(tb)) {
@@ -195,11 +215,17 @@ template <int NT, int NTP> struct FwdJob {
         for (int j = 0; j < J; j++) h[j] = H[(size_t)(pq + 4 * j) * NZ];
       }
     }
+  }
+
+  __device__ static void store(const Regs& rg, unsigned char* ah, unsigned char* al) {
+    constexpr uint32_t SBO = (K / 4) * 128;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int col = warp * 8 + (lane & 7), pq = lane >> 3;
 #pragma unroll
     for (int j = 0; j < J; j++) {
       const int p = pq + 4 * j;
-      put_split(ah, al, tc::koff(col, p, SBO), h[j].x);
-      put_split(ah, al, tc::koff(col, NTP + p, SBO), h[j].y);
+      put_split(ah, al, tc::koff(col, p, SBO), rg.h[j].x);
+      put_split(ah, al, tc::koff(col, NTP + p, SBO), rg.h[j].y);
     }
   }
 
@@ -281,11 +307,20 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   auto wait_batch = [&](int b) -> bool {
     return __syncthreads_and(tc::mbar_wait(&bar_mma[b % ST], (uint32_t)((b / ST) & 1), WAIT_LIMIT)) != 0;
   };
-  for (int tile = blockIdx.x; tile < total && !fault; tile += gridDim.x) {
+  // This CTA's next tile at or after `from` whose member is active (uniform per CTA).
+  auto next_tile = [&](int from) -> int {
+    for (int tt = from; tt < total; tt += gridDim.x) {
+      bool skip;
+      member_source(tb, bf, ctl, tt / T, src, skip);
+      if (!skip) return tt;
+    }
+    return total;
+  };
+  typename JOB::Regs rg;
+  int tile = next_tile(blockIdx.x);
+  if (tile < total) JOB::load(tb, bf, ctl, tile / T, tile % T, src, src32, rg);
+  while (tile < total && !fault) {
     const int mloc = tile / T, t = tile - mloc * T;
-    bool skip;
-    member_source(tb, bf, ctl, mloc, src, skip);
-    if (skip) continue;
     const int j = issued;
     if (ST == 1 && drained < j) {  // the single operand stage is busy until batch j-1 completes
       if (!wait_batch(j - 1)) { fault = true; break; }
@@ -293,12 +328,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       tc::fence_after_sync();
     }
     unsigned char* ah = smraw + (j % ST) * 2 * A_BYTES;
-    JOB::fill(tb, bf, ctl, mloc, t, src, src32, ah, ah + A_BYTES);
+    JOB::store(rg, ah, ah + A_BYTES);
     tc::fence_async_smem();
     tc::fence_before_sync();
     __syncthreads();
     if (tid == 0) issue_3xtf32<K, N>(tmem + (uint32_t)((j & 1) * ACC), ah, ah + A_BYTES, sB, sB + B_BYTES, &bar_mma[j % ST]);
     issued = j + 1;
+    // Next tile's loads now, so that they are in flight while the previous tile drains.
+    const int nxt = next_tile(tile + gridDim.x);
+    if (nxt < total) JOB::load(tb, bf, ctl, nxt / T, nxt % T, src, src32, rg);
     if (j > 0) {  // drain the previous tile while this one is on the tensor cores
       if (drained < j) {
         if (!wait_batch(j - 1)) { fault = true; break; }
@@ -311,6 +349,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     __syncthreads();
     prev_m = mloc;
     prev_t = t;
+    tile = nxt;
   }
   if (!fault && issued > 0) {
     if (wait_batch(issued - 1)) {

@@ -621,6 +621,35 @@ __global__ void to_f32_k(const double2* __restrict__ src, float2* __restrict__ d
   }
 }
 
+// FP32 mirror U32 and its radial derivative DR32 of a group's state (step start):
+// the same conversion and stencil as the linear pass's stages I and J.
+__global__ void mirror_k(Tables tb, const double2* __restrict__ U, float2* __restrict__ U32, float2* __restrict__ DR32) {
+  const long long total = (long long)tb.nmem * 3 * tb.S;
+  const int NR = tb.NR, NT = tb.NT, NZ = tb.NZ, NTNZ = tb.NTNZ;
+  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
+    const long long line = q / tb.S;  // member * 3 + component
+    const long long h = q - line * tb.S;
+    const int c = (int)(line % 3), i = (int)(h / NTNZ), k = (int)(h - (long long)i * NTNZ);
+    const int it = k / NZ, m = it < NT / 2 ? it : it - NT;
+    const double2* col = U + line * tb.S + k;
+    const double2 a = col[(size_t)i * NTNZ];
+    U32[q] = make_float2(f64_to_f32(a.x), f64_to_f32(a.y));
+    const int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
+    const int tab = abs((abs(m) % 2) - (c < 2 ? 1 : 0));
+    const float* Dr = tb.D32 + tab * STEN * NR + STEN * i + i0;
+    DR32[q] = dr32_line(Dr, left, len, [&](int row) {
+      const double2 b = col[(size_t)row * NTNZ];
+      return make_float2(f64_to_f32(b.x), f64_to_f32(b.y));
+    });
+  }
+}
+
+void launch_mirror(const Tables& tb, const double2* U, float2* U32, float2* DR32, cudaStream_t st) {
+  const long long n = (long long)tb.nmem * 3 * tb.S;
+  const int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
+  mirror_k<<<blocks, 256, 0, st>>>(tb, U, U32, DR32);
+}
+
 void launch_to_f32(const double2* src, float2* dst, long long n, cudaStream_t st) {
   int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
   to_f32_k<<<blocks, 256, 0, st>>>(src, dst, n);
