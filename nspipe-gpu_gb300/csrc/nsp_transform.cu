@@ -283,6 +283,19 @@ __device__ __forceinline__ cpx<T> z_pair_spec(const cpx<T>* Ga, const cpx<T>* Gb
   return (direct || mirror) ? z : mk<T>(0, 0);
 }
 
+// The same for an index range known to be all direct (MIRROR false: q = n) or all
+// mirrored (MIRROR true: q = NZR - n, conjugated); q = 0 only where ZERO_OK.
+template <typename T, bool MIRROR, bool ZERO_OK>
+__device__ __forceinline__ cpx<T> z_pair_spec_in(const cpx<T>* Ga, const cpx<T>* Gb, bool dza, bool dzb, int qq, T kzs) {
+  cpx<T> a = Ga[qq], b = Gb[qq];
+  const T kz = kzs * (T)qq;
+  if (dza) a = mk<T>(-kz * a.y, kz * a.x);
+  if (dzb) b = mk<T>(-kz * b.y, kz * b.x);
+  if (MIRROR) { a.y = -a.y; b.y = -b.y; }
+  if (ZERO_OK && qq == 0) { a.y = (T)0; b.y = (T)0; }
+  return mk<T>(a.x - b.y, a.y + b.x);
+}
+
 template <typename T, int NZRC, int N1, int N2, int R>
 __global__ void __launch_bounds__(ZTH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl, int standalone) {
   static_assert(N1 * N2 == NZRC && R % 2 == 0 && NZRC % 3 == 0, "z split");
@@ -313,7 +326,15 @@ __global__ void __launch_bounds__(ZTH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl,
     const cpx<T>* Gb = Gi + (size_t)(fb < 9 ? fb : fb - 9) * fstride;
     cpx<T> x[N2];
 #pragma unroll
-    for (int n2 = 0; n2 < N2; n2++) x[n2] = z_pair_spec<T, NZ, NZRC>(Ga, Gb, fa >= 9, fb >= 9, n1 + N1 * n2, kzs);
+    for (int n2 = 0; n2 < N2; n2++) {
+      // The 16-wide range of n = n1 + N1 n2 is classified at compile time; only a
+      // range that straddles a boundary of the Hermitian extension takes the general path.
+      const int lo = N1 * n2, hi = lo + N1 - 1;
+      if (hi < NZ) x[n2] = z_pair_spec_in<T, false, true>(Ga, Gb, fa >= 9, fb >= 9, n1 + lo, kzs);
+      else if (lo > NZRC - NZ) x[n2] = z_pair_spec_in<T, true, false>(Ga, Gb, fa >= 9, fb >= 9, NZRC - n1 - lo, kzs);
+      else if (lo >= NZ && hi <= NZRC - NZ) x[n2] = mk<T>(0, 0);  // dealiasing band: no load
+      else x[n2] = z_pair_spec<T, NZ, NZRC>(Ga, Gb, fa >= 9, fb >= 9, n1 + lo, kzs);
+    }
     reg_fft<T, +1, N2>(x);
     cpx<T>* Yt = Y + (r * 6 + t) * YT + n1;
 #pragma unroll
