@@ -155,6 +155,13 @@ int nsp_grid(nsp_ctx* ctx, int member, double* r, double* rdr);
  * without the time stamp.  out holds NR doubles (host memory). */
 int nsp_mean_profile(nsp_ctx* ctx, int member, double* out);
 
+/* Cross-section integrals of one member at the NZR = 3(NZ-1) physical axial points
+ * z_n: q[n] = sum_i rdr_i <u_r^2 + u_theta^2>_theta and u[n] = sum_i rdr_i <u_z^2>_theta,
+ * the data rows of wrt_qcr / wrt_ucr (mod_io_nonlinear.cu:572-660; theta rule of
+ * q1kernel_k, radial rule of intq, mod_cublasflux.cu:119-130) without the time stamp.
+ * Computed in FP64 on the device; q and u are host arrays of NZR doubles. */
+int nsp_cross_sections(nsp_ctx* ctx, int member, double* q, double* u);
+
 /* Number of kernel launches issued by the last nsp_step call (all graph nodes run). */
 long long nsp_kernel_launches(nsp_ctx* ctx);
 

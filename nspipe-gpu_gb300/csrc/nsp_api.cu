@@ -64,6 +64,8 @@ struct nsp_ctx {
   double2* scratch = nullptr;  // 2 x 3 x Smax, for nsp_nonlinear
   float2* scratch32 = nullptr; // 3 x Smax, FP32 input of nsp_nonlinear in the mixed form
   unsigned long long* diagbuf = nullptr;  // 2 ordered-bit maxima of the divergence diagnostic
+  double* crossbuf = nullptr;             // per-level partials of the cross-section diagnostics
+  size_t crossbuf_n = 0;
   // Parallel branches of the step graph: one per member group beyond the first.
   std::vector<cudaStream_t> side;
   cudaEvent_t ev_fork = nullptr;
@@ -853,6 +855,36 @@ int nsp_diag(nsp_ctx* c, int m, nsp_diag_out* out) {
   memcpy(dv, bits, sizeof dv);
   out->div_max = dv[0];
   out->div_wall = dv[1];
+  return NSP_OK;
+}
+
+int nsp_cross_sections(nsp_ctx* c, int m, double* q, double* u) {
+  if (int rc = check_member(c, m)) return rc;
+  if (!q || !u) return fail(c, NSP_ERR_ARG, "null output");
+  if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_cross_sections before nsp_setup");
+  const Group& g = c->groups[c->grp[m]];
+  const int NR = g.tb.NR, NZR = g.tb.NZR;
+  const size_t n = (size_t)2 * NR * NZR;
+  if (c->crossbuf_n < n) {  // grows to the largest member shape asked for, then reused
+    void* p = nullptr;
+    if (int rc = dalloc(c, &p, n * sizeof(double))) return rc;
+    c->crossbuf = static_cast<double*>(p);
+    c->crossbuf_n = n;
+  }
+  launch_diag_cross(g.tb, state_ptr(c, m, 0), c->crossbuf, c->st);
+  CK(cudaGetLastError());
+  std::vector<double> part(n);
+  CK(cudaMemcpyAsync(part.data(), c->crossbuf, n * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  for (int z = 0; z < NZR; z++) {
+    double sq = 0.0, su = 0.0;
+    for (int i = 0; i < NR; i++) {  // the radial quadrature, in level order
+      sq += part[(size_t)i * NZR + z];
+      su += part[(size_t)(NR + i) * NZR + z];
+    }
+    q[z] = sq;
+    u[z] = su;
+  }
   return NSP_OK;
 }
 

@@ -114,6 +114,8 @@ void launch_lusolve(const Tables& tb, int kind, const double2* rhs, double2* sol
 void launch_fp64_peak(double* out, int blocks, int threads, int iters, cudaStream_t st);
 // max |div u| over the interior rows -> out[0], over the wall row -> out[1] (ordered bits).
 void launch_diag_div(const Tables& tb, const double2* U, unsigned long long* out, cudaStream_t st);
+// Per-level partials of the q / u cross-section diagnostics: part[2][NR][NZR].
+void launch_diag_cross(const Tables& tb, const double2* U, double* part, cudaStream_t st);
 // Fixed device scratch of the allocation-free entry point (nsp_noalloc.cu).
 size_t noalloc_scratch_bytes();
 cudaError_t noalloc_scratch(int device, void** ptr);

@@ -556,6 +556,58 @@ void launch_diag_div(const Tables& tb, const double2* U, unsigned long long* out
   diag_div_k<<<(tb.NTNZ + 127) / 128, 128, 0, st>>>(tb, U, out);
 }
 
+// Cross-section diagnostics of one member's state (wrt_qcr / wrt_ucr with q0kernel_k,
+// u0kernel_k, q1kernel_k and intq, mod_io_nonlinear.cu:54-117, 572-660 and
+// mod_cublasflux.cu:119-130): at every physical axial point z_n,
+//   q(z_n) = sum_i rdr_i (1/NTP) sum_theta (u_r^2 + u_theta^2),   u(z_n) = the same with u_z^2.
+// (The reference's periodic Simpson rule in theta with unit weights sums to the plain
+// mean.)  The theta mean is taken by Parseval from the spectral coefficients: at
+// (r_i, z_n), u(theta) = Re sum_m P_m e^{i m theta} with P_m = c_{m,0} + 2 sum_{l>0}
+// c_{m,l} e^{i k_l z_n} (the reference's C2R extension), whose mean square is
+// (Re P_0)^2 + 2 sum_{0<mu<NT/2} |(P_mu + conj P_-mu)/2|^2 + |P_-NT/2|^2 / 2.
+// One thread per (level, z_n); per-level partials rdr_i * mean square go to
+// part[2][NR][NZR], summed over i on the host in a fixed order.
+__global__ void diag_cross_k(Tables tb, const double2* __restrict__ U, double* __restrict__ part) {
+  const int i = blockIdx.y, n = blockIdx.x * blockDim.x + threadIdx.x;
+  const int NT = tb.NT, NZ = tb.NZ, NZR = tb.NZR, NTNZ = tb.NTNZ;
+  if (n >= NZR) return;
+  const long long S = tb.S;
+  double ms[3];
+  for (int c = 0; c < 3; c++) {
+    const double2* col = U + c * S + (size_t)i * NTNZ;
+    // P of theta slot it at z_n
+    auto P = [&](int it) {
+      const double2* a = col + (size_t)it * NZ;
+      double px = a[0].x, py = a[0].y;
+      for (int l = 1; l < NZ; l++) {
+        const double2 w = tb.tw_z[(size_t)l * n % NZR];  // exp(-2 pi i l n / NZR); E_l = conj(w)
+        const double2 b = a[l];
+        px += 2.0 * (b.x * w.x + b.y * w.y);
+        py += 2.0 * (b.y * w.x - b.x * w.y);
+      }
+      return make_double2(px, py);
+    };
+    const double2 p0 = P(0);
+    double s = p0.x * p0.x;
+    for (int mu = 1; mu < NT / 2; mu++) {
+      const double2 pp = P(mu), pm = P(NT - mu);
+      const double qx = 0.5 * (pp.x + pm.x), qy = 0.5 * (pp.y - pm.y);
+      s += 2.0 * (qx * qx + qy * qy);
+    }
+    const double2 pn = P(NT / 2);  // m = -NT/2, no +NT/2 partner
+    s += 0.5 * (pn.x * pn.x + pn.y * pn.y);
+    ms[c] = s;
+  }
+  const double w = tb.rdr[i];
+  part[(size_t)i * NZR + n] = w * (ms[0] + ms[1]);
+  part[(size_t)(tb.NR + i) * NZR + n] = w * ms[2];
+}
+
+void launch_diag_cross(const Tables& tb, const double2* U, double* part, cudaStream_t st) {
+  dim3 g((tb.NZR + 63) / 64, tb.NR);
+  diag_cross_k<<<g, 64, 0, st>>>(tb, U, part);
+}
+
 // FP64 throughput probe: 8 independent multiply-add chains per thread, no memory
 // traffic; the measured denominator of the FP64 roofline.
 __global__ void fp64_peak_k(double* out, int iters, double a, double b) {

@@ -25,7 +25,7 @@ EXPORTS = [
     "nsp_set_state_host", "nsp_get_state_host", "nsp_set_state_device", "nsp_get_state_device",
     "nsp_step", "nsp_nonlinear", "nsp_lusolve", "nsp_diag", "nsp_grid", "nsp_kernel_launches",
     "nsp_sync", "nsp_last_error", "nsp_destroy", "nsp_set_stream", "nsp_profile_stages",
-    "nsp_measure_fp64_peak", "nsp_nonlinear_static", "nsp_describe", "nsp_mean_profile",
+    "nsp_measure_fp64_peak", "nsp_nonlinear_static", "nsp_describe", "nsp_mean_profile", "nsp_cross_sections",
 ]
 
 
@@ -87,6 +87,7 @@ def lib():
         L.nsp_nonlinear_static.argtypes = [vp, ip, vp, vp]
         L.nsp_describe.argtypes = [vp, ctypes.c_char_p, ip]
         L.nsp_mean_profile.argtypes = [vp, ip, dp]
+        L.nsp_cross_sections.argtypes = [vp, ip, dp, dp]
         L.nsp_last_error.argtypes = [vp]
         L.nsp_last_error.restype = ctypes.c_char_p
         L.nsp_destroy.argtypes = [vp]
@@ -246,6 +247,14 @@ class Stepper:
         out = np.zeros(self.params[m].NR)
         self._check(lib().nsp_mean_profile(self._h, m, _dp(out)))
         return out
+
+    def cross_sections(self, m=0):
+        """(q, u): r-integrated theta means of u_r^2 + u_theta^2 and of u_z^2 at the NZR
+        physical axial points (the data rows of the reference's q / u cross-section files)."""
+        nzr = 3 * (self.params[m].NZ - 1)
+        q, u = np.zeros(nzr), np.zeros(nzr)
+        self._check(lib().nsp_cross_sections(self._h, m, _dp(q), _dp(u)))
+        return q, u
 
     def grid(self, m=0):
         NR = self.params[m].NR

@@ -48,7 +48,8 @@ void orc_div_wall(orc_ctx* c, double* div1, const double* ur, const double* ut, 
 void orc_nonlinear(orc_ctx* c, const double* ur, const double* ut, const double* uz,
                    double* nr, double* nt, double* nz);
 /* Physical-space 2-D transforms of one radial level: spectral double2[NT][NZ] <-> real
- * double[NTP][2*NZP] (the in-place cuFFT layout of mod_fft.cu:23-26). */
+ * double[NTP][NZR] (the physical theta x z points of the in-place cuFFT layout of
+ * mod_fft.cu:23-26, without its two padding entries per theta row). */
 void orc_level_backward(orc_ctx* c, const double* spec_level, double* phys_level);
 void orc_level_forward(orc_ctx* c, const double* phys_level, double* spec_level);
 

@@ -57,6 +57,28 @@ def test_diag_matches_oracle(nsp, orc):
     st.close()
 
 
+def test_cross_sections_match_oracle(nsp, orc):
+    """q and u cross-section rows (the reference's wrt_qcr / wrt_ucr data) against the
+    oracle's physical-space levels: r-weighted theta means of u_r^2 + u_theta^2, u_z^2."""
+    name = "c0"
+    o = orc(name)
+    NR = CFG[name][0]
+    st = stepper(nsp, name, nsp.NSP_FP64)
+    st.set_state(0, init(nsp, name))
+    st.step(2)
+    u = st.get_state(0)
+    q, uu = st.cross_sections(0)
+    rdr = o.grid()["rdr"]
+    q_ref, u_ref = np.zeros_like(q), np.zeros_like(uu)
+    for i in range(NR):
+        pr, pt, pz = (o.level_backward(a[i]) for a in u)  # [NTP][NZR] physical values
+        q_ref += rdr[i] * (pr ** 2 + pt ** 2).mean(axis=0)
+        u_ref += rdr[i] * (pz ** 2).mean(axis=0)
+    assert rel(q, q_ref) < 1e-12
+    assert rel(uu, u_ref) < 1e-12
+    st.close()
+
+
 def _low(u, NT):
     m_slots = [0, 1, 2, 3, 4, NT - 4, NT - 3, NT - 2, NT - 1]
     return np.stack([a[:, m_slots, :6] for a in u])
