@@ -190,6 +190,103 @@ int nsp_profile_stages(nsp_ctx* ctx, int reps, double* ms_out);
  * best of 3 timed launches), the denominator of the FP64 roofline. */
 int nsp_measure_fp64_peak(nsp_ctx* ctx, double* tflops);
 
+/* Parameters of one member; the context's member count and precision (either
+ * output pointer may be NULL). */
+int nsp_get_params(nsp_ctx* ctx, int member, nsp_params* out);
+int nsp_info(nsp_ctx* ctx, int* n_members, int* precision);
+
+/* ---- Time-integration driver ------------------------------------------------------
+ * The reference's integrate() (mod_integrate.cu:98-160) around nsp_step: the time
+ * accumulators and output cadence of mod_integrate.cu:109,131-152, the diagnostic
+ * files of setIO / wrt_frc / wrt_qcr / wrt_ucr / wrt_mpr (mod_io_nonlinear.cu:260-318,
+ * 460-687) in the reference's text formats, the final state dump of main.cu:42-44, and
+ * (no reference counterpart) periodic checkpoints with a metadata sidecar from which
+ * an interrupted run resumes with the same output files it would have written.
+ *
+ * Output cadence, per member and per file: after each step the member's dt is added
+ * to its time t and to the file's accumulator (double additions, in the reference's
+ * order); when the accumulator is >= the file's interval a row is sampled and the
+ * accumulator reset to 0.  An interval < 0 switches the file off.
+ *
+ * Files, one member: io_friction.txt, io_qcross.txt, io_ucross.txt and io_meanpr.txt
+ * in out_dir; several members: the same names in out_dir/member_NNNN/ (NNNN the
+ * member index, 4 digits).  Formats (each value "%.8e", as the reference prints):
+ *   io_friction.txt  rows "t  u_centre  u_tau"                            (no header)
+ *   io_qcross.txt    header 0, z_0 .. z_{NZR-1}; rows t, q[NZR]    (z_n = LZ n / NZR)
+ *   io_ucross.txt    header 0, z_0 .. z_{NZR-1}; rows t, u[NZR]
+ *   io_meanpr.txt    header 0, r_0 .. r_{NR-1};  rows t, Re u_z(0,0)(r_i)
+ * The reference writes rows in blocks of dc rows and drops a final partial block;
+ * here rows are written in blocks of rows_per_write, and every pending row is written
+ * at each checkpoint and by nsp_run_close.
+ *
+ * Checkpoints: ckpt_dir/step_SSSSSSSSSS/ (S the steps since the run opened, 10
+ * digits) holds each member's ur_s.bin, ut_s.bin, uz_s.bin (one member: in the
+ * directory itself, so that it is a restart directory of the reference, initField
+ * mod_io_nonlinear.cu:426-429; several: in member_NNNN/) and checkpoint.json, written
+ * last: the parameters, time, step and output accumulators of every member, the
+ * FNV-1a 64 checksum of each state file and the size each output file had. */
+typedef struct nsp_run_opts {
+  const char* out_dir;  /* directory of the diagnostic files (created); NULL: no files   */
+  double dt_frc;        /* interval of io_friction.txt rows              head.h:33     */
+  double dt_qcr;        /* of io_qcross.txt and io_ucross.txt rows      head.h:36     */
+  double dt_mnp;        /* of io_meanpr.txt rows                        head.h:39     */
+  int rows_per_write;   /* rows buffered per file write (dc_frc/dc_qcr/dc_mnp) head.h:34-40 */
+  const char* ckpt_dir; /* checkpoint directory (created); NULL: no checkpoints          */
+  int ckpt_every;       /* steps between periodic checkpoints; 0: only nsp_run_checkpoint */
+  int ckpt_keep;        /* complete checkpoints kept, older ones removed; 0: keep all    */
+  int final_state;      /* nsp_run_close writes ur.bin, ut.bin, uz.bin of each member to
+                           its output directory (main.cu:42-44)                         */
+  int verbose;          /* print the reference's progress lines at each friction row
+                           (mod_integrate.cu:136)                                       */
+} nsp_run_opts;
+
+typedef struct nsp_run nsp_run;
+
+/* The reference's schedule: out_dir ".", every interval 0.5, 100 rows per write, no
+ * checkpoints (ckpt_every 0, ckpt_keep 2), final_state 1, verbose 0. */
+int nsp_run_default_opts(nsp_run_opts* o);
+
+/* Starts a run at t = 0 on the context's current state (after nsp_setup and the
+ * initial field): creates the output files and writes their header rows (setIO). */
+int nsp_run_open(nsp_ctx* ctx, const nsp_run_opts* o, nsp_run** out);
+
+/* Resumes a run from a checkpoint: ckpt is a step_* directory, or a checkpoint
+ * directory (its newest complete checkpoint is taken).  Checks that the context has
+ * the checkpoint's members and parameters and that every state file has its recorded
+ * size and checksum (NSP_ERR_ARG / NSP_ERR_IO otherwise), loads the states, restores
+ * the times and accumulators, and cuts each output file back to its recorded size so
+ * that the rows written after the checkpoint are written again exactly once. */
+int nsp_run_resume(nsp_ctx* ctx, const nsp_run_opts* o, const char* ckpt, nsp_run** out);
+
+/* Advances every member by nsteps steps (nsp_step in chunks that end where a row or a
+ * periodic checkpoint is due), writing rows and checkpoints on the way.  iters_out
+ * (optional): nsteps * n_members corrector iteration counts, step-major.  A member
+ * whose field becomes non-finite ends the call with NSP_ERR_NONFINITE after the rows
+ * of that chunk are written, and no checkpoint is written for that state. */
+int nsp_run_advance(nsp_run* run, int nsteps, int* iters_out);
+
+/* Writes a checkpoint of the current state now (pending rows are written first). */
+int nsp_run_checkpoint(nsp_run* run);
+
+/* Time and steps of one member since the run's t = 0. */
+int nsp_run_time(nsp_run* run, int member, double* t, long long* steps);
+
+/* Writes pending rows, the final states when final_state is set, closes the files and
+ * frees the run (not the context).  A NULL run is a no-op. */
+int nsp_run_close(nsp_run* run);
+
+/* Host only (no context, no GPU): finds the checkpoint as nsp_run_resume does, checks
+ * its state files against the sidecar, and copies the sidecar (JSON) and the resolved
+ * checkpoint directory into json / path (either may be NULL; NUL-terminated).
+ * NSP_ERR_IO for a missing, incomplete or corrupt checkpoint, NSP_ERR_ARG if a buffer
+ * is too small. */
+int nsp_checkpoint_info(const char* ckpt, char* json, int json_cap, char* path, int path_cap);
+
+/* Host only: the output cadence.  For nsteps steps of length dt from accumulator *acc,
+ * due[j] = 1 if a row is sampled after step j+1, else 0; *acc is updated.  An
+ * interval < 0 gives no rows. */
+int nsp_output_schedule(double dt, double interval, int nsteps, double* acc, unsigned char* due);
+
 /* Waits for all work of the context. */
 int nsp_sync(nsp_ctx* ctx);
 

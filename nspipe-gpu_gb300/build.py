@@ -24,7 +24,7 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I", o
              "-I", os.path.join(HERE, "..", "include")]
 
 CU_UNITS = ["nsp_api.cu", "nsp_linear.cu", "nsp_transform.cu", "nsp_noalloc.cu", "nsp_theta_tc.cu"]
-CXX_UNITS = ["nsp_setup.cpp"]
+CXX_UNITS = ["nsp_setup.cpp", "nsp_run.cpp"]
 HEADERS = ["nsp_internal.h", "nsp_fft.cuh", "nsp_cvt.cuh", "nsp_state.cuh", "nsp_tc.cuh", os.path.join("..", "..", "include", "nspipe_gb300.h")]
 
 

@@ -371,6 +371,13 @@ int build_graph(nsp_ctx* c) {
 
 }  // namespace
 
+namespace nsp {
+int ctx_fail(nsp_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+}  // namespace nsp
+
 extern "C" {
 
 int nsp_default_params(nsp_params* p) {
@@ -1014,6 +1021,20 @@ int nsp_measure_fp64_peak(nsp_ctx* c, double* tflops) {
 int nsp_sync(nsp_ctx* c) {
   if (!c) return NSP_ERR_ARG;
   CK(cudaStreamSynchronize(c->st));
+  return NSP_OK;
+}
+
+int nsp_get_params(nsp_ctx* c, int m, nsp_params* out) {
+  if (int rc = check_member(c, m)) return rc;
+  if (!out) return fail(c, NSP_ERR_ARG, "null output");
+  *out = c->prm[m];
+  return NSP_OK;
+}
+
+int nsp_info(nsp_ctx* c, int* n_members, int* precision) {
+  if (!c) return NSP_ERR_ARG;
+  if (n_members) *n_members = c->nmem;
+  if (precision) *precision = c->precision;
   return NSP_OK;
 }
 

@@ -132,6 +132,9 @@ void configure_theta_tc_kernels();
 void launch_theta_tc(const Tables& tb, const Bufs& bf, Ctl* dctl, int dir, const double2* src, const float2* src32,
                      double2* dst, cudaStream_t st);
 
+// Records msg as the context's last error (nsp_last_error) and returns code.
+int ctx_fail(nsp_ctx* c, int code, const std::string& msg);
+
 // Host-side operator construction (nsp_setup.cpp).
 struct HostOps {
   int NR;

@@ -26,6 +26,8 @@ EXPORTS = [
     "nsp_step", "nsp_nonlinear", "nsp_lusolve", "nsp_diag", "nsp_grid", "nsp_kernel_launches",
     "nsp_sync", "nsp_last_error", "nsp_destroy", "nsp_set_stream", "nsp_profile_stages",
     "nsp_measure_fp64_peak", "nsp_nonlinear_static", "nsp_describe", "nsp_mean_profile", "nsp_cross_sections",
+    "nsp_get_params", "nsp_info", "nsp_run_default_opts", "nsp_run_open", "nsp_run_resume", "nsp_run_advance",
+    "nsp_run_checkpoint", "nsp_run_time", "nsp_run_close", "nsp_checkpoint_info", "nsp_output_schedule",
 ]
 
 
@@ -44,6 +46,15 @@ class NspDiag(ctypes.Structure):
         ("u_centre", ctypes.c_double), ("u_tau", ctypes.c_double), ("flux", ctypes.c_double),
         ("last_err", ctypes.c_double), ("last_iters", ctypes.c_int), ("status", ctypes.c_int),
         ("re_tau", ctypes.c_double), ("div_max", ctypes.c_double), ("div_wall", ctypes.c_double),
+    ]
+
+
+class NspRunOpts(ctypes.Structure):
+    _fields_ = [
+        ("out_dir", ctypes.c_char_p), ("dt_frc", ctypes.c_double), ("dt_qcr", ctypes.c_double),
+        ("dt_mnp", ctypes.c_double), ("rows_per_write", ctypes.c_int), ("ckpt_dir", ctypes.c_char_p),
+        ("ckpt_every", ctypes.c_int), ("ckpt_keep", ctypes.c_int), ("final_state", ctypes.c_int),
+        ("verbose", ctypes.c_int),
     ]
 
 
@@ -88,6 +99,17 @@ def lib():
         L.nsp_describe.argtypes = [vp, ctypes.c_char_p, ip]
         L.nsp_mean_profile.argtypes = [vp, ip, dp]
         L.nsp_cross_sections.argtypes = [vp, ip, dp, dp]
+        L.nsp_get_params.argtypes = [vp, ip, ctypes.POINTER(NspParams)]
+        L.nsp_info.argtypes = [vp, ctypes.POINTER(ip), ctypes.POINTER(ip)]
+        L.nsp_run_default_opts.argtypes = [ctypes.POINTER(NspRunOpts)]
+        L.nsp_run_open.argtypes = [vp, ctypes.POINTER(NspRunOpts), ctypes.POINTER(vp)]
+        L.nsp_run_resume.argtypes = [vp, ctypes.POINTER(NspRunOpts), ctypes.c_char_p, ctypes.POINTER(vp)]
+        L.nsp_run_advance.argtypes = [vp, ip, ctypes.POINTER(ip)]
+        L.nsp_run_checkpoint.argtypes = [vp]
+        L.nsp_run_time.argtypes = [vp, ip, dp, ctypes.POINTER(ctypes.c_longlong)]
+        L.nsp_run_close.argtypes = [vp]
+        L.nsp_checkpoint_info.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ip, ctypes.c_char_p, ip]
+        L.nsp_output_schedule.argtypes = [ctypes.c_double, ctypes.c_double, ip, dp, ctypes.POINTER(ctypes.c_ubyte)]
         L.nsp_last_error.argtypes = [vp]
         L.nsp_last_error.restype = ctypes.c_char_p
         L.nsp_destroy.argtypes = [vp]
@@ -280,3 +302,77 @@ class Stepper:
 
     def sync(self):
         self._check(lib().nsp_sync(self._h))
+
+
+def output_schedule(dt, interval, nsteps, acc=0.0):
+    """The output cadence of the run driver: (due, acc) where due[j] is True when a row
+    is written after step j+1 (accumulator += dt per step, row when >= interval)."""
+    due = np.zeros(nsteps, np.uint8)
+    a = ctypes.c_double(acc)
+    rc = lib().nsp_output_schedule(dt, interval, nsteps, ctypes.byref(a),
+                                   due.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)))
+    if rc != NSP_OK:
+        raise NspError(rc, "nsp_output_schedule")
+    return due.astype(bool), a.value
+
+
+def checkpoint_info(path):
+    """(sidecar dict, resolved checkpoint directory) of a checkpoint, after checking its
+    state files against the sidecar; NspError(NSP_ERR_IO) if missing or corrupt."""
+    js = ctypes.create_string_buffer(1 << 20)
+    where = ctypes.create_string_buffer(4096)
+    rc = lib().nsp_checkpoint_info(os.fsencode(path), js, len(js), where, len(where))
+    if rc != NSP_OK:
+        raise NspError(rc, "checkpoint %s unusable" % path)
+    return json.loads(js.value.decode()), where.value.decode()
+
+
+class Run:
+    """The reference's integrate() around a Stepper: the output files io_friction.txt,
+    io_qcross.txt, io_ucross.txt, io_meanpr.txt at their cadence, periodic checkpoints
+    with a JSON sidecar, and resume (include/nspipe_gb300.h, nsp_run_*).
+
+    Keyword arguments are the fields of nsp_run_opts; resume= names a checkpoint (a
+    step_* directory or a checkpoint directory) to continue from."""
+
+    def __init__(self, stepper, out_dir=".", dt_frc=0.5, dt_qcr=0.5, dt_mnp=0.5, rows_per_write=100,
+                 ckpt_dir=None, ckpt_every=0, ckpt_keep=2, final_state=True, verbose=False, resume=None):
+        self.stepper = stepper
+        o = NspRunOpts()
+        lib().nsp_run_default_opts(ctypes.byref(o))
+        self._strings = [os.fsencode(out_dir) if out_dir is not None else None,
+                         os.fsencode(ckpt_dir) if ckpt_dir is not None else None]
+        o.out_dir, o.ckpt_dir = self._strings
+        o.dt_frc, o.dt_qcr, o.dt_mnp = float(dt_frc), float(dt_qcr), float(dt_mnp)
+        o.rows_per_write, o.ckpt_every, o.ckpt_keep = rows_per_write, ckpt_every, ckpt_keep
+        o.final_state, o.verbose = int(bool(final_state)), int(bool(verbose))
+        self._h = ctypes.c_void_p()
+        if resume is None:
+            rc = lib().nsp_run_open(stepper._h, ctypes.byref(o), ctypes.byref(self._h))
+        else:
+            rc = lib().nsp_run_resume(stepper._h, ctypes.byref(o), os.fsencode(resume), ctypes.byref(self._h))
+        stepper._check(rc)
+
+    def advance(self, nsteps):
+        iters = np.zeros((nsteps, self.stepper.n), np.int32)
+        self.stepper._check(lib().nsp_run_advance(self._h, nsteps, iters.ctypes.data_as(ctypes.POINTER(ctypes.c_int))))
+        return iters
+
+    def checkpoint(self):
+        self.stepper._check(lib().nsp_run_checkpoint(self._h))
+
+    def time(self, m=0):
+        t, n = ctypes.c_double(), ctypes.c_longlong()
+        self.stepper._check(lib().nsp_run_time(self._h, m, ctypes.byref(t), ctypes.byref(n)))
+        return t.value, n.value
+
+    def close(self):
+        if self._h:
+            h, self._h = self._h, None
+            self.stepper._check(lib().nsp_run_close(h))
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

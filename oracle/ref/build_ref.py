@@ -14,6 +14,11 @@ build.  This script
                      wrapping nonlinear() at link time to count calls,
   run(cfg, mode, ..) runs it in oracle/_ref/<cfg>/<mode>/run/ on given u?_s.bin.
 
+Modes: 'trace' (nsteps=1, integrate() called once per step), 'time' (nsteps=N,
+one integrate() call, output files off) and 'io' (as 'time', with the output
+schedule IO_SCHEDULE patched into head.h:33-40 so that integrate() writes its
+io_*.txt files into the run directory).
+
 No reference source is modified other than the #define values; nothing is
 copied into the tracked tree.
 """
@@ -55,7 +60,13 @@ def stage(src=REF_SRC_DEFAULT):
     return dst
 
 
-def _patch_header(text, NR, NT, NZ, LZ, Re, dt, nsteps):
+# mode 'io': dt_frc, dt_qcr, dt_mnp (head.h:33,36,39) and the rows buffered per write
+# dc_frc = dc_qcr = dc_mnp (head.h:34,37,40).  With dt = 0.005 (s2) the accumulated
+# time reaches 0.05 only after 11 steps (ten additions of 0.005 fall short of 0.05).
+IO_SCHEDULE = (0.015, 0.05, 0.035, 4)
+
+
+def _patch_header(text, NR, NT, NZ, LZ, Re, dt, nsteps, io=None):
     def sub(name, value):
         nonlocal text
         pat = re.compile(r"^#define\s+%s\b.*$" % re.escape(name), re.M)
@@ -68,8 +79,11 @@ def _patch_header(text, NR, NT, NZ, LZ, Re, dt, nsteps):
     sub("LZ", LZ)
     sub("Re", "(%r)" % float(Re))
     sub("restart", 1)
-    for k in ("dt_frc", "dt_qcr", "dt_mnp"):
-        sub(k, "1e30")
+    for k, v in zip(("dt_frc", "dt_qcr", "dt_mnp"), io[:3] if io else (1e30,) * 3):
+        sub(k, repr(float(v)))
+    if io:
+        for k in ("dc_frc", "dc_qcr", "dc_mnp"):
+            sub(k, int(io[3]))
     sub("dt", repr(float(dt)))
     sub("nsteps", nsteps)
     return text
@@ -92,7 +106,7 @@ def build(cfg, mode="trace", nsteps=None, jobs=8):
     with open(os.path.join(out, "head.h")) as fh:
         hdr = fh.read()
     with open(os.path.join(out, "head.h"), "w") as fh:
-        fh.write(_patch_header(hdr, NR, NT, NZ, LZ, Re, dt, nsteps))
+        fh.write(_patch_header(hdr, NR, NT, NZ, LZ, Re, dt, nsteps, IO_SCHEDULE if mode == "io" else None))
     shutil.copy2(os.path.join(HERE, "ref_driver.cu"), os.path.join(out, "ref_driver.cu"))
     units = sorted(f for f in os.listdir(out) if f.endswith(".cu") and f != "main.cu")
 
@@ -115,7 +129,7 @@ def run(cfg, mode, fields_dir, nsteps, snaps=None, nsteps_build=None):
     os.makedirs(rundir, exist_ok=True)
     for c in "rtz":
         shutil.copy2(os.path.join(fields_dir, "u%s_s.bin" % c), os.path.join(rundir, "u%s_s.bin" % c))
-    args = [exe, mode, str(nsteps)] + ([",".join(str(s) for s in snaps)] if snaps else [])
+    args = [exe, "trace" if mode == "trace" else "time", str(nsteps)] + ([",".join(str(s) for s in snaps)] if snaps else [])
     p = subprocess.run(args, cwd=rundir, capture_output=True, text=True)
     with open(os.path.join(rundir, "stdout.txt"), "w") as fh:
         fh.write(p.stdout + p.stderr)

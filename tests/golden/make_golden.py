@@ -15,6 +15,11 @@ recorded) and reduces the snapshots it writes to fixtures:
     component L2 norms and 8 seeded random projections of every component
     (a checksum of the whole field).
 
+'io_s2' runs s2 from its seeded field for 100 steps in the 'io' mode (output
+schedule build_ref.IO_SCHEDULE: rows every 0.015 / 0.05 / 0.035 time units, 4
+rows per write) and keeps the four files integrate() writes, io_friction.txt,
+io_qcross.txt, io_ucross.txt and io_meanpr.txt, as written (tests/golden/io_s2/).
+
 The projections use real weights w ~ N(0,1) from SplitMix64(seed ^ 0x5bd1e995):
 p = sum_h w_h u_h over the flattened field.
 """
@@ -60,11 +65,34 @@ def reduce_field(u, seed):
     return out
 
 
+IO_FILES = ("io_friction.txt", "io_qcross.txt", "io_ucross.txt", "io_meanpr.txt")
+
+
+def make_io(outdir, cfg="s2", nsteps=100):
+    amp, seed = RUNS[cfg][:2]
+    NR, NT, NZ, LZexpr, Re, dt = build_ref.CONFIGS[cfg]
+    LZ = eval(LZexpr.replace("PI2", repr(PI2)))
+    init_dir = os.path.join(tempfile.mkdtemp(prefix="nsp_golden_"), cfg + "_init")
+    write_state(seeded_field(NR, NT, NZ, LZ, amp, seed), init_dir)
+    rundir = build_ref.run(cfg, "io", init_dir, nsteps, nsteps_build=nsteps)
+    dst = os.path.join(outdir, "io_" + cfg)
+    os.makedirs(dst, exist_ok=True)
+    for f in IO_FILES:
+        shutil.copy2(os.path.join(rundir, f), os.path.join(dst, f))
+    shutil.rmtree(init_dir)
+    print("io", cfg, sorted(os.listdir(dst)), flush=True)
+
+
 def main():
     outdir = os.path.abspath(sys.argv[1])
     cfgs = sys.argv[2:] or ["s2", "c0", "c1"]
     os.makedirs(outdir, exist_ok=True)
     summary = {}
+    if "io_s2" in cfgs:
+        make_io(outdir)
+        cfgs = [c for c in cfgs if c != "io_s2"]
+        if not cfgs:
+            return
     for cfg in cfgs:
         amp, seed, nsteps, snaps, full = RUNS[cfg]
         NR, NT, NZ, LZexpr, Re, dt = build_ref.CONFIGS[cfg]
