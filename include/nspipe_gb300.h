@@ -287,9 +287,43 @@ int nsp_checkpoint_info(const char* ckpt, char* json, int json_cap, char* path, 
  * interval < 0 gives no rows. */
 int nsp_output_schedule(double dt, double interval, int nsteps, double* acc, unsigned char* due);
 
+/* ---- Re_Mesh: change of resolution ------------------------------------------------
+ * The reference's Re_Mesh tool (tools/Re_Mesh/src/mod_remesh.cu:50-124; its main
+ * main.cu:14-33) as a batched device kernel.  A plan maps fields of shape (NR, NT, NZ)
+ * to (Nrd, Ntd, Nzd): radial Lagrange interpolation on 2*iw points of the old grid
+ * extended by iw points mirrored across the axis, with even / odd folding by the
+ * parity of m and component (rmsh_k :8-29; weights fd_weights_rmsh :152-178; table
+ * :70-115, the mirrored points' columns as the tool assigns them); theta and z modes
+ * kept where both grids have them (-Ntd/2 <= m < Ntd/2, l < Nzd), zero elsewhere;
+ * mode (0,0) with u_r = 0 and zero imaginary parts (modeZZ_k :34-40).  Grids of both
+ * resolutions are init_fd's.  A member's field is its three components (u_r, u_theta,
+ * u_z) back to back, each in the state layout above. */
+typedef struct nsp_remesh nsp_remesh;
+
+/* Builds the plan's tables on the host (no device work until the first launch);
+ * iw in [1, 8] (the tool's default is 3). */
+int nsp_remesh_create(int NR, int NT, int NZ, int Nrd, int Ntd, int Nzd, int iw, int device, nsp_remesh** out);
+/* The interpolation tables RM[2][Nrd][NR] (0: even folding, 1: odd) into out (host). */
+int nsp_remesh_matrix(const nsp_remesh* rm, double* out);
+/* Remeshes `count` fields in one launch on `stream` (NULL: the legacy stream) and
+ * waits for it: src[k] / dst[k] are device pointers (host arrays of them) to member
+ * k's old / new field.  Every value of each dst field is written. */
+int nsp_remesh_device(nsp_remesh* rm, int count, const void* const* src, void* const* dst, void* stream);
+/* Remeshes context members in one launch: the state of src member src_members[k]
+ * becomes the state of dst member dst_members[k] (src and dst may be the same context,
+ * e.g. two groups of an uneven ensemble).  Shapes must be the plan's. */
+int nsp_remesh_members(nsp_remesh* rm, nsp_ctx* src, const int* src_members, nsp_ctx* dst, const int* dst_members,
+                       int count);
+/* The tool itself: reads ur_o.bin, ut_o.bin, uz_o.bin from dir_in, writes ur_s.bin,
+ * ut_s.bin, uz_s.bin to dir_out (mod_remesh.cu:56-58, main.cu:28-30). */
+int nsp_remesh_files(nsp_remesh* rm, const char* dir_in, const char* dir_out);
+int nsp_remesh_destroy(nsp_remesh* rm);
+
 /* Waits for all work of the context. */
 int nsp_sync(nsp_ctx* ctx);
 
+/* The last failure of the context; with ctx NULL, the last failure of a context-free
+ * call (nsp_remesh_*, nsp_checkpoint_info) in the calling thread. */
 const char* nsp_last_error(nsp_ctx* ctx);
 int nsp_destroy(nsp_ctx* ctx);
 

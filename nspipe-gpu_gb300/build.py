@@ -23,7 +23,7 @@ CU_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I", os.path.join(CUDA, "include"),
              "-I", os.path.join(HERE, "..", "include")]
 
-CU_UNITS = ["nsp_api.cu", "nsp_linear.cu", "nsp_transform.cu", "nsp_noalloc.cu", "nsp_theta_tc.cu"]
+CU_UNITS = ["nsp_api.cu", "nsp_linear.cu", "nsp_transform.cu", "nsp_noalloc.cu", "nsp_theta_tc.cu", "nsp_remesh.cu"]
 CXX_UNITS = ["nsp_setup.cpp", "nsp_run.cpp"]
 HEADERS = ["nsp_internal.h", "nsp_fft.cuh", "nsp_cvt.cuh", "nsp_state.cuh", "nsp_tc.cuh", os.path.join("..", "..", "include", "nspipe_gb300.h")]
 

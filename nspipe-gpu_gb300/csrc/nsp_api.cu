@@ -374,8 +374,12 @@ int build_graph(nsp_ctx* c) {
 namespace nsp {
 int ctx_fail(nsp_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
+  else set_host_error(msg);
   return code;
 }
+
+thread_local std::string g_host_err;
+void set_host_error(const std::string& msg) { g_host_err = msg; }
 }  // namespace nsp
 
 extern "C" {
@@ -1038,7 +1042,44 @@ int nsp_info(nsp_ctx* c, int* n_members, int* precision) {
   return NSP_OK;
 }
 
-const char* nsp_last_error(nsp_ctx* c) { return c ? c->err.c_str() : "null context"; }
+const char* nsp_last_error(nsp_ctx* c) {
+  if (c) return c->err.c_str();
+  return g_host_err.empty() ? "null context" : g_host_err.c_str();
+}
+
+int nsp_remesh_members(nsp_remesh* rm, nsp_ctx* src, const int* src_members, nsp_ctx* dst, const int* dst_members,
+                       int count) {
+  if (!rm || !src || !dst || count < 0 || (count > 0 && (!src_members || !dst_members))) return NSP_ERR_ARG;
+  int old3[3], new3[3];
+  remesh_shape(rm, old3, new3);
+  if (src->device != remesh_device(rm) || dst->device != remesh_device(rm))
+    return fail(dst, NSP_ERR_ARG, "the remesh plan and both contexts must be on one device");
+  std::vector<const void*> sp(count);
+  std::vector<void*> dp(count);
+  for (int k = 0; k < count; k++) {
+    const int a = src_members[k], b = dst_members[k];
+    if (int rc = check_member(src, a)) return rc == NSP_ERR_ARG && src != dst ? fail(dst, rc, "%s", src->err.c_str()) : rc;
+    if (int rc = check_member(dst, b)) return rc;
+    const nsp_params &ps = src->prm[a], &pd = dst->prm[b];
+    if (ps.NR != old3[0] || ps.NT != old3[1] || ps.NZ != old3[2])
+      return fail(dst, NSP_ERR_ARG, "source member %d is %dx%dx%d, the plan's source shape %dx%dx%d", a, ps.NR, ps.NT,
+                  ps.NZ, old3[0], old3[1], old3[2]);
+    if (pd.NR != new3[0] || pd.NT != new3[1] || pd.NZ != new3[2])
+      return fail(dst, NSP_ERR_ARG, "destination member %d is %dx%dx%d, the plan's destination shape %dx%dx%d", b, pd.NR,
+                  pd.NT, pd.NZ, new3[0], new3[1], new3[2]);
+    sp[k] = state_ptr(src, a, 0);
+    dp[k] = state_ptr(dst, b, 0);
+  }
+  for (int k = 0; k < count; k++)
+    for (int q = 0; q < count; q++)
+      if (sp[k] == dp[q]) return fail(dst, NSP_ERR_ARG, "a member is both a source and a destination");
+  nsp_ctx* c = dst;  // CUDA failures are reported on the destination context
+  CK(cudaSetDevice(dst->device));
+  CK(cudaStreamSynchronize(src->st));
+  int rc = remesh_launch(rm, count, sp.data(), dp.data(), dst->st);
+  if (rc) return fail(dst, rc, "%s", g_host_err.c_str());
+  return NSP_OK;
+}
 
 int nsp_destroy(nsp_ctx* c) {
   if (!c) return NSP_OK;

@@ -134,6 +134,13 @@ void launch_theta_tc(const Tables& tb, const Bufs& bf, Ctl* dctl, int dir, const
 
 // Records msg as the context's last error (nsp_last_error) and returns code.
 int ctx_fail(nsp_ctx* c, int code, const std::string& msg);
+// Records the failure of a context-free call (nsp_last_error(NULL)), per thread.
+void set_host_error(const std::string& msg);
+// Re_Mesh plans (nsp_remesh.cu): launch over `count` members (host arrays of device
+// pointers to each member's three components), shapes and device of a plan.
+int remesh_launch(nsp_remesh* p, int count, const void* const* src, void* const* dst, cudaStream_t st);
+void remesh_shape(const nsp_remesh* p, int* old3, int* new3);
+int remesh_device(const nsp_remesh* p);
 
 // Host-side operator construction (nsp_setup.cpp).
 struct HostOps {

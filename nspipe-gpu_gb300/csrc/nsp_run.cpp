@@ -812,7 +812,7 @@ int nsp_checkpoint_info(const char* ckpt, char* json, int json_cap, char* path, 
   if (!ckpt) return NSP_ERR_ARG;
   std::string dir, text, why;
   Json side;
-  if (int rc = load_checkpoint(ckpt, &dir, &side, &text, &why)) return rc;
+  if (int rc = load_checkpoint(ckpt, &dir, &side, &text, &why)) return nsp::ctx_fail(nullptr, rc, why);
   if (json) {
     if ((int)text.size() + 1 > json_cap) return NSP_ERR_ARG;
     memcpy(json, text.c_str(), text.size() + 1);

@@ -28,6 +28,8 @@ EXPORTS = [
     "nsp_measure_fp64_peak", "nsp_nonlinear_static", "nsp_describe", "nsp_mean_profile", "nsp_cross_sections",
     "nsp_get_params", "nsp_info", "nsp_run_default_opts", "nsp_run_open", "nsp_run_resume", "nsp_run_advance",
     "nsp_run_checkpoint", "nsp_run_time", "nsp_run_close", "nsp_checkpoint_info", "nsp_output_schedule",
+    "nsp_remesh_create", "nsp_remesh_matrix", "nsp_remesh_device", "nsp_remesh_members", "nsp_remesh_files",
+    "nsp_remesh_destroy",
 ]
 
 
@@ -110,6 +112,12 @@ def lib():
         L.nsp_run_close.argtypes = [vp]
         L.nsp_checkpoint_info.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ip, ctypes.c_char_p, ip]
         L.nsp_output_schedule.argtypes = [ctypes.c_double, ctypes.c_double, ip, dp, ctypes.POINTER(ctypes.c_ubyte)]
+        L.nsp_remesh_create.argtypes = [ip, ip, ip, ip, ip, ip, ip, ip, ctypes.POINTER(vp)]
+        L.nsp_remesh_matrix.argtypes = [vp, dp]
+        L.nsp_remesh_device.argtypes = [vp, ip, ctypes.POINTER(vp), ctypes.POINTER(vp), vp]
+        L.nsp_remesh_members.argtypes = [vp, vp, ctypes.POINTER(ip), vp, ctypes.POINTER(ip), ip]
+        L.nsp_remesh_files.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p]
+        L.nsp_remesh_destroy.argtypes = [vp]
         L.nsp_last_error.argtypes = [vp]
         L.nsp_last_error.restype = ctypes.c_char_p
         L.nsp_destroy.argtypes = [vp]
@@ -316,6 +324,11 @@ def output_schedule(dt, interval, nsteps, acc=0.0):
     return due.astype(bool), a.value
 
 
+def host_error():
+    """Message of the last failed context-free call in this thread (nsp_last_error(NULL))."""
+    return lib().nsp_last_error(None).decode()
+
+
 def checkpoint_info(path):
     """(sidecar dict, resolved checkpoint directory) of a checkpoint, after checking its
     state files against the sidecar; NspError(NSP_ERR_IO) if missing or corrupt."""
@@ -323,7 +336,7 @@ def checkpoint_info(path):
     where = ctypes.create_string_buffer(4096)
     rc = lib().nsp_checkpoint_info(os.fsencode(path), js, len(js), where, len(where))
     if rc != NSP_OK:
-        raise NspError(rc, "checkpoint %s unusable" % path)
+        raise NspError(rc, host_error())
     return json.loads(js.value.decode()), where.value.decode()
 
 
@@ -376,3 +389,60 @@ class Run:
 
     def __exit__(self, *exc):
         self.close()
+
+
+class Remesh:
+    """A Re_Mesh plan (nsp_remesh_*): fields of shape old = (NR, NT, NZ) to new =
+    (Nrd, Ntd, Nzd), radial Lagrange interpolation on 2*iw points, theta / z modes
+    truncated or zero-padded, batched over members in one launch."""
+
+    def __init__(self, old, new, iw=3, device=0):
+        self.old, self.new, self.iw = tuple(old), tuple(new), iw
+        self._h = ctypes.c_void_p()
+        rc = lib().nsp_remesh_create(*self.old, *self.new, iw, device, ctypes.byref(self._h))
+        if rc != NSP_OK:
+            raise NspError(rc, host_error())
+
+    def _check(self, rc):
+        if rc != NSP_OK:
+            raise NspError(rc, host_error())
+
+    def matrix(self):
+        """RM[2][Nrd][NR]: 0 even folding, 1 odd folding."""
+        out = np.zeros((2, self.new[0], self.old[0]))
+        self._check(lib().nsp_remesh_matrix(self._h, _dp(out)))
+        return out
+
+    def device(self, src, dst, stream=None):
+        """src / dst: sequences of device buffers (torch tensors or int pointers), each a
+        member's three components back to back; one launch for all of them."""
+        n = len(src)
+        if len(dst) != n:
+            raise ValueError("src and dst lengths differ")
+        sp = (ctypes.c_void_p * max(n, 1))(*[_ptr(x) for x in src])
+        dp_ = (ctypes.c_void_p * max(n, 1))(*[_ptr(x) for x in dst])
+        self._check(lib().nsp_remesh_device(self._h, n, sp, dp_, stream))
+
+    def members(self, src, src_members, dst, dst_members):
+        """State of src member src_members[k] -> state of dst member dst_members[k]."""
+        n = len(src_members)
+        a = (ctypes.c_int * max(n, 1))(*src_members)
+        b = (ctypes.c_int * max(n, 1))(*dst_members)
+        rc = lib().nsp_remesh_members(self._h, src._h, a, dst._h, b, n)
+        if rc != NSP_OK:
+            raise NspError(rc, dst.last_error())
+
+    def files(self, dir_in, dir_out):
+        """The tool: u?_o.bin in dir_in -> u?_s.bin in dir_out."""
+        self._check(lib().nsp_remesh_files(self._h, os.fsencode(dir_in), os.fsencode(dir_out)))
+
+    def close(self):
+        if self._h:
+            lib().nsp_remesh_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -33,6 +33,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 REF_OUT = os.path.join(ORACLE, "_ref")
 REF_SRC_DEFAULT = "/root/reference/Main_Code/src"
+REMESH_SRC_DEFAULT = "/root/reference/tools/Re_Mesh/src"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 # name -> (NR, NT, NZ, LZ expression, Re, dt in code units)
@@ -136,6 +137,65 @@ def run(cfg, mode, fields_dir, nsteps, snaps=None, nsteps_build=None):
     if p.returncode != 0:
         raise RuntimeError("reference run failed (%d): %s" % (p.returncode, (p.stdout + p.stderr)[-2000:]))
     return rundir
+
+
+# ---- the Re_Mesh tool (tools/Re_Mesh/src): mod_remesh.cu + mod_io.cu + remesh_driver.cu
+
+def stage_remesh(src=REMESH_SRC_DEFAULT):
+    """Copy the Re_Mesh sources to oracle/_ref/remesh_src (once, where the reference exists)."""
+    dst = os.path.join(REF_OUT, "remesh_src")
+    if not os.path.isdir(src):
+        if os.path.isdir(dst):
+            return dst
+        raise FileNotFoundError("Re_Mesh sources not found: %s" % src)
+    os.makedirs(dst, exist_ok=True)
+    for f in os.listdir(src):
+        shutil.copy2(os.path.join(src, f), os.path.join(dst, f))
+        os.chmod(os.path.join(dst, f), 0o644)
+    return dst
+
+
+def build_remesh(old, new, iw=3):
+    """Compile oracle/_ref/remesh/<tag>/Remesh for old=(NR, NT, NZ) -> new=(Nrd, Ntd, Nzd)."""
+    src = stage_remesh()
+    tag = "%dx%dx%d_%dx%dx%d_iw%d" % (tuple(old) + tuple(new) + (iw,))
+    out = os.path.join(REF_OUT, "remesh", tag)
+    exe = os.path.join(out, "Remesh")
+    if os.path.exists(exe):
+        return exe
+    os.makedirs(out, exist_ok=True)
+    for f in ("head.h", "mod_remesh.cu", "mod_io.cu"):
+        shutil.copy2(os.path.join(src, f), os.path.join(out, f))
+    with open(os.path.join(out, "head.h")) as fh:
+        text = fh.read()
+    for name, value in zip(("NR", "NT", "NZ", "Nrd", "Ntd", "Nzd", "iw"), tuple(old) + tuple(new) + (iw,)):
+        pat = re.compile(r"^#define\s+%s\b.*$" % name, re.M)
+        assert pat.search(text), name
+        text = pat.sub("#define %s %d" % (name, value), text, count=1)
+    with open(os.path.join(out, "head.h"), "w") as fh:
+        fh.write(text)
+    shutil.copy2(os.path.join(HERE, "remesh_driver.cu"), os.path.join(out, "remesh_driver.cu"))
+    objs = []
+    for u in ("mod_remesh.cu", "mod_io.cu", "remesh_driver.cu"):
+        obj = os.path.join(out, u[:-3] + ".o")
+        subprocess.run(["nvcc", "-O3", ARCH, "-I", out, "-c", os.path.join(out, u), "-o", obj], check=True)
+        objs.append(obj)
+    subprocess.run(["nvcc", ARCH, "-o", exe] + objs, check=True)
+    return exe
+
+
+def run_remesh(old, new, iw, fields):
+    """Run the tool on fields (3 complex arrays of shape old); returns the 3 new arrays."""
+    import numpy as np
+    exe = build_remesh(old, new, iw)
+    rundir = os.path.join(os.path.dirname(exe), "run")
+    os.makedirs(rundir, exist_ok=True)
+    for c, a in zip("rtz", fields):
+        np.ascontiguousarray(a, np.complex128).tofile(os.path.join(rundir, "u%s_o.bin" % c))
+    p = subprocess.run([exe], cwd=rundir, capture_output=True, text=True)
+    if p.returncode != 0:
+        raise RuntimeError("Re_Mesh failed (%d): %s" % (p.returncode, (p.stdout + p.stderr)[-2000:]))
+    return [np.fromfile(os.path.join(rundir, "u%s_s.bin" % c), np.complex128).reshape(new) for c in "rtz"]
 
 
 if __name__ == "__main__":

@@ -20,6 +20,12 @@ schedule build_ref.IO_SCHEDULE: rows every 0.015 / 0.05 / 0.035 time units, 4
 rows per write) and keeps the four files integrate() writes, io_friction.txt,
 io_qcross.txt, io_ucross.txt and io_meanpr.txt, as written (tests/golden/io_s2/).
 
+'remesh' runs the reference Re_Mesh tool (tools/Re_Mesh/src, built by
+build_ref.build_remesh with a driver main of its own) on seeded fields for the
+cases in REMESH_CASES and keeps input seeds and outputs (tests/golden/remesh.npz).
+The inputs are uniform in [-1, 1) from SplitMix64 (remesh_input), so they are
+regenerated bit for bit from the seed.
+
 The projections use real weights w ~ N(0,1) from SplitMix64(seed ^ 0x5bd1e995):
 p = sum_h w_h u_h over the flattened field.
 """
@@ -65,6 +71,34 @@ def reduce_field(u, seed):
     return out
 
 
+# name -> old (NR, NT, NZ), new (Nrd, Ntd, Nzd), iw, seed: refinement in every
+# direction, coarsening in every direction (theta and z truncation), a radial-only
+# refinement with a 4-point stencil.
+REMESH_CASES = {
+    "up": ((24, 8, 9), (32, 12, 13), 3, 101),
+    "down": ((32, 16, 17), (24, 8, 9), 3, 102),
+    "radial_iw2": ((24, 8, 9), (40, 8, 9), 2, 103),
+}
+
+
+def remesh_input(shape, seed):
+    """Three complex fields of the given shape, real and imaginary parts uniform in [-1, 1)."""
+    rng = SplitMix64(seed)
+    n = int(np.prod(shape))
+    vals = np.array([2.0 * rng.uniform() - 1.0 for _ in range(6 * n)])
+    return [(vals[2 * n * c:2 * n * (c + 1):2] + 1j * vals[2 * n * c + 1:2 * n * (c + 1):2]).reshape(shape)
+            for c in range(3)]
+
+
+def make_remesh(outdir):
+    fx = {}
+    for name, (old, new, iw, seed) in REMESH_CASES.items():
+        out = build_ref.run_remesh(old, new, iw, remesh_input(old, seed))
+        fx[name] = np.stack(out)
+        print("remesh", name, old, "->", new, "iw", iw, flush=True)
+    np.savez_compressed(os.path.join(outdir, "remesh.npz"), **fx)
+
+
 IO_FILES = ("io_friction.txt", "io_qcross.txt", "io_ucross.txt", "io_meanpr.txt")
 
 
@@ -88,6 +122,11 @@ def main():
     cfgs = sys.argv[2:] or ["s2", "c0", "c1"]
     os.makedirs(outdir, exist_ok=True)
     summary = {}
+    if "remesh" in cfgs:
+        make_remesh(outdir)
+        cfgs = [c for c in cfgs if c != "remesh"]
+        if not cfgs:
+            return
     if "io_s2" in cfgs:
         make_io(outdir)
         cfgs = [c for c in cfgs if c != "io_s2"]
