@@ -204,7 +204,9 @@ def run_uneven(args):
             k += 1
 
     def timed(precision):
-        st = nsp.Stepper(prm, precision=precision)
+        t_setup = time.perf_counter()
+        st = nsp.Stepper(prm, precision=precision)  # operator tables of 28 parameter sets, autotune, graph
+        t_setup = time.perf_counter() - t_setup
         for m, f in enumerate(fields):
             st.set_state(m, f)
         desc = st.describe()
@@ -224,6 +226,7 @@ def run_uneven(args):
         finite = all(d.status == 0 for d in (st.diag(m) for m in range(len(prm))))
         st.set_stream(0)
         st.close()
+        desc["setup_seconds"] = round(t_setup, 3)
         return sec, iters, clk.summary(), desc, launches, finite
 
     sec, iters, clocks, desc, launches, finite = timed(nsp.NSP_MIXED)
@@ -318,8 +321,11 @@ def main():
         st.set_stream(0)
         return ms / 1e3, iters, clk.summary()
 
+    t_setup = time.perf_counter()
     st = make(prec)
+    t_setup = time.perf_counter() - t_setup
     describe = st.describe()  # graph, autotuned linear-pass block, theta-transform path
+    describe["setup_seconds"] = round(t_setup, 3)
     sec, iters, clocks = device_timed(st, args.steps, args.warmup)
     launches = st.kernel_launches()
     sec_max = max_over_ranks(sec)

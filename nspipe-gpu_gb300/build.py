@@ -23,9 +23,13 @@ CU_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-I", os.path.join(CUDA, "include"),
              "-I", os.path.join(HERE, "..", "include")]
 
-CU_UNITS = ["nsp_api.cu", "nsp_linear.cu", "nsp_transform.cu", "nsp_noalloc.cu", "nsp_theta_tc.cu", "nsp_remesh.cu"]
+CU_UNITS = ["nsp_api.cu", "nsp_linear.cu", "nsp_transform.cu", "nsp_noalloc.cu", "nsp_theta_tc.cu", "nsp_remesh.cu",
+            "nsp_setup_dev.cu"]
+# Per-unit extra flags.  nsp_setup_dev.cu builds the operator tables that nsp_setup.cpp
+# builds on the host (-ffp-contract=off): without FMA contraction both give the same bits.
+CU_EXTRA = {"nsp_setup_dev.cu": ["-fmad=false"]}
 CXX_UNITS = ["nsp_setup.cpp", "nsp_run.cpp"]
-HEADERS = ["nsp_internal.h", "nsp_fft.cuh", "nsp_cvt.cuh", "nsp_state.cuh", "nsp_tc.cuh", os.path.join("..", "..", "include", "nspipe_gb300.h")]
+HEADERS = ["nsp_internal.h", "nsp_setup_mode.h", "nsp_fft.cuh", "nsp_cvt.cuh", "nsp_state.cuh", "nsp_tc.cuh", os.path.join("..", "..", "include", "nspipe_gb300.h")]
 
 
 def _stale(obj, src):
@@ -42,7 +46,7 @@ def build(force=False, verbose=False):
     for u in CU_UNITS:
         src, obj = os.path.join(CSRC, u), os.path.join(BUILD, u + ".o")
         if force or _stale(obj, src):
-            jobs.append([NVCC] + CU_FLAGS + ["-c", src, "-o", obj])
+            jobs.append([NVCC] + CU_FLAGS + CU_EXTRA.get(u, []) + ["-c", src, "-o", obj])
     for u in CXX_UNITS:
         src, obj = os.path.join(CSRC, u), os.path.join(BUILD, u + ".o")
         if force or _stale(obj, src):

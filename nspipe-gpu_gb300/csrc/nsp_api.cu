@@ -38,7 +38,8 @@ struct Group {
   std::vector<int> users;   // user member indices, in slot order
   std::vector<double> sets; // distinct Re of the group (operator parameter sets)
   std::vector<int> mset;    // [slot] parameter set of each member
-  HostOps ops;              // shape data and set 0's operators (host copy)
+  HostOps ops;              // radial tables and set 0's flux response (host copy)
+  bool device_setup = true; // mode tables built on the device (else on the host)
   Tables tb{};
   Bufs bf{};
 };
@@ -524,22 +525,26 @@ int nsp_setup(nsp_ctx* c) {
     Tables& tb = g.tb;
     const nsp_params& p = g.p;
     HostOps& o = g.ops;
-    // Operators of every parameter set (distinct Re), concatenated set-major.
+    // Radial tables of the group's shape, then every parameter set's (distinct Re)
+    // scalars, flux response and explicit Laplacian, concatenated set-major.
+    radial_fd(p.NR, o);
     const int nsets = (int)g.sets.size();
-    std::vector<double> fac_all, Luc_all, uc_all, sscal;
-    std::vector<double2> V_all;
+    std::vector<double> Luc_all, uc_all, sscal, c_im(nsets);
     for (int k = 0; k < nsets; k++) {
       nsp_params pk = p;
       pk.Re = g.sets[k];
-      HostOps ok;
-      build_operators(pk, ok);
+      std::vector<double> uck;
+      double Qck = 0.0;
+      flux_response(pk, o, uck, Qck);
       const double c_ex = (1.0 - pk.d_im) / pk.Re;
-      fac_all.insert(fac_all.end(), ok.fac.begin(), ok.fac.end());
-      V_all.insert(V_all.end(), ok.V.begin(), ok.V.end());
-      uc_all.insert(uc_all.end(), ok.uc.begin(), ok.uc.end());
-      for (size_t e = 0; e < ok.Lu.size(); e++) Luc_all.push_back(0.5 * (c_ex * ok.Lu[e]));
-      sscal.insert(sscal.end(), {c_ex, 2.0 / pk.Re, ok.Qc, pk.Re});
-      if (k == 0) o = std::move(ok);
+      uc_all.insert(uc_all.end(), uck.begin(), uck.end());
+      for (size_t e = 0; e < o.Lu.size(); e++) Luc_all.push_back(0.5 * (c_ex * o.Lu[e]));
+      sscal.insert(sscal.end(), {c_ex, 2.0 / pk.Re, Qck, pk.Re});
+      c_im[k] = pk.d_im / pk.Re;
+      if (k == 0) {
+        o.uc = uck;
+        o.Qc = Qck;
+      }
     }
     std::vector<double> rinv(p.NR), rinv2(p.NR);
     std::vector<float> D32(o.D.size());
@@ -549,9 +554,37 @@ int nsp_setup(nsp_ctx* c) {
     if ((rc = upload(c, &tb.r, o.r)) || (rc = upload(c, &tb.rinv, rinv)) || (rc = upload(c, &tb.rinv2, rinv2)) ||
         (rc = upload(c, &tb.rdr, o.rdr)) || (rc = upload(c, &tb.uc, uc_all)) || (rc = upload(c, &tb.D, o.D)) ||
         (rc = upload(c, &tb.D32, D32)) || (rc = upload(c, &tb.Lu, o.Lu)) || (rc = upload(c, &tb.Luc, Luc_all)) ||
-        (rc = upload(c, &tb.fac, fac_all)) || (rc = upload(c, &tb.V, V_all)) || (rc = upload(c, &tb.sscal, sscal)) ||
-        (rc = upload(c, &tb.mset, g.mset)))
+        (rc = upload(c, &tb.sscal, sscal)) || (rc = upload(c, &tb.mset, g.mset)))
       return rc;
+    // Factors and correction profiles of every (set, mode): on the device by default,
+    // one thread per (set, mode); NSP_DEVICE_SETUP=0 builds the same bits on the host.
+    const size_t NTNZ = (size_t)p.NT * p.NZ;
+    const size_t fac_n = (size_t)nsets * 4 * p.NR * NFAC * NTNZ, V_n = (size_t)nsets * 3 * p.NR * NTNZ;
+    const char* se = getenv("NSP_DEVICE_SETUP");
+    g.device_setup = !(se && se[0] == '0');
+    if (g.device_setup) {
+      double* fac = nullptr;
+      double2* V = nullptr;
+      const double* Lp = nullptr;
+      if ((rc = dalloc(c, &fac, sizeof(double) * fac_n)) || (rc = dalloc(c, &V, sizeof(double2) * V_n)) ||
+          (rc = upload(c, &Lp, o.Lp)))
+        return rc;
+      std::string err;
+      if ((rc = launch_mode_tables(p, nsets, c_im.data(), tb.r, tb.D, tb.Lu, Lp, fac, V, c->st, &err)))
+        return fail(c, rc, "%s", err.c_str());
+      tb.fac = fac;
+      tb.V = V;
+    } else {
+      std::vector<double> fac_all(fac_n);
+      std::vector<double2> V_all(V_n);
+      for (int k = 0; k < nsets; k++) {
+        nsp_params pk = p;
+        pk.Re = g.sets[k];
+        mode_tables(pk, o, fac_all.data() + (size_t)k * 4 * p.NR * NFAC * NTNZ,
+                    V_all.data() + (size_t)k * 3 * p.NR * NTNZ);
+      }
+      if ((rc = upload(c, &tb.fac, fac_all)) || (rc = upload(c, &tb.V, V_all))) return rc;
+    }
     tb.nsets = nsets;
     std::vector<double2> wt = twiddles(tb.NTP), wz = twiddles(tb.NZR);
     if ((rc = upload(c, &tb.tw_t, wt)) || (rc = upload(c, &tb.tw_z, wz)) || (rc = upload(c, &tb.tw_t32, to_f32(wt))) ||
@@ -582,9 +615,6 @@ int nsp_setup(nsp_ctx* c) {
         return rc;
       tb.tc_theta = 1;
     }
-    // Release the large host tables; keep grid data for diagnostics.
-    std::vector<double>().swap(o.fac);
-    std::vector<double2>().swap(o.V);
   }
   configure_transform_kernels();
   configure_linear_kernels();
@@ -933,11 +963,13 @@ int nsp_describe(nsp_ctx* c, char* buf, int cap) {
     int v = linear_variant_fits(tb.lin_variant, tb.NR) ? tb.lin_variant : linear_default_variant(tb.NR);
     int LM = 0, NTH = 0;
     linear_shape(v, &LM, &NTH);
-    char g[256];
+    char g[384];
     snprintf(g, sizeof(g),
-             "%s{\"shape\": [%d, %d, %d], \"members\": %d, \"linear_block\": [%d, %d], \"theta\": \"%s\"}",
-             k ? ", " : "", tb.NR, tb.NT, tb.NZ, tb.nmem, LM, NTH,
-             c->precision != NSP_MIXED ? "fft-fp64" : (tb.tc_theta ? "tcgen05-3xtf32" : "fft-fp32"));
+             "%s{\"shape\": [%d, %d, %d], \"members\": %d, \"parameter_sets\": %d, \"linear_block\": [%d, %d], "
+             "\"theta\": \"%s\", \"setup\": \"%s\"}",
+             k ? ", " : "", tb.NR, tb.NT, tb.NZ, tb.nmem, tb.nsets, LM, NTH,
+             c->precision != NSP_MIXED ? "fft-fp64" : (tb.tc_theta ? "tcgen05-3xtf32" : "fft-fp32"),
+             c->groups[k].device_setup ? "device" : "host");
     s += g;
   }
   s += "]}";

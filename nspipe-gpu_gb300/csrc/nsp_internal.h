@@ -153,5 +153,14 @@ struct HostOps {
 };
 void build_operators(const nsp_params& p, HostOps& out);
 void radial_fd(int NR, HostOps& out);
+// One parameter set's mode tables on the host: fac [4][NR][NFAC][NT*NZ], V [3][NR][NT*NZ].
+void mode_tables(const nsp_params& p, const HostOps& o, double* fac, double2* V);
+// Flux response of one parameter set (mode (0,0) u_z solve with unit forcing) and its flux.
+void flux_response(const nsp_params& p, const HostOps& o, std::vector<double>& uc, double& Qc);
+// The same mode tables on the device (nsp_setup_dev.cu), bit-identical to mode_tables:
+// nsets parameter sets of one shape (set k: c_im[k] = d_im / Re_k), written set-major
+// into fac and V (device memory).  r, D, Lu, Lp: device copies of o's radial tables.
+int launch_mode_tables(const nsp_params& p, int nsets, const double* c_im_host, const double* r, const double* D,
+                       const double* Lu, const double* Lp, double* fac, double2* V, cudaStream_t st, std::string* err);
 
 }  // namespace nsp

@@ -21,15 +21,11 @@
 #include <cstring>
 
 #include "nsp_internal.h"
+#include "nsp_setup_mode.h"
 
 namespace nsp {
 
 namespace {
-
-struct cd {
-  double x, y;
-};
-inline cd cmul(cd a, cd b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
 
 // Fornberg's recursion for the weights of derivatives 0..m at z on the points
 // x[0..n-1]; w[k*n + j] is the weight of point j for derivative k.
@@ -146,217 +142,64 @@ void radial_fd(int NR, HostOps& o) {
 
 namespace {
 
-struct ModeOps {
-  int NR;
-  const HostOps* o;
-  double c_im, inv_dt;
-};
-
-// Doolittle factors of one banded operator row by row, in the operation order of
-// LUsolve_*_k.  kind 0: u+, 1: u-, 2: u_z, 3: p.  Writes f[i*NFAC + e].
-void factor_mode(const ModeOps& M, int kind, int m, double kt, double kz, bool mode00, double* f) {
-  const int NR = M.NR;
-  const int hD = STEN * NR;
-  int odd = kind <= 1 ? 1 : 0;
-  int tab = std::abs((std::abs(m) % 2) - odd);
-  const double* LHS = (kind == 3 ? M.o->Lp.data() : M.o->Lu.data()) + tab * hD;
-  const double* r = M.o->r.data();
-  std::vector<double> U((size_t)NR * (IW + 1), 0.0);
-  double L[IW + 1];
-  bool zz = (kind == 3) && mode00;
-  for (int i = 0; i < NR; i++) {
-    int left = i - IW > 0 ? i - IW : 0, right = i + IW < NR - 1 ? i + IW : NR - 1;
-    int i0 = i + IW - right, coun = 0;
-    bool wall = (i == NR - 1);
-    double r2 = r[i] * r[i];
-    for (int j = 0; j < i - left; j++) {
-      double XM = LHS[j + i0 + STEN * i];
-      if (!wall && kind != 3) XM = -(M.c_im) * XM;
-      if (wall && zz) XM = 0.0;
-      L[j] = XM;
-      coun += 1;
-      for (int h = 0; h < j; h++) L[j] -= L[h] * U[(size_t)(IW + 1) * (h + left) + j - h];
-      L[j] = L[j] / U[(size_t)(j + left) * (IW + 1)];
-    }
-    int coun2 = coun;
-    for (int j = 0; j < right - i + 1; j++) {
-      double XM = LHS[STEN * i + i0 + coun];
-      if (!wall) {
-        if (j == 0) {
-          if (kind == 0) XM += -(1.0 / r2) - (2.0 * kt / r2) - kz * kz - kt * kt / r2;
-          else if (kind == 1) XM += -(1.0 / r2) + (2.0 * kt / r2) - kz * kz - kt * kt / r2;
-          else XM += -kz * kz - kt * kt / r2;
-          if (kind != 3) XM = M.inv_dt - M.c_im * XM;
-        } else if (kind != 3) {
-          XM = -(M.c_im) * XM;
-        }
-      } else if (zz) {
-        XM = (j == 0) ? 1.0 : 0.0;
-      }
-      double& Uij = U[j + (size_t)(IW + 1) * i];
-      Uij = XM;
-      int hleft = coun - IW > 0 ? coun - IW : 0;
-      coun += 1;
-      for (int h = hleft; h < i - left; h++) Uij -= L[h] * U[(size_t)(IW + 1) * (h + left) + j + coun2 - h];
-    }
-    double* fr = f + (size_t)i * NFAC;
-    for (int d = 1; d <= IW; d++) {  // column i-d sits at L[i-d-left]
-      int j = i - d - left;
-      fr[IW - d] = (j >= 0) ? L[j] : 0.0;
-    }
-    fr[IW] = 1.0 / U[(size_t)i * (IW + 1)];
-    for (int d = 1; d <= IW; d++) fr[IW + d] = (i + d <= right) ? U[d + (size_t)(IW + 1) * i] : 0.0;
-  }
-}
-
-// Forward and backward substitution with stored factors (the device algorithm).
-void solve_mode(int NR, const double* f, cd* x) {
-  for (int i = 0; i < NR; i++) {
-    const double* fr = f + (size_t)i * NFAC;
-    for (int d = (i < IW ? i : IW); d >= 1; d--) {
-      x[i].x -= fr[IW - d] * x[i - d].x;
-      x[i].y -= fr[IW - d] * x[i - d].y;
-    }
-  }
-  for (int i = NR - 1; i >= 0; i--) {
-    const double* fr = f + (size_t)i * NFAC;
-    for (int d = 1; d <= IW && i + d < NR; d++) {
-      x[i].x -= fr[IW + d] * x[i + d].x;
-      x[i].y -= fr[IW + d] * x[i + d].y;
-    }
-    x[i].x = x[i].x * fr[IW];
-    x[i].y = x[i].y * fr[IW];
-  }
-}
-
-// Wall divergence of a (u_r, u_theta, u_z) mode line (divWall_k, mod_radialFD.cu:34-63).
-cd div_wall(const HostOps& o, int NR, int m, double kt, double kz, const cd* ur, const cd* ut, const cd* uz) {
-  int tab = std::abs((std::abs(m) % 2) - 1);
-  const double* D = o.D.data() + tab * STEN * NR + STEN * (NR - 1);
-  cd p = {0.0, 0.0};
-  for (int j = 0; j <= IW; j++) {
-    p.x += D[j + IW] * ur[NR - 1 - IW + j].x;
-    p.y += D[j + IW] * ur[NR - 1 - IW + j].y;
-  }
-  int w = NR - 1;
-  p.x += ur[w].x;
-  p.y += ur[w].y;
-  p.x += -kt * ut[w].y;
-  p.y += kt * ut[w].x;
-  p.x += -kz * uz[w].y;
-  p.y += kz * uz[w].x;
-  return p;
-}
+setup::Radial radial_view(const HostOps& o) { return setup::Radial{o.NR, o.r.data(), o.D.data(), o.Lu.data(), o.Lp.data()}; }
 
 }  // namespace
 
-void build_operators(const nsp_params& p, HostOps& o) {
-  const int NR = p.NR, NT = p.NT, NZ = p.NZ, NTNZ = NT * NZ;
-  radial_fd(NR, o);
-  ModeOps M{NR, &o, p.d_im / p.Re, 1.0 / p.dt};
+// Factors and correction profiles of every mode of one parameter set, on the host:
+// fac [4][NR][NFAC][NTNZ], V [3][NR][NTNZ].  Each mode is built in contiguous
+// temporaries by the shared per-mode code, then scattered into the tables.
+void mode_tables(const nsp_params& p, const HostOps& o, double* fac, double2* V) {
+  using setup::cd;
+  using setup::Strided;
+  const int NR = p.NR, NT = p.NT, NZ = p.NZ;
+  const long long NTNZ = (long long)NT * NZ;
+  const setup::Radial R = radial_view(o);
+  const double c_im = p.d_im / p.Re, inv_dt = 1.0 / p.dt;
   const double kts = PI2 / p.LT, kzs = PI2 / p.LZ;
-  o.fac.assign((size_t)4 * NR * NFAC * NTNZ, 0.0);
-  o.V.assign((size_t)3 * NR * NTNZ, double2{0.0, 0.0});
+  std::vector<double> fk((size_t)4 * NR * NFAC);
+  std::vector<cd> vk((size_t)3 * NR), ph(NR);
+  for (long long k = 0; k < NTNZ; k++) {
+    const int it = (int)(k / NZ), l = (int)(k % NZ);
+    const int m = it < NT / 2 ? it : it - NT;
+    const double kt = kts * (double)m, kz = kzs * (double)l;
+    Strided<double> f[4];
+    Strided<cd> v[3];
+    for (int op = 0; op < 4; op++) f[op] = Strided<double>{fk.data() + (size_t)op * NR * NFAC, 1};
+    for (int c = 0; c < 3; c++) v[c] = Strided<cd>{vk.data() + (size_t)c * NR, 1};
+    setup::setup_mode(R, c_im, inv_dt, m, kt, kz, m == 0 && l == 0, f[0], f[1], f[2], f[3], v[0], v[1], v[2],
+                      Strided<cd>{ph.data(), 1});
+    for (size_t e = 0; e < fk.size(); e++) fac[e * NTNZ + k] = fk[e];
+    for (size_t e = 0; e < vk.size(); e++) V[e * NTNZ + k] = double2{vk[e].x, vk[e].y};
+  }
+}
+
+// Flux response: u_z-Helmholtz with unit right-hand side, zero wall value, mode (0,0)
+// (setCublasFlux, mod_cublasflux.cu:56-81).
+void flux_response(const nsp_params& p, const HostOps& o, std::vector<double>& uc, double& Qc) {
+  using setup::cd;
+  using setup::Strided;
+  const int NR = p.NR;
   std::vector<double> f((size_t)NR * NFAC);
-  std::vector<double> fk[4];
-  for (auto& v : fk) v.resize((size_t)NR * NFAC);
-  std::vector<cd> uh[3], ph(NR), uP[3], zero(NR, cd{0.0, 0.0}), tr(NR), tt(NR);
-  for (int c = 0; c < 3; c++) { uh[c].resize(NR); uP[c].resize(NR); }
-  const int hD = STEN * NR;
-  for (int k = 0; k < NTNZ; k++) {
-    int it = k / NZ, l = k % NZ;
-    int m = it < NT / 2 ? it : it - NT;
-    double kt = kts * (double)m, kz = kzs * (double)l;
-    bool m00 = (m == 0 && l == 0);
-    for (int op = 0; op < 4; op++) {
-      factor_mode(M, op, m, kt, kz, m00, fk[op].data());
-      for (int i = 0; i < NR; i++)
-        for (int e = 0; e < NFAC; e++)
-          o.fac[(((size_t)op * NR + i) * NFAC + e) * NTNZ + k] = fk[op][(size_t)i * NFAC + e];
-    }
-    // Homogeneous solutions: unit wall values (1, 1, i) and pressure with p_wall = -1.
-    for (int c = 0; c < 3; c++) {
-      for (int i = 0; i < NR; i++) uh[c][i] = cd{0.0, 0.0};
-      uh[c][NR - 1] = (c == 2) ? cd{0.0, 1.0} : cd{1.0, 0.0};
-      solve_mode(NR, fk[c].data(), uh[c].data());
-    }
-    for (int i = 0; i < NR; i++) ph[i] = cd{0.0, 0.0};
-    ph[NR - 1] = cd{-1.0, 0.0};
-    solve_mode(NR, fk[3].data(), ph.data());
-    // Wall divergences of the velocity solutions in r/theta form.
-    cd a41, a42, a43, a44;
-    for (int i = 0; i < NR; i++) {  // (u+, 0) -> r/theta
-      cd u = uh[0][i];
-      tr[i] = cd{0.5 * (u.x + 0.0), 0.5 * (u.y + 0.0)};
-      tt[i] = cd{0.5 * (u.y - 0.0), -0.5 * (u.x - 0.0)};
-    }
-    a41 = div_wall(o, NR, m, kt, kz, tr.data(), tt.data(), zero.data());
-    for (int i = 0; i < NR; i++) {  // (0, u-) -> r/theta
-      cd u = uh[1][i];
-      tr[i] = cd{0.5 * (0.0 + u.x), 0.5 * (0.0 + u.y)};
-      tt[i] = cd{0.5 * (0.0 - u.y), -0.5 * (0.0 - u.x)};
-    }
-    a42 = div_wall(o, NR, m, kt, kz, tr.data(), tt.data(), zero.data());
-    a43 = div_wall(o, NR, m, kt, kz, zero.data(), zero.data(), uh[2].data());
-    // Pressure-driven velocity grad p_h (derivr flag 0, derivt, derivz), then +/- form.
-    {
-      int tab = std::abs(m) % 2;
-      const double* D = o.D.data() + tab * hD;
-      for (int i = 0; i < NR; i++) {
-        int left = i - IW > 0 ? i - IW : 0, right = i + IW < NR - 1 ? i + IW : NR - 1;
-        int len = right + 1 - left, i0 = i + IW - right;
-        cd s = {0.0, 0.0};
-        for (int j = 0; j < len; j++) {
-          s.x += D[STEN * i + j + i0] * ph[left + j].x;
-          s.y += D[STEN * i + j + i0] * ph[left + j].y;
-        }
-        uP[0][i] = s;
-        uP[1][i] = cd{-kt * ph[i].y / o.r[i], kt * ph[i].x / o.r[i]};
-        uP[2][i] = cd{-kz * ph[i].y, kz * ph[i].x};
-      }
-    }
-    a44 = div_wall(o, NR, m, kt, kz, uP[0].data(), uP[1].data(), uP[2].data());
-    for (int i = 0; i < NR; i++) {
-      cd a = uP[0][i], b = uP[1][i];
-      uP[0][i] = cd{a.x - b.y, a.y + b.x};
-      uP[1][i] = cd{a.x + b.y, a.y - b.x};
-    }
-    int w = NR - 1;
-    cd a14 = uP[0][w], a24 = uP[1][w], a34 = uP[2][w], ax, Det;
-    ax.x = a44.x - a24.x * a42.x + a24.y * a42.y - a14.x * a41.x + a14.y * a41.y;
-    ax.y = a44.y - a24.x * a42.y - a24.y * a42.x - a14.x * a41.y - a14.y * a41.x;
-    Det.x = -ax.y - a34.x * a43.x + a34.y * a43.y;
-    Det.y = ax.x - a34.x * a43.y - a34.y * a43.x;
-    double D1 = Det.x * Det.x + Det.y * Det.y;
-    cd iDet = {Det.x / D1, -Det.y / D1};
-    cd col3[4] = {cd{a14.y, -a14.x}, cd{a24.y, -a24.x}, cd{-a34.x, -a34.y}, cd{0.0, 1.0}};
-    for (int j = 0; j < 4; j++) col3[j] = cmul(col3[j], iDet);
-    // Mode (0,0): p_h is constant, so grad p_h and the determinant vanish in exact
-    // arithmetic and the reference inverts rounding noise (0/0 = NaN when the noise
-    // is exactly zero).  The exact correction only changes u_r(0,0), which modeZZ
-    // sets to zero, so no correction is applied to this mode.
-    if (m00)
-      for (int j = 0; j < 4; j++) col3[j] = cd{0.0, 0.0};
-    for (int c = 0; c < 3; c++)
-      for (int i = 0; i < NR; i++) {
-        cd v1 = cmul(col3[c], uh[c][i]), v2 = cmul(col3[3], uP[c][i]);
-        o.V[((size_t)c * NR + i) * NTNZ + k] = double2{v1.x + v2.x, v1.y + v2.y};
-      }
+  std::vector<cd> x(NR, cd{1.0, 0.0});
+  x[NR - 1] = cd{0.0, 0.0};
+  setup::factor_mode(radial_view(o), p.d_im / p.Re, 1.0 / p.dt, 2, 0, 0.0, 0.0, true, Strided<double>{f.data(), 1});
+  setup::solve_mode(NR, Strided<double>{f.data(), 1}, Strided<cd>{x.data(), 1});
+  uc.resize(NR);
+  double Q = 0.0;
+  for (int i = 0; i < NR; i++) {
+    uc[i] = x[i].x;
+    Q += o.rdr[i] * uc[i];
   }
-  // Flux response: u_z-Helmholtz with unit right-hand side, zero wall value, mode (0,0).
-  {
-    std::vector<cd> x(NR, cd{1.0, 0.0});
-    x[NR - 1] = cd{0.0, 0.0};
-    factor_mode(M, 2, 0, 0.0, 0.0, true, f.data());
-    solve_mode(NR, f.data(), x.data());
-    o.uc.resize(NR);
-    double Q = 0.0;
-    for (int i = 0; i < NR; i++) {
-      o.uc[i] = x[i].x;
-      Q += o.rdr[i] * o.uc[i];
-    }
-    o.Qc = Q;
-  }
+  Qc = Q;
+}
+
+void build_operators(const nsp_params& p, HostOps& o) {
+  radial_fd(p.NR, o);
+  o.fac.assign((size_t)4 * p.NR * NFAC * p.NT * p.NZ, 0.0);
+  o.V.assign((size_t)3 * p.NR * p.NT * p.NZ, double2{0.0, 0.0});
+  mode_tables(p, o, o.fac.data(), o.V.data());
+  flux_response(p, o, o.uc, o.Qc);
 }
 
 }  // namespace nsp
