@@ -115,6 +115,17 @@ int nsp_get_state_device(nsp_ctx* ctx, int member, void* ur, void* ut, void* uz)
  * NaN/Inf (the other members are still advanced). */
 int nsp_step(nsp_ctx* ctx, int nsteps, int* iters_out);
 
+/* Host-resident form of integrate() over the whole ensemble: the states in `in` are
+ * advanced by nsteps steps and written to `out`.  Both hold every member's field
+ * member-major -- member 0's u_r, u_theta, u_z, then member 1's, ... (3*NR*NT*NZ
+ * complex doubles per member); in and out may alias.  The result equals
+ * nsp_set_state_host + nsp_step + nsp_get_state_host bit for bit.  The members are
+ * stepped in chunks, each with its own step graph, so that the first step's copies in
+ * and the last step's copies out overlap the other chunks' compute; the host arrays
+ * should be pinned (cudaHostAlloc / cudaHostRegister) for the copies to overlap.
+ * iters_out as nsp_step. */
+int nsp_step_host(nsp_ctx* ctx, int nsteps, const double* in, double* out, int* iters_out);
+
 /* The nonlinear term -(u.grad)u of one member's field (r/theta form), 3/2-dealiased,
  * with the mean pressure-gradient forcing on mode (0,0) (nonlinear,
  * mod_io_nonlinear.cu:380-409).  All six pointers are device arrays of NR*NT*NZ

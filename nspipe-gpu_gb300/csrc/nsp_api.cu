@@ -12,6 +12,7 @@
 #include <sys/stat.h>
 
 #include <cmath>
+#include <algorithm>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -71,6 +72,11 @@ struct nsp_ctx {
   std::vector<cudaStream_t> side;
   cudaEvent_t ev_fork = nullptr;
   std::vector<cudaEvent_t> ev_join;
+  // nsp_step_host: copy streams and per-chunk events (created on first use)
+  cudaStream_t cp_in = nullptr, cp_out = nullptr;
+  std::vector<cudaEvent_t> ev_in, ev_done;
+  std::vector<cudaGraphExec_t> chunk_exec;  // step graphs of the member chunks
+  std::vector<int> chunk_lo;                // their internal member bounds (K+1 values)
   long long Smax = 0;
   std::vector<void*> allocs;
   std::string err;
@@ -166,6 +172,28 @@ Tables member_view(const Group& g, int slot) {
   t.sscal += (size_t)4 * ps;
   t.nsets = 1;
   return t;
+}
+
+// The group's tables and buffers restricted to its members [a, b) (local slots): the
+// kernels then cover only those members (chunked steps).
+void range_view(const Group& g, bool mixed, int a, int b, Tables* t, Bufs* bf) {
+  *t = g.tb;
+  *bf = g.bf;
+  t->nmem = b - a;
+  t->mem0 = g.tb.mem0 + a;
+  if (g.tb.nsets > 1) t->mset = g.tb.mset + a;
+  const size_t s3 = (size_t)a * 3 * g.tb.S;
+  for (int k = 0; k < 2; k++) {
+    bf->U[k] += s3;
+    if (bf->U32[k]) bf->U32[k] += s3;
+    if (bf->DR32[k]) bf->DR32[k] += s3;
+  }
+  bf->RHSW += s3;
+  bf->N += s3;
+  const size_t esz = mixed ? sizeof(float2) : sizeof(double2);
+  const size_t plane = (size_t)g.tb.NR * g.tb.NTP * g.tb.NZ * esz;
+  bf->G = static_cast<char*>(g.bf.G) + (size_t)a * 9 * plane;
+  bf->H = static_cast<char*>(g.bf.H) + (size_t)a * 3 * plane;
 }
 
 int check_params(nsp_ctx* c, const nsp_params& p, int idx) {
@@ -315,8 +343,10 @@ int autotune(nsp_ctx* c) {
   return reset_control(c);
 }
 
-int build_graph(nsp_ctx* c) {
-  if (c->gexec) { cudaGraphExecDestroy(c->gexec); c->gexec = nullptr; }
+// The step graph of the members with internal index in [lo, hi) (all members: the
+// context's step graph; a sub-range: a chunk graph of nsp_step_host) into *out.
+int build_graph_range(nsp_ctx* c, int lo, int hi, cudaGraphExec_t* out) {
+  if (*out) { cudaGraphExecDestroy(*out); *out = nullptr; }
   cudaGraph_t g = nullptr;
   CK(cudaGraphCreate(&g, 0));
   cudaGraphConditionalHandle h;
@@ -356,19 +386,27 @@ int build_graph(nsp_ctx* c) {
     Group& gr = c->groups[k];
     cudaStream_t sk = k == 0 ? c->st : c->side[k - 1];
     if (k > 0) CK(cudaStreamWaitEvent(sk, c->ev_fork, 0));
-    launch_nonlinear(gr.tb, gr.bf, c->dctl, c->precision == NSP_MIXED, nullptr, nullptr, sk);
-    launch_linear(gr.tb, gr.bf, c->dctl, sk);
+    const int a = std::max(lo, gr.tb.mem0) - gr.tb.mem0, b = std::min(hi, gr.tb.mem0 + gr.tb.nmem) - gr.tb.mem0;
+    if (a < b) {  // (an empty branch still forks and joins)
+      Tables t;
+      Bufs bf;
+      range_view(gr, c->precision == NSP_MIXED, a, b, &t, &bf);
+      launch_nonlinear(t, bf, c->dctl, c->precision == NSP_MIXED, nullptr, nullptr, sk);
+      launch_linear(t, bf, c->dctl, sk);
+    }
     if (k > 0) CK(cudaEventRecord(c->ev_join[k - 1], sk));
   }
   for (size_t k = 1; k < ng; k++) CK(cudaStreamWaitEvent(c->st, c->ev_join[k - 1], 0));
   launch_converge(c->dctl, c->nmem, (unsigned long long)h, 1, c->st);
   cudaGraph_t cap = nullptr;
   CK(cudaStreamEndCapture(c->st, &cap));
-  CK(cudaGraphInstantiate(&c->gexec, g, 0));
+  CK(cudaGraphInstantiate(out, g, 0));
   cudaGraphDestroy(g);
   c->use_graph = true;
   return NSP_OK;
 }
+
+int build_graph(nsp_ctx* c) { return build_graph_range(c, 0, c->nmem, &c->gexec); }
 
 }  // namespace
 
@@ -671,24 +709,46 @@ int nsp_save_state(nsp_ctx* c, int m, const char* fr, const char* ft, const char
   return NSP_OK;
 }
 
+// A run of consecutive user members [m0, m0+n) stored in consecutive slots of one
+// group: each component of the run is one pitched copy (host: the members' arrays back
+// to back; device: member stride 3 S).
+static int member_run(nsp_ctx* c, int m0, int mend) {
+  int n = 1;
+  while (m0 + n < mend && c->grp[m0 + n] == c->grp[m0] && c->slot[m0 + n] == c->slot[m0] + n) n++;
+  return n;
+}
+
+static int copy_states(nsp_ctx* c, int m, double* const* host, bool to_device) {
+  const int m0 = m < 0 ? 0 : m, mend = m < 0 ? c->nmem : m + 1;
+  size_t off = 0;  // doubles into each host component array
+  for (int mm = m0; mm < mend;) {
+    const int n = member_run(c, mm, mend);
+    const size_t bytes = sizeof(double2) * (size_t)c->groups[c->grp[mm]].tb.S;
+    for (int k = 0; k < 3; k++) {
+      double* h = host[k] + off;
+      double2* d = state_ptr(c, mm, k);
+      if (to_device)
+        CK(cudaMemcpy2DAsync(d, 3 * bytes, h, bytes, bytes, n, cudaMemcpyHostToDevice, c->st));
+      else
+        CK(cudaMemcpy2DAsync(h, bytes, d, 3 * bytes, bytes, n, cudaMemcpyDeviceToHost, c->st));
+    }
+    off += (size_t)n * bytes / sizeof(double);
+    mm += n;
+  }
+  CK(cudaStreamSynchronize(c->st));
+  return NSP_OK;
+}
+
 // Host transfers of one member, or of all members (member == NSP_ALL_MEMBERS) from/to
-// arrays holding every member's component back to back in member order; one
-// synchronisation per call.
+// arrays holding every member's component back to back in member order; one pitched
+// copy per component per run of members stored together, one synchronisation per call.
 int nsp_set_state_host(nsp_ctx* c, int m, const double* ur, const double* ut, const double* uz) {
   if (!c) return NSP_ERR_ARG;
   if (m != NSP_ALL_MEMBERS)
     if (int rc = check_member(c, m)) return rc;
   if (!ur || !ut || !uz) return fail(c, NSP_ERR_ARG, "null state pointer");
-  const double* src[3] = {ur, ut, uz};
-  size_t off = 0;
-  for (int mm = (m < 0 ? 0 : m); mm < (m < 0 ? c->nmem : m + 1); mm++) {
-    size_t n = 2 * (size_t)c->groups[c->grp[mm]].tb.S;
-    for (int k = 0; k < 3; k++)
-      CK(cudaMemcpyAsync(state_ptr(c, mm, k), src[k] + off, n * sizeof(double), cudaMemcpyHostToDevice, c->st));
-    off += n;
-  }
-  CK(cudaStreamSynchronize(c->st));
-  return NSP_OK;
+  double* src[3] = {const_cast<double*>(ur), const_cast<double*>(ut), const_cast<double*>(uz)};
+  return copy_states(c, m, src, true);
 }
 
 int nsp_get_state_host(nsp_ctx* c, int m, double* ur, double* ut, double* uz) {
@@ -697,15 +757,7 @@ int nsp_get_state_host(nsp_ctx* c, int m, double* ur, double* ut, double* uz) {
     if (int rc = check_member(c, m)) return rc;
   if (!ur || !ut || !uz) return fail(c, NSP_ERR_ARG, "null state pointer");
   double* dst[3] = {ur, ut, uz};
-  size_t off = 0;
-  for (int mm = (m < 0 ? 0 : m); mm < (m < 0 ? c->nmem : m + 1); mm++) {
-    size_t n = 2 * (size_t)c->groups[c->grp[mm]].tb.S;
-    for (int k = 0; k < 3; k++)
-      CK(cudaMemcpyAsync(dst[k] + off, state_ptr(c, mm, k), n * sizeof(double), cudaMemcpyDeviceToHost, c->st));
-    off += n;
-  }
-  CK(cudaStreamSynchronize(c->st));
-  return NSP_OK;
+  return copy_states(c, m, dst, false);
 }
 
 int nsp_set_state_device(nsp_ctx* c, int m, const void* ur, const void* ut, const void* uz) {
@@ -728,6 +780,73 @@ int nsp_get_state_device(nsp_ctx* c, int m, void* ur, void* ut, void* uz) {
   return NSP_OK;
 }
 
+// One step of every member whose phase is 0 at its start (members at -1 sit it out):
+// the step graph, or the same kernels driven from the host (NSP_GRAPH=0).
+static int run_step(nsp_ctx* c, int chunk = -1) {
+  if (c->use_graph) {
+    CK(cudaGraphLaunch(chunk < 0 ? c->gexec : c->chunk_exec[chunk], c->st));
+    return NSP_OK;
+  }
+  const int lo = chunk < 0 ? 0 : c->chunk_lo[chunk], hi = chunk < 0 ? c->nmem : c->chunk_lo[chunk + 1];
+  for (int it = 0; it <= c->hctl.maxit; it++) {
+    for (auto& g : c->groups) {
+      const int a = std::max(lo, g.tb.mem0) - g.tb.mem0, b = std::min(hi, g.tb.mem0 + g.tb.nmem) - g.tb.mem0;
+      if (a >= b) continue;
+      Tables t;
+      Bufs bf;
+      range_view(g, c->precision == NSP_MIXED, a, b, &t, &bf);
+      launch_nonlinear(t, bf, c->dctl, c->precision == NSP_MIXED, nullptr, nullptr, c->st);
+      launch_linear(t, bf, c->dctl, c->st);
+    }
+    launch_converge(c->dctl, c->nmem, 0ull, 0, c->st);
+    CK(cudaGetLastError());
+    int any = 1;
+    CK(cudaMemcpyAsync(&any, &c->dctl->any, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    if (!any) break;
+  }
+  return NSP_OK;
+}
+
+// Copies between a member-major host array (each member's u_r, u_theta, u_z back to
+// back, members in order) and the state buffers of parity `par`, for the members whose
+// internal index is in [lo, hi): one copy per run of members stored together.
+static int copy_chunk(nsp_ctx* c, int lo, int hi, int par, double* host, bool to_device, cudaStream_t st) {
+  std::vector<size_t> off(c->nmem + 1, 0);
+  for (int u = 0; u < c->nmem; u++) off[u + 1] = off[u] + 6 * (size_t)c->groups[c->grp[u]].tb.S;
+  std::vector<int> users;
+  for (int u = 0; u < c->nmem; u++)
+    if (c->internal[u] >= lo && c->internal[u] < hi) users.push_back(u);
+  for (size_t a = 0; a < users.size();) {
+    size_t b = a + 1;
+    while (b < users.size() && users[b] == users[b - 1] + 1 && c->grp[users[b]] == c->grp[users[a]] &&
+           c->slot[users[b]] == c->slot[users[b - 1]] + 1)
+      b++;
+    const int u0 = users[a];
+    Group& g = c->groups[c->grp[u0]];
+    const size_t bytes = (b - a) * 3 * sizeof(double2) * (size_t)g.tb.S;
+    double2* d = g.bf.U[par] + (size_t)c->slot[u0] * 3 * g.tb.S;
+    if (to_device)
+      CK(cudaMemcpyAsync(d, host + off[u0], bytes, cudaMemcpyHostToDevice, st));
+    else
+      CK(cudaMemcpyAsync(host + off[u0], d, bytes, cudaMemcpyDeviceToHost, st));
+    a = b;
+  }
+  return NSP_OK;
+}
+
+// Mixed form: the FP32 mirror of the state for the members with internal index in [lo, hi).
+static void mirror_range(nsp_ctx* c, int lo, int hi, int par) {
+  for (auto& g : c->groups) {
+    const int a = std::max(lo, g.tb.mem0), b = std::min(hi, g.tb.mem0 + g.tb.nmem);
+    if (a >= b) continue;
+    Tables t = g.tb;
+    t.nmem = b - a;
+    const size_t o = (size_t)(a - g.tb.mem0) * 3 * g.tb.S;
+    launch_mirror(t, g.bf.U[par] + o, g.bf.U32[par] + o, g.bf.DR32[par] + o, c->st);
+  }
+}
+
 int nsp_step(nsp_ctx* c, int nsteps, int* iters_out) {
   if (!c) return NSP_ERR_ARG;
   if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_step before nsp_setup");
@@ -746,24 +865,8 @@ int nsp_step(nsp_ctx* c, int nsteps, int* iters_out) {
   for (int done = 0; done < nsteps;) {
     int chunk = std::min(cap, nsteps - done);
     CK(cudaMemsetAsync(&c->dctl->step, 0, sizeof(int), c->st));
-    if (c->use_graph) {
-      for (int s = 0; s < chunk; s++) CK(cudaGraphLaunch(c->gexec, c->st));
-    } else {
-      for (int s = 0; s < chunk; s++) {
-        for (int it = 0; it <= c->hctl.maxit; it++) {
-          for (auto& g : c->groups) {
-            launch_nonlinear(g.tb, g.bf, c->dctl, c->precision == NSP_MIXED, nullptr, nullptr, c->st);
-            launch_linear(g.tb, g.bf, c->dctl, c->st);
-          }
-          launch_converge(c->dctl, nm, 0ull, 0, c->st);
-          CK(cudaGetLastError());
-          int any = 1;
-          CK(cudaMemcpyAsync(&any, &c->dctl->any, sizeof(int), cudaMemcpyDeviceToHost, c->st));
-          CK(cudaStreamSynchronize(c->st));
-          if (!any) break;
-        }
-      }
-    }
+    for (int s = 0; s < chunk; s++)
+      if (int rc = run_step(c)) return rc;
     CK(cudaGetLastError());
     hist.resize((size_t)chunk * nm);
     CK(cudaMemcpyAsync(hist.data(), c->hctl.hist, sizeof(int) * hist.size(), cudaMemcpyDeviceToHost, c->st));
@@ -778,6 +881,115 @@ int nsp_step(nsp_ctx* c, int nsteps, int* iters_out) {
     c->parity ^= (chunk & 1);
     done += chunk;
   }
+  c->launches_last = launches;
+  if (int rc = check_fault(c)) return rc;
+  std::vector<int> status(nm);
+  CK(cudaMemcpy(status.data(), c->hctl.status, sizeof(int) * nm, cudaMemcpyDeviceToHost));
+  for (int m = 0; m < nm; m++)
+    if (status[c->internal[m]] & NSP_ERR_NONFINITE)
+      return fail(c, NSP_ERR_NONFINITE, "member %d: non-finite velocity or convergence measure", m);
+  return NSP_OK;
+}
+
+int nsp_step_host(nsp_ctx* c, int nsteps, const double* in, double* out, int* iters_out) {
+  if (!c) return NSP_ERR_ARG;
+  if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_step_host before nsp_setup");
+  if (nsteps < 0) return fail(c, NSP_ERR_ARG, "nsteps < 0");
+  if (!in || !out) return fail(c, NSP_ERR_ARG, "null state pointer");
+  CK(cudaSetDevice(c->device));
+  const int nm = c->nmem;
+  double* hin = const_cast<double*>(in);
+  if (nsteps == 0) {
+    if (int rc = copy_chunk(c, 0, nm, c->parity, hin, true, c->st)) return rc;
+    if (int rc = copy_chunk(c, 0, nm, c->parity, out, false, c->st)) return rc;
+    CK(cudaStreamSynchronize(c->st));
+    return NSP_OK;
+  }
+  // Member chunks (internal order), each with its own step graph: the first step copies
+  // chunk k+1 in while chunk k steps, the last step copies chunk k out while chunk k+1 steps.
+  int K = nm >= 16 ? 4 : (nm >= 4 ? 2 : 1);
+  if (const char* ke = getenv("NSP_HOST_CHUNKS")) K = std::max(1, std::min(nm, atoi(ke)));  // tuning override
+  if ((int)c->chunk_lo.size() != K + 1) {
+    for (cudaGraphExec_t x : c->chunk_exec)
+      if (x) cudaGraphExecDestroy(x);
+    c->chunk_exec.assign(K, nullptr);
+    c->chunk_lo.resize(K + 1);
+    for (int k = 0; k <= K; k++) c->chunk_lo[k] = (int)((long long)k * nm / K);
+    if (c->use_graph)
+      for (int k = 0; k < K; k++)
+        if (int rc = build_graph_range(c, c->chunk_lo[k], c->chunk_lo[k + 1], &c->chunk_exec[k])) return rc;
+  }
+  if (!c->cp_in) {
+    CK(cudaStreamCreateWithFlags(&c->cp_in, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c->cp_out, cudaStreamNonBlocking));
+  }
+  while ((int)c->ev_in.size() < K) {
+    cudaEvent_t e1, e2;
+    CK(cudaEventCreateWithFlags(&e1, cudaEventDisableTiming));
+    CK(cudaEventCreateWithFlags(&e2, cudaEventDisableTiming));
+    c->ev_in.push_back(e1);
+    c->ev_done.push_back(e2);
+  }
+  // Copies in may start only once earlier work on the state is done.
+  CK(cudaEventRecord(c->ev_done[0], c->st));
+  CK(cudaStreamWaitEvent(c->cp_in, c->ev_done[0], 0));
+  const int cap = c->hctl.hist_cap;
+  const long long per_iter = 4LL * (long long)c->groups.size() + 1;
+  long long launches = 0;
+  std::vector<int> hist;
+  for (int done = 0; done < nsteps;) {
+    const int batch = std::min(cap, nsteps - done);
+    CK(cudaMemsetAsync(&c->dctl->step, 0, sizeof(int), c->st));
+    std::vector<char> chunked(batch, 0);
+    for (int s = 0; s < batch; s++) {
+      const bool first = done + s == 0, last = done + s == nsteps - 1;
+      const int p = c->parity;
+      if (first || last) {
+        chunked[s] = 1;
+        CK(cudaMemsetAsync(&c->dctl->hold, 1, sizeof(int), c->st));
+        for (int k = 0; k < K; k++) {
+          const int lo = c->chunk_lo[k], hi = c->chunk_lo[k + 1];
+          if (first) {
+            if (int rc = copy_chunk(c, lo, hi, p, hin, true, c->cp_in)) return rc;
+            CK(cudaEventRecord(c->ev_in[k], c->cp_in));
+            CK(cudaStreamWaitEvent(c->st, c->ev_in[k], 0));
+            if (c->precision == NSP_MIXED) mirror_range(c, lo, hi, p);
+          }
+          CK(cudaMemsetAsync(c->hctl.phase, 0xFF, sizeof(int) * nm, c->st));  // -1: sits this chunk out
+          CK(cudaMemsetAsync(c->hctl.phase + lo, 0, sizeof(int) * (hi - lo), c->st));
+          if (int rc = run_step(c, k)) return rc;
+          if (last) {
+            CK(cudaEventRecord(c->ev_done[k], c->st));
+            CK(cudaStreamWaitEvent(c->cp_out, c->ev_done[k], 0));
+            if (int rc = copy_chunk(c, lo, hi, p ^ 1, out, false, c->cp_out)) return rc;
+          }
+        }
+        CK(cudaMemsetAsync(&c->dctl->hold, 0, sizeof(int), c->st));
+        launch_finish_step(c->dctl, c->st);
+      } else {
+        if (int rc = run_step(c)) return rc;
+      }
+      CK(cudaGetLastError());
+      c->parity ^= 1;
+    }
+    hist.resize((size_t)batch * nm);
+    CK(cudaMemcpyAsync(hist.data(), c->hctl.hist, sizeof(int) * hist.size(), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (int s = 0; s < batch; s++) {
+      const int* row = hist.data() + (size_t)s * nm;
+      if (chunked[s]) {
+        for (int k = 0; k < K; k++)
+          launches += (1 + *std::max_element(row + c->chunk_lo[k], row + c->chunk_lo[k + 1])) * per_iter;
+      } else {
+        launches += (1 + *std::max_element(row, row + nm)) * per_iter;
+      }
+      if (iters_out)
+        for (int m = 0; m < nm; m++) iters_out[(size_t)(done + s) * nm + m] = row[c->internal[m]];
+    }
+    done += batch;
+  }
+  CK(cudaStreamSynchronize(c->cp_out));
+  CK(cudaStreamSynchronize(c->cp_in));
   c->launches_last = launches;
   if (int rc = check_fault(c)) return rc;
   std::vector<int> status(nm);
@@ -1122,6 +1334,12 @@ int nsp_destroy(nsp_ctx* c) {
   for (cudaStream_t s2 : c->side) cudaStreamDestroy(s2);
   for (cudaEvent_t e2 : c->ev_join) cudaEventDestroy(e2);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
+  if (c->cp_in) cudaStreamSynchronize(c->cp_in), cudaStreamDestroy(c->cp_in);
+  if (c->cp_out) cudaStreamSynchronize(c->cp_out), cudaStreamDestroy(c->cp_out);
+  for (cudaEvent_t e2 : c->ev_in) cudaEventDestroy(e2);
+  for (cudaEvent_t e2 : c->ev_done) cudaEventDestroy(e2);
+  for (cudaGraphExec_t x : c->chunk_exec)
+    if (x) cudaGraphExecDestroy(x);
   if (c->own_st) cudaStreamDestroy(c->own_st);
   delete c;
   return NSP_OK;

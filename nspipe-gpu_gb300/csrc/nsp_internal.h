@@ -100,6 +100,8 @@ struct Ctl {
   int* hist;           // [cap][nmem]: iterations of each step of the call
   int hist_cap;
   int fault;           // nonzero: a device-side wait ran out and a kernel abandoned its work
+  int hold;            // nonzero: a completed step keeps parity and step count (chunked
+                       // steps: members advance chunk by chunk, then finish_step flips once)
 };
 
 // Kernel launchers (nsp_transform.cu, nsp_linear.cu).
@@ -110,6 +112,9 @@ void launch_nonlinear(const Tables& tb, const Bufs& bf, Ctl* dctl, bool mixed, c
                       double2* dst_override, cudaStream_t st, int mask = 7, const float2* src32_override = nullptr);
 void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st);
 void launch_converge(Ctl* dctl, int nmem, unsigned long long cond_handle, int use_cond, cudaStream_t st);
+// Completes a step taken in member chunks: parity flip and step count (converge_k's
+// completion work, held back while the chunks ran).
+void launch_finish_step(Ctl* dctl, cudaStream_t st);
 void launch_lusolve(const Tables& tb, int kind, const double2* rhs, double2* sol, cudaStream_t st);
 void launch_fp64_peak(double* out, int blocks, int threads, int iters, cudaStream_t st);
 // max |div u| over the interior rows -> out[0], over the wall row -> out[1] (ordered bits).

@@ -502,13 +502,18 @@ __global__ void converge_k(Ctl* ctl, cudaGraphConditionalHandle h, int use_cond)
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    if (!any) {
+    if (!any && !ctl->hold) {
       ctl->parity ^= 1;
       ctl->step += 1;
     }
     ctl->any = any;
     if (use_cond) cudaGraphSetConditional(h, any ? 1u : 0u);
   }
+}
+
+__global__ void finish_step_k(Ctl* ctl) {
+  ctl->parity ^= 1;
+  ctl->step += 1;
 }
 
 // Divergence diagnostic of one member's state (div_k / divWall_k, mod_radialFD.cu:34-96):
@@ -685,6 +690,8 @@ void launch_converge(Ctl* dctl, int nmem, unsigned long long cond_handle, int us
   (void)nmem;
   converge_k<<<1, 256, 0, st>>>(dctl, (cudaGraphConditionalHandle)cond_handle, use_cond);
 }
+
+void launch_finish_step(Ctl* dctl, cudaStream_t st) { finish_step_k<<<1, 1, 0, st>>>(dctl); }
 
 void launch_lusolve(const Tables& tb, int kind, const double2* rhs, double2* sol, cudaStream_t st) {
   lusolve_k<<<(tb.NTNZ + 127) / 128, 128, 0, st>>>(tb, kind, rhs, sol);

@@ -29,7 +29,7 @@ EXPORTS = [
     "nsp_get_params", "nsp_info", "nsp_run_default_opts", "nsp_run_open", "nsp_run_resume", "nsp_run_advance",
     "nsp_run_checkpoint", "nsp_run_time", "nsp_run_close", "nsp_checkpoint_info", "nsp_output_schedule",
     "nsp_remesh_create", "nsp_remesh_matrix", "nsp_remesh_device", "nsp_remesh_members", "nsp_remesh_files",
-    "nsp_remesh_destroy",
+    "nsp_remesh_destroy", "nsp_step_host",
 ]
 
 
@@ -87,6 +87,7 @@ def lib():
         L.nsp_set_state_device.argtypes = [vp, ip, vp, vp, vp]
         L.nsp_get_state_device.argtypes = [vp, ip, vp, vp, vp]
         L.nsp_step.argtypes = [vp, ip, ctypes.POINTER(ctypes.c_int)]
+        L.nsp_step_host.argtypes = [vp, ip, dp, dp, ctypes.POINTER(ctypes.c_int)]
         L.nsp_nonlinear.argtypes = [vp, ip, vp, vp, vp, vp, vp, vp]
         L.nsp_lusolve.argtypes = [vp, ip, ip, vp, vp]
         L.nsp_diag.argtypes = [vp, ip, ctypes.POINTER(NspDiag)]
@@ -247,6 +248,36 @@ class Stepper:
         if check:
             self._check(rc)
         return iters
+
+    def member_major_size(self):
+        return 3 * self._all_size()
+
+    def pack(self, fields):
+        """Member-major array (each member's u_r, u_theta, u_z back to back) of per-member fields."""
+        return np.concatenate([np.ascontiguousarray(a, np.complex128).reshape(-1) for f in fields for a in f])
+
+    def unpack(self, flat):
+        """Per-member [u_r, u_theta, u_z] views of a member-major array."""
+        out, off = [], 0
+        for m in range(self.n):
+            n = int(np.prod(self.shape(m)))
+            out.append([flat[off + c * n: off + (c + 1) * n].reshape(self.shape(m)) for c in range(3)])
+            off += 3 * n
+        return out
+
+    def step_host(self, nsteps, u, out=None, check=True):
+        """Host-resident steps (nsp_step_host) on a member-major array; returns (out, iters).
+        Copies overlap compute member chunk by chunk (pin the arrays for the overlap)."""
+        u = np.ascontiguousarray(u, np.complex128)
+        out = out if out is not None else np.zeros(self.member_major_size(), np.complex128)
+        for a in (u, out):
+            if a.size != self.member_major_size() or a.dtype != np.complex128 or not a.flags["C_CONTIGUOUS"]:
+                raise ValueError("expected C-contiguous complex128 arrays of %d values" % self.member_major_size())
+        iters = np.zeros((nsteps, self.n), np.int32)
+        rc = lib().nsp_step_host(self._h, nsteps, _dp(u), _dp(out), iters.ctypes.data_as(ctypes.POINTER(ctypes.c_int)))
+        if check:
+            self._check(rc)
+        return out, iters
 
     def kernel_launches(self):
         return lib().nsp_kernel_launches(self._h)

@@ -75,3 +75,63 @@ def test_uneven_mixed_close_to_fp64(nsp):
         st.close()
     for m in range(len(NAMES)):
         assert rel(res[nsp.NSP_MIXED][m], res[nsp.NSP_FP64][m]) < 1e-6, m
+
+
+def test_all_member_transfers_interleaved_groups(nsp):
+    """NSP_ALL_MEMBERS transfers (one pitched copy per component per run of members
+    stored together) on members whose groups interleave in user order: the arrays
+    hold each member's component back to back in user order, both directions."""
+    from conftest import PI2
+    shapes = [(24, 8, 9), (32, 16, 17), (24, 8, 9), (24, 8, 9), (32, 16, 17)]
+    st = nsp.Stepper([nsp.make_params(*s, 1000.0 + 50 * k, 0.005, PI2) for k, s in enumerate(shapes)])
+    fields = [nsp.seeded_field(*s, PI2, 0.05, 60 + k) for k, s in enumerate(shapes)]
+    flat = [np.concatenate([f[c].reshape(-1) for f in fields]) for c in range(3)]
+    st.set_states_all(flat)
+    for k, f in enumerate(fields):
+        got = st.get_state(k)
+        for c in range(3):
+            assert np.array_equal(got[c], f[c]), (k, c)
+    st.step(2)
+    back = st.get_states_all()
+    off = 0
+    for k, s in enumerate(shapes):
+        n = int(np.prod(s))
+        one = st.get_state(k)
+        for c in range(3):
+            assert np.array_equal(back[c][off:off + n].reshape(s), one[c]), (k, c)
+        off += n
+    st.close()
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+@pytest.mark.parametrize("nsteps", [1, 3])
+def test_step_host_matches_step(nsp, precision, nsteps):
+    """nsp_step_host (members stepped in chunks, copies overlapping compute) gives the
+    states and iteration counts of set_states_all + step + get_states_all bit for bit,
+    on 17 members of two interleaved shapes (chunks straddle the groups), and leaves
+    the context ready for further steps."""
+    from conftest import PI2
+    shapes = [(24, 8, 9) if k % 3 else (32, 16, 17) for k in range(17)]
+    prm = [nsp.make_params(*s, 1000.0 + 10 * k, 0.005, PI2) for k, s in enumerate(shapes)]
+    fields = [nsp.seeded_field(*s, PI2, 0.05, 80 + k) for k, s in enumerate(shapes)]
+    flat = [np.concatenate([f[c].reshape(-1) for f in fields]) for c in range(3)]
+    a = nsp.Stepper(prm, precision=precision)
+    a.set_states_all(flat)
+    it_a = a.step(nsteps)
+    out_a = a.get_states_all()
+    b = nsp.Stepper(prm, precision=precision)
+    out_b, it_b = b.step_host(nsteps, b.pack(fields))
+    for m, f in enumerate(b.unpack(out_b)):  # member-major out vs component-major out_a
+        n = f[0].size
+        off = sum(int(np.prod(s)) for s in shapes[:m])
+        for c in range(3):
+            assert np.array_equal(f[c].reshape(-1), out_a[c][off:off + n]), (m, c)
+    assert np.array_equal(it_a, it_b)
+    same, _ = b.step_host(0, out_b)  # zero steps: in -> state -> out
+    assert np.array_equal(same, out_b)
+    a.step(2)
+    b.step(2)
+    for c, (x, y) in enumerate(zip(a.get_states_all(), b.get_states_all())):
+        assert np.array_equal(x, y), c
+    a.close()
+    b.close()
