@@ -173,6 +173,14 @@ int nsp_mean_profile(nsp_ctx* ctx, int member, double* out);
  * Computed in FP64 on the device; q and u are host arrays of NZR doubles. */
 int nsp_cross_sections(nsp_ctx* ctx, int member, double* q, double* u);
 
+/* The same three diagnostics for every member at once (one launch per member group and
+ * kernel, one synchronisation): out[n_members]; mean profiles and cross sections of all
+ * members back to back in member order (sum of NR_m, resp. NZR_m values).  Values equal
+ * the per-member calls' bit for bit. */
+int nsp_diag_all(nsp_ctx* ctx, nsp_diag_out* out);
+int nsp_mean_profile_all(nsp_ctx* ctx, double* out);
+int nsp_cross_sections_all(nsp_ctx* ctx, double* q, double* u);
+
 /* Number of kernel launches issued by the last nsp_step call (all graph nodes run). */
 long long nsp_kernel_launches(nsp_ctx* ctx);
 

@@ -1062,6 +1062,38 @@ int nsp_lusolve(nsp_ctx* c, int m, int kind, const void* rhs, void* sol) {
   return NSP_OK;
 }
 
+// Friction diagnostics of one member from Re u_z(0,0)(r_i) (wrt_frc_k,
+// mod_io_nonlinear.cu:40-52; flux as adj_flux, mod_cublasflux.cu:90-103).
+static void friction(const HostOps& o, int NR, const double* uz0, double Re, nsp_diag_out* out) {
+  double ucen = 0.0, du = 0.0, Q = 0.0;
+  for (int i = 0; i <= IW; i++) ucen += uz0[i] * o.dr0[i];
+  for (int i = 0; i < STEN; i++) du += uz0[NR - STEN + i] * o.D[(size_t)(NR - 1) * STEN + i];
+  for (int i = 0; i < NR; i++) Q += o.rdr[i] * uz0[i];
+  out->u_centre = ucen;
+  out->u_tau = std::sqrt(std::fabs(du) / Re);
+  out->flux = Q;
+  out->re_tau = Re * out->u_tau;
+}
+
+static int ensure_diagbuf(nsp_ctx* c) {
+  if (!c->diagbuf) {
+    void* p = nullptr;
+    if (int rc = dalloc(c, &p, 2 * sizeof(unsigned long long) * c->nmem)) return rc;
+    c->diagbuf = static_cast<unsigned long long*>(p);
+  }
+  return NSP_OK;
+}
+
+static int ensure_crossbuf(nsp_ctx* c, size_t n) {
+  if (c->crossbuf_n < n) {  // grows to the largest size asked for, then reused
+    void* p = nullptr;
+    if (int rc = dalloc(c, &p, n * sizeof(double))) return rc;
+    c->crossbuf = static_cast<double*>(p);
+    c->crossbuf_n = n;
+  }
+  return NSP_OK;
+}
+
 int nsp_diag(nsp_ctx* c, int m, nsp_diag_out* out) {
   if (int rc = check_member(c, m)) return rc;
   if (!out) return fail(c, NSP_ERR_ARG, "null output");
@@ -1079,25 +1111,14 @@ int nsp_diag(nsp_ctx* c, int m, nsp_diag_out* out) {
   int ite = 0;
   CK(cudaMemcpyAsync(&ite, c->hctl.ite + mi, sizeof(int), cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
-  const HostOps& o = g.ops;
-  double ucen = 0.0, du = 0.0, Q = 0.0;
-  for (int i = 0; i <= IW; i++) ucen += uz[i].x * o.dr0[i];
-  for (int i = 0; i < STEN; i++) du += uz[NR - STEN + i].x * o.D[(size_t)(NR - 1) * STEN + i];
-  for (int i = 0; i < NR; i++) Q += o.rdr[i] * uz[i].x;
-  out->u_centre = ucen;
-  const double Re_m = c->prm[m].Re;
-  out->u_tau = std::sqrt(std::fabs(du) / Re_m);
-  out->flux = Q;
+  std::vector<double> uz0(NR);
+  for (int i = 0; i < NR; i++) uz0[i] = uz[i].x;
+  friction(g.ops, NR, uz0.data(), c->prm[m].Re, out);
   out->last_err = err;
   out->last_iters = ite;
   out->status = (status & NSP_ERR_NONFINITE) ? NSP_ERR_NONFINITE : NSP_OK;
-  out->re_tau = Re_m * out->u_tau;
   // Divergence of the state on the device.
-  if (!c->diagbuf) {
-    void* p = nullptr;
-    if (int rc = dalloc(c, &p, 2 * sizeof(unsigned long long))) return rc;
-    c->diagbuf = static_cast<unsigned long long*>(p);
-  }
+  if (int rc = ensure_diagbuf(c)) return rc;
   CK(cudaMemsetAsync(c->diagbuf, 0, 2 * sizeof(unsigned long long), c->st));
   launch_diag_div(g.tb, state_ptr(c, m, 0), c->diagbuf, c->st);
   CK(cudaGetLastError());
@@ -1111,6 +1132,115 @@ int nsp_diag(nsp_ctx* c, int m, nsp_diag_out* out) {
   return NSP_OK;
 }
 
+// Re u_z(0,0)(r) of every member into prof (internal order, each group's members
+// NR_g values apiece) on the device, then to the host.  poff[g]: group offsets.
+static int gather_means(nsp_ctx* c, std::vector<double>& prof, std::vector<size_t>& poff) {
+  size_t n = 0;
+  poff.assign(c->groups.size(), 0);
+  for (size_t k = 0; k < c->groups.size(); k++) {
+    poff[k] = n;
+    n += (size_t)c->groups[k].tb.nmem * c->groups[k].tb.NR;
+  }
+  if (int rc = ensure_crossbuf(c, n)) return rc;
+  for (size_t k = 0; k < c->groups.size(); k++) {
+    const Group& g = c->groups[k];
+    launch_gather_mean(g.tb, g.bf.U[c->parity], c->crossbuf + poff[k], g.tb.nmem, c->st);
+  }
+  CK(cudaGetLastError());
+  prof.resize(n);
+  CK(cudaMemcpyAsync(prof.data(), c->crossbuf, n * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  return NSP_OK;
+}
+
+int nsp_diag_all(nsp_ctx* c, nsp_diag_out* out) {
+  if (!c) return NSP_ERR_ARG;
+  if (!out) return fail(c, NSP_ERR_ARG, "null output");
+  if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_diag_all before nsp_setup");
+  const int nm = c->nmem;
+  if (int rc = ensure_diagbuf(c)) return rc;
+  CK(cudaMemsetAsync(c->diagbuf, 0, 2 * sizeof(unsigned long long) * nm, c->st));
+  for (const Group& g : c->groups)
+    launch_diag_div(g.tb, g.bf.U[c->parity], c->diagbuf + 2 * g.tb.mem0, c->st, g.tb.nmem);
+  CK(cudaGetLastError());
+  std::vector<unsigned long long> bits(2 * (size_t)nm);
+  std::vector<double> err(nm);
+  std::vector<int> status(nm), ite(nm);
+  CK(cudaMemcpyAsync(bits.data(), c->diagbuf, sizeof(unsigned long long) * bits.size(), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(err.data(), c->hctl.err, sizeof(double) * nm, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(status.data(), c->hctl.status, sizeof(int) * nm, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(ite.data(), c->hctl.ite, sizeof(int) * nm, cudaMemcpyDeviceToHost, c->st));
+  std::vector<double> prof;
+  std::vector<size_t> poff;
+  if (int rc = gather_means(c, prof, poff)) return rc;  // synchronises the stream
+  for (int m = 0; m < nm; m++) {
+    const int gi = c->grp[m], mi = c->internal[m];
+    const Group& g = c->groups[gi];
+    friction(g.ops, g.tb.NR, prof.data() + poff[gi] + (size_t)c->slot[m] * g.tb.NR, c->prm[m].Re, out + m);
+    out[m].last_err = err[mi];
+    out[m].last_iters = ite[mi];
+    out[m].status = (status[mi] & NSP_ERR_NONFINITE) ? NSP_ERR_NONFINITE : NSP_OK;
+    double dv[2];
+    memcpy(dv, bits.data() + 2 * (size_t)mi, sizeof dv);
+    out[m].div_max = dv[0];
+    out[m].div_wall = dv[1];
+  }
+  return NSP_OK;
+}
+
+int nsp_mean_profile_all(nsp_ctx* c, double* out) {
+  if (!c) return NSP_ERR_ARG;
+  if (!out) return fail(c, NSP_ERR_ARG, "null output");
+  std::vector<double> prof;
+  std::vector<size_t> poff;
+  if (int rc = gather_means(c, prof, poff)) return rc;
+  size_t o = 0;
+  for (int m = 0; m < c->nmem; m++) {
+    const Group& g = c->groups[c->grp[m]];
+    memcpy(out + o, prof.data() + poff[c->grp[m]] + (size_t)c->slot[m] * g.tb.NR, sizeof(double) * g.tb.NR);
+    o += g.tb.NR;
+  }
+  return NSP_OK;
+}
+
+int nsp_cross_sections_all(nsp_ctx* c, double* q, double* u) {
+  if (!c) return NSP_ERR_ARG;
+  if (!q || !u) return fail(c, NSP_ERR_ARG, "null output");
+  if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_cross_sections_all before nsp_setup");
+  std::vector<size_t> poff(c->groups.size());
+  size_t n = 0;
+  for (size_t k = 0; k < c->groups.size(); k++) {
+    poff[k] = n;
+    n += (size_t)c->groups[k].tb.nmem * 2 * c->groups[k].tb.NR * c->groups[k].tb.NZR;
+  }
+  if (int rc = ensure_crossbuf(c, n)) return rc;
+  for (size_t k = 0; k < c->groups.size(); k++) {
+    const Group& g = c->groups[k];
+    launch_diag_cross(g.tb, g.bf.U[c->parity], c->crossbuf + poff[k], c->st, g.tb.nmem);
+  }
+  CK(cudaGetLastError());
+  std::vector<double> part(n);
+  CK(cudaMemcpyAsync(part.data(), c->crossbuf, n * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  size_t o = 0;
+  for (int m = 0; m < c->nmem; m++) {
+    const Group& g = c->groups[c->grp[m]];
+    const int NR = g.tb.NR, NZR = g.tb.NZR;
+    const double* pm = part.data() + poff[c->grp[m]] + (size_t)c->slot[m] * 2 * NR * NZR;
+    for (int z = 0; z < NZR; z++) {
+      double sq = 0.0, su = 0.0;
+      for (int i = 0; i < NR; i++) {  // the radial quadrature, in level order
+        sq += pm[(size_t)i * NZR + z];
+        su += pm[(size_t)(NR + i) * NZR + z];
+      }
+      q[o + z] = sq;
+      u[o + z] = su;
+    }
+    o += NZR;
+  }
+  return NSP_OK;
+}
+
 int nsp_cross_sections(nsp_ctx* c, int m, double* q, double* u) {
   if (int rc = check_member(c, m)) return rc;
   if (!q || !u) return fail(c, NSP_ERR_ARG, "null output");
@@ -1118,12 +1248,7 @@ int nsp_cross_sections(nsp_ctx* c, int m, double* q, double* u) {
   const Group& g = c->groups[c->grp[m]];
   const int NR = g.tb.NR, NZR = g.tb.NZR;
   const size_t n = (size_t)2 * NR * NZR;
-  if (c->crossbuf_n < n) {  // grows to the largest member shape asked for, then reused
-    void* p = nullptr;
-    if (int rc = dalloc(c, &p, n * sizeof(double))) return rc;
-    c->crossbuf = static_cast<double*>(p);
-    c->crossbuf_n = n;
-  }
+  if (int rc = ensure_crossbuf(c, n)) return rc;
   launch_diag_cross(g.tb, state_ptr(c, m, 0), c->crossbuf, c->st);
   CK(cudaGetLastError());
   std::vector<double> part(n);

@@ -117,10 +117,13 @@ void launch_converge(Ctl* dctl, int nmem, unsigned long long cond_handle, int us
 void launch_finish_step(Ctl* dctl, cudaStream_t st);
 void launch_lusolve(const Tables& tb, int kind, const double2* rhs, double2* sol, cudaStream_t st);
 void launch_fp64_peak(double* out, int blocks, int threads, int iters, cudaStream_t st);
-// max |div u| over the interior rows -> out[0], over the wall row -> out[1] (ordered bits).
-void launch_diag_div(const Tables& tb, const double2* U, unsigned long long* out, cudaStream_t st);
-// Per-level partials of the q / u cross-section diagnostics: part[2][NR][NZR].
-void launch_diag_cross(const Tables& tb, const double2* U, double* part, cudaStream_t st);
+// max |div u| over the interior rows -> out[0], over the wall row -> out[1] (ordered bits);
+// nmem consecutive members from U: out[2 * member + 0/1].
+void launch_diag_div(const Tables& tb, const double2* U, unsigned long long* out, cudaStream_t st, int nmem = 1);
+// Per-level partials of the q / u cross-section diagnostics: part[member][2][NR][NZR].
+void launch_diag_cross(const Tables& tb, const double2* U, double* part, cudaStream_t st, int nmem = 1);
+// Re u_z(0,0)(r_i) of nmem consecutive members: out[member][NR].
+void launch_gather_mean(const Tables& tb, const double2* U, double* out, int nmem, cudaStream_t st);
 // Fixed device scratch of the allocation-free entry point (nsp_noalloc.cu).
 size_t noalloc_scratch_bytes();
 cudaError_t noalloc_scratch(int device, void** ptr);

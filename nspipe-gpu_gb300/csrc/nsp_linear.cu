@@ -523,6 +523,8 @@ __global__ void diag_div_k(Tables tb, const double2* __restrict__ U, unsigned lo
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int NR = tb.NR, NT = tb.NT, NZ = tb.NZ, NTNZ = tb.NTNZ;
   const long long S = tb.S;
+  U += (size_t)blockIdx.z * 3 * S;  // member blockIdx.z of a batched launch
+  out += 2 * blockIdx.z;
   double mi = 0.0, mw = 0.0;
   if (k < NTNZ) {
     const int it = k / NZ, l = k - it * NZ, m = it < NT / 2 ? it : it - NT;
@@ -557,8 +559,20 @@ __global__ void diag_div_k(Tables tb, const double2* __restrict__ U, unsigned lo
   }
 }
 
-void launch_diag_div(const Tables& tb, const double2* U, unsigned long long* out, cudaStream_t st) {
-  diag_div_k<<<(tb.NTNZ + 127) / 128, 128, 0, st>>>(tb, U, out);
+void launch_diag_div(const Tables& tb, const double2* U, unsigned long long* out, cudaStream_t st, int nmem) {
+  diag_div_k<<<dim3((tb.NTNZ + 127) / 128, 1, nmem), 128, 0, st>>>(tb, U, out);
+}
+
+// Re u_z(m=0, k_z=0)(r_i) of nmem consecutive members -> out[member][NR].
+__global__ void gather_mean_k(Tables tb, const double2* __restrict__ U, double* __restrict__ out, int nmem) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= nmem * tb.NR) return;
+  const int m = q / tb.NR, i = q - m * tb.NR;
+  out[q] = U[((size_t)m * 3 + 2) * tb.S + (size_t)i * tb.NTNZ].x;
+}
+
+void launch_gather_mean(const Tables& tb, const double2* U, double* out, int nmem, cudaStream_t st) {
+  gather_mean_k<<<(nmem * tb.NR + 127) / 128, 128, 0, st>>>(tb, U, out, nmem);
 }
 
 // Cross-section diagnostics of one member's state (wrt_qcr / wrt_ucr with q0kernel_k,
@@ -577,6 +591,8 @@ __global__ void diag_cross_k(Tables tb, const double2* __restrict__ U, double* _
   const int NT = tb.NT, NZ = tb.NZ, NZR = tb.NZR, NTNZ = tb.NTNZ;
   if (n >= NZR) return;
   const long long S = tb.S;
+  U += (size_t)blockIdx.z * 3 * S;  // member blockIdx.z of a batched launch
+  part += (size_t)blockIdx.z * 2 * tb.NR * NZR;
   double ms[3];
   for (int c = 0; c < 3; c++) {
     const double2* col = U + c * S + (size_t)i * NTNZ;
@@ -608,8 +624,8 @@ __global__ void diag_cross_k(Tables tb, const double2* __restrict__ U, double* _
   part[(size_t)(tb.NR + i) * NZR + n] = w * ms[2];
 }
 
-void launch_diag_cross(const Tables& tb, const double2* U, double* part, cudaStream_t st) {
-  dim3 g((tb.NZR + 63) / 64, tb.NR);
+void launch_diag_cross(const Tables& tb, const double2* U, double* part, cudaStream_t st, int nmem) {
+  dim3 g((tb.NZR + 63) / 64, tb.NR, nmem);
   diag_cross_k<<<g, 64, 0, st>>>(tb, U, part);
 }
 

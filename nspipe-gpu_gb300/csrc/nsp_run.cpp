@@ -5,15 +5,16 @@
 // the final state dump (main.cu:42-44), and checkpoints with a JSON sidecar.
 //
 // Host code only: the context is driven through its public entry points (nsp_step in
-// chunks that end where a row or a checkpoint is due, then nsp_diag,
-// nsp_cross_sections and nsp_mean_profile for the rows), so the driver is the same for
-// both precisions and every member layout.
+// chunks that end where a row or a checkpoint is due, then nsp_diag_all,
+// nsp_cross_sections_all and nsp_mean_profile_all, one batched call per kind for every
+// member), so the driver is the same for both precisions and every member layout.
 #include <dirent.h>
 #include <sys/stat.h>
 #include <sys/types.h>
 #include <unistd.h>
 
 #include <algorithm>
+#include <array>
 #include <cerrno>
 #include <cinttypes>
 #include <cmath>
@@ -505,33 +506,59 @@ int steps_until_due(double acc, double dt, double interval, int cap) {
   return cap;
 }
 
-// Rows of one member after a chunk whose last step made the rows in due[] due
-// (wrt_frc, wrt_qcr + wrt_ucr, wrt_mpr in integrate's order, mod_integrate.cu:134-152).
-int sample(nsp_run* r, int mi, const bool due[3], long long target) {
-  Member& m = r->mem[mi];
-  if (due[0]) {
-    nsp_diag_out d{};
-    if (int rc = nsp_diag(r->ctx, mi, &d)) return rc;
-    if (r->o.verbose) {
-      printf("\n err=%e\n", d.last_err);
-      if (r->mem.size() > 1) printf(" Step %lld of %lld (member %d)\n", m.step, target, mi);
-      else printf(" Step %lld of %lld\n", m.step, target);
+// Rows after a chunk whose last step made them due (due[member][kind]): wrt_frc,
+// wrt_qcr + wrt_ucr, wrt_mpr in integrate's order (mod_integrate.cu:134-152).  Each
+// kind is sampled for every member in one batched call when any member is due.
+int sample(nsp_run* r, const std::vector<std::array<bool, 3>>& due, long long target) {
+  const int n = (int)r->mem.size();
+  bool any[3] = {false, false, false};
+  for (int i = 0; i < n; i++)
+    for (int c = 0; c < 3; c++) any[c] = any[c] || due[i][c];
+  if (any[0]) {
+    std::vector<nsp_diag_out> d(n);
+    if (int rc = nsp_diag_all(r->ctx, d.data())) return rc;
+    for (int i = 0; i < n; i++) {
+      if (!due[i][0]) continue;
+      Member& m = r->mem[i];
+      if (r->o.verbose) {
+        printf("\n err=%e\n", d[i].last_err);
+        if (n > 1) printf(" Step %lld of %lld (member %d)\n", m.step, target, i);
+        else printf(" Step %lld of %lld\n", m.step, target);
+      }
+      if (m.out[F_FRC].f)
+        if (int rc = add_row(r, m.out[F_FRC], e8(m.t) + "  " + e8(d[i].u_centre) + "  " + e8(d[i].u_tau) + "\n"))
+          return rc;
     }
-    if (m.out[F_FRC].f)
-      if (int rc = add_row(r, m.out[F_FRC], e8(m.t) + "  " + e8(d.u_centre) + "  " + e8(d.u_tau) + "\n")) return rc;
   }
-  if (due[1] && (m.out[F_QCR].f || m.out[F_UCR].f)) {
-    std::vector<double> q(m.NZR), u(m.NZR);
-    if (int rc = nsp_cross_sections(r->ctx, mi, q.data(), u.data())) return rc;
-    if (m.out[F_QCR].f)
-      if (int rc = add_row(r, m.out[F_QCR], value_row(m.t, q.data(), m.NZR))) return rc;
-    if (m.out[F_UCR].f)
-      if (int rc = add_row(r, m.out[F_UCR], value_row(m.t, u.data(), m.NZR))) return rc;
+  if (any[1]) {
+    size_t tot = 0;
+    for (const Member& m : r->mem) tot += m.NZR;
+    std::vector<double> q(tot), u(tot);
+    if (int rc = nsp_cross_sections_all(r->ctx, q.data(), u.data())) return rc;
+    size_t o = 0;
+    for (int i = 0; i < n; i++) {
+      Member& m = r->mem[i];
+      if (due[i][1]) {
+        if (m.out[F_QCR].f)
+          if (int rc = add_row(r, m.out[F_QCR], value_row(m.t, q.data() + o, m.NZR))) return rc;
+        if (m.out[F_UCR].f)
+          if (int rc = add_row(r, m.out[F_UCR], value_row(m.t, u.data() + o, m.NZR))) return rc;
+      }
+      o += m.NZR;
+    }
   }
-  if (due[2] && m.out[F_MNP].f) {
-    std::vector<double> prof(m.p.NR);
-    if (int rc = nsp_mean_profile(r->ctx, mi, prof.data())) return rc;
-    if (int rc = add_row(r, m.out[F_MNP], value_row(m.t, prof.data(), m.p.NR))) return rc;
+  if (any[2]) {
+    size_t tot = 0;
+    for (const Member& m : r->mem) tot += m.p.NR;
+    std::vector<double> prof(tot);
+    if (int rc = nsp_mean_profile_all(r->ctx, prof.data())) return rc;
+    size_t o = 0;
+    for (int i = 0; i < n; i++) {
+      Member& m = r->mem[i];
+      if (due[i][2] && m.out[F_MNP].f)
+        if (int rc = add_row(r, m.out[F_MNP], value_row(m.t, prof.data() + o, m.p.NR))) return rc;
+      o += m.p.NR;
+    }
   }
   return NSP_OK;
 }
@@ -751,20 +778,25 @@ int nsp_run_advance(nsp_run* r, int nsteps, int* iters_out) {
     if (iters_out) std::copy(it.begin(), it.end(), iters_out + (size_t)done * n);
     r->step += k;
     done += k;
+    std::vector<std::array<bool, 3>> due(n);
     for (int i = 0; i < n; i++) {
       Member& m = r->mem[i];
-      bool due[3] = {false, false, false};
+      due[i] = {false, false, false};
       for (int j = 0; j < k; j++) {  // c_t++; t += dt; t_frc += dt; ... (mod_integrate.cu:131)
         m.step++;
         m.t += m.p.dt;
         for (int c = 0; c < 3; c++) {
           m.acc[c] += m.p.dt;
-          due[c] = r->interval[c] >= 0.0 && m.acc[c] >= r->interval[c];
-          if (due[c]) m.acc[c] = 0.0;
+          due[i][c] = r->interval[c] >= 0.0 && m.acc[c] >= r->interval[c];
+          if (due[i][c]) m.acc[c] = 0.0;
         }
       }
-      if (int s = sample(r, i, due, target)) return s;
+      // a row only where the member writes that file, or prints progress
+      due[i][0] = due[i][0] && (m.out[F_FRC].f || r->o.verbose);
+      due[i][1] = due[i][1] && (m.out[F_QCR].f || m.out[F_UCR].f);
+      due[i][2] = due[i][2] && m.out[F_MNP].f;
     }
+    if (int s = sample(r, due, target)) return s;
     if (rc == NSP_ERR_NONFINITE) {
       flush_all(r);
       return rc;

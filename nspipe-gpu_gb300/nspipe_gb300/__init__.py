@@ -29,7 +29,7 @@ EXPORTS = [
     "nsp_get_params", "nsp_info", "nsp_run_default_opts", "nsp_run_open", "nsp_run_resume", "nsp_run_advance",
     "nsp_run_checkpoint", "nsp_run_time", "nsp_run_close", "nsp_checkpoint_info", "nsp_output_schedule",
     "nsp_remesh_create", "nsp_remesh_matrix", "nsp_remesh_device", "nsp_remesh_members", "nsp_remesh_files",
-    "nsp_remesh_destroy", "nsp_step_host",
+    "nsp_remesh_destroy", "nsp_step_host", "nsp_diag_all", "nsp_mean_profile_all", "nsp_cross_sections_all",
 ]
 
 
@@ -101,6 +101,9 @@ def lib():
         L.nsp_nonlinear_static.argtypes = [vp, ip, vp, vp]
         L.nsp_describe.argtypes = [vp, ctypes.c_char_p, ip]
         L.nsp_mean_profile.argtypes = [vp, ip, dp]
+        L.nsp_diag_all.argtypes = [vp, ctypes.POINTER(NspDiag)]
+        L.nsp_mean_profile_all.argtypes = [vp, dp]
+        L.nsp_cross_sections_all.argtypes = [vp, dp, dp]
         L.nsp_cross_sections.argtypes = [vp, ip, dp, dp]
         L.nsp_get_params.argtypes = [vp, ip, ctypes.POINTER(NspParams)]
         L.nsp_info.argtypes = [vp, ctypes.POINTER(ip), ctypes.POINTER(ip)]
@@ -316,6 +319,27 @@ class Stepper:
         q, u = np.zeros(nzr), np.zeros(nzr)
         self._check(lib().nsp_cross_sections(self._h, m, _dp(q), _dp(u)))
         return q, u
+
+    def diag_all(self):
+        """nsp_diag of every member in one pass: a list of NspDiag in member order."""
+        out = (NspDiag * self.n)()
+        self._check(lib().nsp_diag_all(self._h, out))
+        return list(out)
+
+    def mean_profile_all(self):
+        """Mean profiles of every member (list of arrays of NR_m values)."""
+        sizes = [p.NR for p in self.params]
+        flat = np.zeros(sum(sizes))
+        self._check(lib().nsp_mean_profile_all(self._h, _dp(flat)))
+        return np.split(flat, np.cumsum(sizes)[:-1])
+
+    def cross_sections_all(self):
+        """(q, u) cross sections of every member (lists of arrays of NZR_m values)."""
+        sizes = [3 * (p.NZ - 1) for p in self.params]
+        q, u = np.zeros(sum(sizes)), np.zeros(sum(sizes))
+        self._check(lib().nsp_cross_sections_all(self._h, _dp(q), _dp(u)))
+        cut = np.cumsum(sizes)[:-1]
+        return np.split(q, cut), np.split(u, cut)
 
     def grid(self, m=0):
         NR = self.params[m].NR

@@ -135,3 +135,25 @@ def test_step_host_matches_step(nsp, precision, nsteps):
         assert np.array_equal(x, y), c
     a.close()
     b.close()
+
+
+def test_batched_diagnostics_equal_per_member(nsp):
+    """nsp_diag_all / nsp_mean_profile_all / nsp_cross_sections_all (one launch per group
+    and kernel) give each member's per-member values bit for bit."""
+    from conftest import PI2
+    shapes = [(24, 8, 9), (32, 16, 17), (24, 8, 9), (32, 16, 17), (32, 16, 17)]
+    st = nsp.Stepper([nsp.make_params(*s, 1200.0 + 100 * k, 0.005, PI2) for k, s in enumerate(shapes)])
+    for k, s in enumerate(shapes):
+        st.set_state(k, nsp.seeded_field(*s, PI2, 0.05, 90 + k))
+    st.step(3)
+    d_all = st.diag_all()
+    p_all = st.mean_profile_all()
+    q_all, u_all = st.cross_sections_all()
+    for m in range(len(shapes)):
+        d = st.diag(m)
+        for f, _ in nsp.NspDiag._fields_:
+            assert getattr(d_all[m], f) == getattr(d, f), (m, f)
+        assert np.array_equal(p_all[m], st.mean_profile(m)), m
+        q, u = st.cross_sections(m)
+        assert np.array_equal(q_all[m], q) and np.array_equal(u_all[m], u), m
+    st.close()
