@@ -946,6 +946,18 @@ int nsp_step_host(nsp_ctx* c, int nsteps, const double* in, double* out, int* it
       const int p = c->parity;
       if (first || last) {
         chunked[s] = 1;
+        // On a failure between chunks, put the control block back to its between-steps
+        // state (no held parity, every member active) before reporting it.
+        struct Restore {
+          nsp_ctx* c;
+          bool armed = true;
+          ~Restore() {
+            if (!armed) return;
+            cudaMemsetAsync(&c->dctl->hold, 0, sizeof(int), c->st);
+            cudaMemsetAsync(c->hctl.phase, 0, sizeof(int) * c->nmem, c->st);
+            cudaStreamSynchronize(c->st);
+          }
+        } restore{c};
         CK(cudaMemsetAsync(&c->dctl->hold, 1, sizeof(int), c->st));
         for (int k = 0; k < K; k++) {
           const int lo = c->chunk_lo[k], hi = c->chunk_lo[k + 1];
@@ -966,6 +978,7 @@ int nsp_step_host(nsp_ctx* c, int nsteps, const double* in, double* out, int* it
         }
         CK(cudaMemsetAsync(&c->dctl->hold, 0, sizeof(int), c->st));
         launch_finish_step(c->dctl, c->st);
+        restore.armed = false;
       } else {
         if (int rc = run_step(c)) return rc;
       }
