@@ -139,6 +139,45 @@ def run(cfg, mode, fields_dir, nsteps, snaps=None, nsteps_build=None):
     return rundir
 
 
+# ---- the reference's main.cu linked, unchanged, against the GB300 stepper's head.h shim
+
+def build_shim(cfg, nsteps, io=False):
+    """Compile main.cu (unchanged; head.h patched as for the reference builds) with
+    nspipe-gpu_gb300/headshim/nsp_headshim.cu against libnspipe_gb300.so:
+    oracle/_ref/<cfg>/shim[io]<nsteps>/Pipe.  The library must be built first."""
+    NR, NT, NZ, LZ, Re, dt = CONFIGS[cfg]
+    src = stage()
+    repo = os.path.dirname(ORACLE)
+    lib = os.path.join(repo, "nspipe-gpu_gb300")
+    out = os.path.join(REF_OUT, cfg, "shim%s%d" % ("io" if io else "", nsteps))
+    exe = os.path.join(out, "Pipe")
+    if os.path.exists(exe):
+        return exe
+    os.makedirs(out, exist_ok=True)
+    shutil.copy2(os.path.join(src, "main.cu"), os.path.join(out, "main.cu"))
+    with open(os.path.join(src, "head.h")) as fh:
+        hdr = fh.read()
+    with open(os.path.join(out, "head.h"), "w") as fh:
+        fh.write(_patch_header(hdr, NR, NT, NZ, LZ, Re, dt, nsteps, IO_SCHEDULE if io else None))
+    shim = os.path.join(lib, "headshim", "nsp_headshim.cu")
+    objs = [os.path.join(out, "main.o"), os.path.join(out, "shim.o")]
+    subprocess.run(["nvcc", "-O3", ARCH, "-I", out, "-c", os.path.join(out, "main.cu"), "-o", objs[0]], check=True)
+    subprocess.run(["nvcc", "-O3", "-std=c++17", ARCH, "-I", out, "-I", os.path.join(repo, "include"), "-c", shim,
+                    "-o", objs[1]], check=True)
+    subprocess.run(["nvcc", ARCH, "-o", exe] + objs + ["-L", lib, "-lnspipe_gb300", "-Xlinker", "-rpath=" + lib],
+                   check=True)
+    return exe
+
+
+def run_exe(exe, fields_dir, rundir):
+    """Run a build in rundir on u?_s.bin from fields_dir; returns (returncode, output)."""
+    os.makedirs(rundir, exist_ok=True)
+    for c in "rtz":
+        shutil.copy2(os.path.join(fields_dir, "u%s_s.bin" % c), os.path.join(rundir, "u%s_s.bin" % c))
+    p = subprocess.run([exe], cwd=rundir, capture_output=True, text=True)
+    return p.returncode, p.stdout + p.stderr
+
+
 # ---- the Re_Mesh tool (tools/Re_Mesh/src): mod_remesh.cu + mod_io.cu + remesh_driver.cu
 
 def stage_remesh(src=REMESH_SRC_DEFAULT):
