@@ -101,6 +101,7 @@ int nsp_save_state(nsp_ctx* ctx, int member, const char* file_r, const char* fil
  * member = NSP_ALL_MEMBERS: each pointer then holds that component of every member,
  * back to back in member order (one synchronisation for the whole ensemble). */
 #define NSP_ALL_MEMBERS (-1)
+/* Setting a member's state clears its status (NSP_ERR_NONFINITE of an earlier state). */
 int nsp_set_state_host(nsp_ctx* ctx, int member, const double* ur, const double* ut, const double* uz);
 int nsp_get_state_host(nsp_ctx* ctx, int member, double* ur, double* ut, double* uz);
 int nsp_set_state_device(nsp_ctx* ctx, int member, const void* ur, const void* ut, const void* uz);
@@ -337,6 +338,14 @@ int nsp_remesh_members(nsp_remesh* rm, nsp_ctx* src, const int* src_members, nsp
  * ut_s.bin, uz_s.bin to dir_out (mod_remesh.cu:56-58, main.cu:28-30). */
 int nsp_remesh_files(nsp_remesh* rm, const char* dir_in, const char* dir_out);
 int nsp_remesh_destroy(nsp_remesh* rm);
+
+/* Test hook for the device-side failure path (no reference counterpart).  flags bit 0:
+ * the mixed form's tensor-core transforms do not load their DFT-matrix operand, so the
+ * bounded wait for it runs out (after 4096 polls instead of the normal limit); they
+ * record a device fault, skip their tiles and return, and the next nsp_step reports
+ * NSP_ERR_DEVICE.  No fault, trap or unbounded wait is involved; the context stays
+ * usable.  0 clears. */
+int nsp_debug_inject(nsp_ctx* ctx, int flags);
 
 /* Waits for all work of the context. */
 int nsp_sync(nsp_ctx* ctx);

@@ -511,6 +511,7 @@ int nsp_create(const nsp_params* members, int n_members, int precision, int devi
     if ((rc = dalloc(c, &g.bf.H, hsz))) return rc;
     CK(cudaMemset(g.bf.U[0], 0, S3 * sizeof(double2)));
     CK(cudaMemset(g.bf.U[1], 0, S3 * sizeof(double2)));
+    CK(cudaMemset(g.bf.G, 0, gsz));
     CK(cudaMemset(g.bf.H, 0, hsz));
     CK(cudaMemset(g.bf.N, 0, S3 * sizeof(double2)));
     CK(cudaMemset(g.bf.RHSW, 0, S3 * sizeof(double2)));
@@ -718,8 +719,17 @@ static int member_run(nsp_ctx* c, int m0, int mend) {
   return n;
 }
 
+// A member whose state is set from outside starts with a clean status.
+static int clear_status(nsp_ctx* c, int m) {
+  if (m < 0) CK(cudaMemsetAsync(c->hctl.status, 0, sizeof(int) * c->nmem, c->st));
+  else CK(cudaMemsetAsync(c->hctl.status + c->internal[m], 0, sizeof(int), c->st));
+  return NSP_OK;
+}
+
 static int copy_states(nsp_ctx* c, int m, double* const* host, bool to_device) {
   const int m0 = m < 0 ? 0 : m, mend = m < 0 ? c->nmem : m + 1;
+  if (to_device)
+    if (int rc = clear_status(c, m)) return rc;
   size_t off = 0;  // doubles into each host component array
   for (int mm = m0; mm < mend;) {
     const int n = member_run(c, mm, mend);
@@ -765,6 +775,7 @@ int nsp_set_state_device(nsp_ctx* c, int m, const void* ur, const void* ut, cons
   if (!ur || !ut || !uz) return fail(c, NSP_ERR_ARG, "null state pointer");
   size_t bytes = sizeof(double2) * (size_t)c->groups[c->grp[m]].tb.S;
   const void* src[3] = {ur, ut, uz};
+  if (int rc = clear_status(c, m)) return rc;
   for (int k = 0; k < 3; k++) CK(cudaMemcpyAsync(state_ptr(c, m, k), src[k], bytes, cudaMemcpyDeviceToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
   return NSP_OK;
@@ -930,6 +941,7 @@ int nsp_step_host(nsp_ctx* c, int nsteps, const double* in, double* out, int* it
     c->ev_in.push_back(e1);
     c->ev_done.push_back(e2);
   }
+  if (int rc = clear_status(c, NSP_ALL_MEMBERS)) return rc;  // every state comes from `in`
   // Copies in may start only once earlier work on the state is done.
   CK(cudaEventRecord(c->ev_done[0], c->st));
   CK(cudaStreamWaitEvent(c->cp_in, c->ev_done[0], 0));
@@ -1421,6 +1433,13 @@ int nsp_info(nsp_ctx* c, int* n_members, int* precision) {
   if (!c) return NSP_ERR_ARG;
   if (n_members) *n_members = c->nmem;
   if (precision) *precision = c->precision;
+  return NSP_OK;
+}
+
+int nsp_debug_inject(nsp_ctx* c, int flags) {
+  if (!c) return NSP_ERR_ARG;
+  CK(cudaMemcpyAsync(&c->dctl->inject, &flags, sizeof(int), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
   return NSP_OK;
 }
 

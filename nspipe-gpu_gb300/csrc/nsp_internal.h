@@ -102,6 +102,8 @@ struct Ctl {
   int fault;           // nonzero: a device-side wait ran out and a kernel abandoned its work
   int hold;            // nonzero: a completed step keeps parity and step count (chunked
                        // steps: members advance chunk by chunk, then finish_step flips once)
+  int inject;          // test hook (nsp_debug_inject): bit 0 -- the tensor-core transforms'
+                       // operand-image barrier is never arrived on, so their bounded wait runs out
 };
 
 // Kernel launchers (nsp_transform.cu, nsp_linear.cu).

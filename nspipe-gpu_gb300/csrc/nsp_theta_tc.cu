@@ -291,11 +291,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
-  if (tid == 0) {
+  // Test hook: with bit 0 of ctl->inject the image copy is not issued, so nothing ever
+  // arrives on bar_b and the (shortened) bounded wait below runs out -- the fault path.
+  const bool inject = (ctl->inject & 1) != 0;
+  const int limit = inject ? 4096 : WAIT_LIMIT;
+  if (tid == 0 && !inject) {
     tc::mbar_arrive_expect_tx(&bar_b, 2 * B_BYTES);
     tc::bulk_g2s(sB, JOB::image(tb), 2 * B_BYTES, &bar_b);
   }
-  const bool img_ok = __syncthreads_and(tc::mbar_wait(&bar_b, 0, WAIT_LIMIT)) != 0;
+  const bool img_ok = __syncthreads_and(tc::mbar_wait(&bar_b, 0, limit)) != 0;
   const uint32_t tmem = tmem_slot;
   const int T = (JOB::columns(tb) + TM - 1) / TM;
   const int total = (src ? 1 : tb.nmem) * T;
@@ -305,7 +309,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 
   // Wait (block-uniformly) until batch b has completed.
   auto wait_batch = [&](int b) -> bool {
-    return __syncthreads_and(tc::mbar_wait(&bar_mma[b % ST], (uint32_t)((b / ST) & 1), WAIT_LIMIT)) != 0;
+    return __syncthreads_and(tc::mbar_wait(&bar_mma[b % ST], (uint32_t)((b / ST) & 1), limit)) != 0;
   };
   // This CTA's next tile at or after `from` whose member is active (uniform per CTA).
   auto next_tile = [&](int from) -> int {
@@ -362,8 +366,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   }
   // Teardown: an abandoned copy or MMA batch is given (bounded) time to land before
   // the CTA frees its TMEM and exits.
-  if (!img_ok) tc::mbar_wait(&bar_b, 0, WAIT_LIMIT);
-  if (drained < issued) tc::mbar_wait(&bar_mma[(issued - 1) % ST], (uint32_t)(((issued - 1) / ST) & 1), WAIT_LIMIT);
+  if (!img_ok && !inject) tc::mbar_wait(&bar_b, 0, limit);
+  if (drained < issued) tc::mbar_wait(&bar_mma[(issued - 1) % ST], (uint32_t)(((issued - 1) / ST) & 1), limit);
   if (fault && tid == 0) atomicOr(&ctl->fault, 1);
   tc::fence_before_sync();
   __syncthreads();

@@ -30,6 +30,7 @@ EXPORTS = [
     "nsp_run_checkpoint", "nsp_run_time", "nsp_run_close", "nsp_checkpoint_info", "nsp_output_schedule",
     "nsp_remesh_create", "nsp_remesh_matrix", "nsp_remesh_device", "nsp_remesh_members", "nsp_remesh_files",
     "nsp_remesh_destroy", "nsp_step_host", "nsp_diag_all", "nsp_mean_profile_all", "nsp_cross_sections_all",
+    "nsp_debug_inject",
 ]
 
 
@@ -122,6 +123,7 @@ def lib():
         L.nsp_remesh_members.argtypes = [vp, vp, ctypes.POINTER(ip), vp, ctypes.POINTER(ip), ip]
         L.nsp_remesh_files.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p]
         L.nsp_remesh_destroy.argtypes = [vp]
+        L.nsp_debug_inject.argtypes = [vp, ip]
         L.nsp_last_error.argtypes = [vp]
         L.nsp_last_error.restype = ctypes.c_char_p
         L.nsp_destroy.argtypes = [vp]
@@ -362,6 +364,10 @@ class Stepper:
         t = ctypes.c_double()
         self._check(lib().nsp_measure_fp64_peak(self._h, ctypes.byref(t)))
         return t.value
+
+    def debug_inject(self, flags):
+        """Test hook of the device-side failure path (nsp_debug_inject)."""
+        self._check(lib().nsp_debug_inject(self._h, flags))
 
     def sync(self):
         self._check(lib().nsp_sync(self._h))
