@@ -244,7 +244,9 @@ int nsp_info(nsp_ctx* ctx, int* n_members, int* precision);
  * directory itself, so that it is a restart directory of the reference, initField
  * mod_io_nonlinear.cu:426-429; several: in member_NNNN/) and checkpoint.json, written
  * last: the parameters, time, step and output accumulators of every member, the
- * FNV-1a 64 checksum of each state file and the size each output file had. */
+ * FNV-1a 64 checksum of each state file and the size each output file had.  Writing
+ * a checkpoint removes the directory's checkpoints of later steps (left by a run that
+ * was resumed from an earlier checkpoint). */
 typedef struct nsp_run_opts {
   const char* out_dir;  /* directory of the diagnostic files (created); NULL: no files   */
   double dt_frc;        /* interval of io_friction.txt rows              head.h:33     */

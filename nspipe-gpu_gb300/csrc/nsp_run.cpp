@@ -616,8 +616,10 @@ int write_checkpoint(nsp_run* r) {
   ok = (fclose(fh) == 0) && ok;
   if (!ok || rename(tmp.c_str(), join(dir, kSidecar).c_str()) != 0)
     return fail(r, NSP_ERR_IO, "cannot write " + join(dir, kSidecar));
-  // Keep the newest ckpt_keep complete checkpoints; drop incomplete ones older than this.
-  if (r->o.ckpt_keep > 0) {
+  // Checkpoints past this step belong to a timeline that was abandoned when the run
+  // resumed from an older one: remove them.  Then keep the newest ckpt_keep complete
+  // checkpoints and drop incomplete ones older than this.
+  {
     std::vector<std::pair<long long, bool>> found;
     if (DIR* d = opendir(r->ckpt_dir.c_str())) {
       while (dirent* e = readdir(d)) {
@@ -631,8 +633,11 @@ int write_checkpoint(nsp_run* r) {
     std::sort(found.begin(), found.end(), [](const auto& a, const auto& b) { return a.first > b.first; });
     int kept = 0;
     for (const auto& fs : found) {
-      if (fs.first > r->step) continue;
-      if (fs.second && kept < r->o.ckpt_keep) {
+      if (fs.first > r->step) {
+        remove_checkpoint_dir(join(r->ckpt_dir, step_dir_name(fs.first)));
+        continue;
+      }
+      if (fs.second && (r->o.ckpt_keep == 0 || kept < r->o.ckpt_keep)) {
         kept++;
         continue;
       }

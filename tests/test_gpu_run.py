@@ -158,6 +158,16 @@ def test_resume_rejects_other_parameters_and_corrupt_files(nsp, tmp_path):
     st.close()
     step = os.path.join(ck, "step_0000000003")
     assert sorted(os.listdir(step)) == ["checkpoint.json", "ur_s.bin", "ut_s.bin", "uz_s.bin"]
+    # resuming from an older checkpoint abandons the later ones at its first checkpoint
+    st = stepper(nsp, "s2", nsp.NSP_FP64)
+    with nsp.Run(st, out_dir=None, resume=step, ckpt_dir=ck) as run:
+        run.advance(3)
+        run.checkpoint()  # step 6
+    with nsp.Run(st, out_dir=None, resume=step, ckpt_dir=ck) as run:
+        run.advance(1)
+        run.checkpoint()  # step 4: step 6 is from the abandoned timeline
+    assert sorted(os.listdir(ck)) == ["step_0000000003", "step_0000000004"]
+    st.close()
     # a one-member checkpoint is a restart directory of the reference
     st = stepper(nsp, "s2", nsp.NSP_FP64)
     st.load(0, step)
@@ -173,6 +183,6 @@ def test_resume_rejects_other_parameters_and_corrupt_files(nsp, tmp_path):
         fh.seek(100)
         fh.write(bytes([b[0] ^ 0x40]))
     with pytest.raises(nsp.NspError) as e:
-        nsp.Run(st, out_dir=None, resume=ck)
+        nsp.Run(st, out_dir=None, resume=step)
     assert e.value.code == nsp.NSP_ERR_IO and "checksum" in str(e.value)
     st.close()
