@@ -40,6 +40,7 @@ struct Tables {
   const double* rdr;
   const double* uc;
   const double* D;     // [2][NR][7]: first derivative, parity tables (0 even-extended, 1 odd)
+  const double* Ddiv;  // D with 1/r_i added to row i's centre weight: d_r u + u / r in one stencil
   const float* D32;    // the same in FP32 (mixed-form transforms)
   const double* Lu;    // [2][NR][7]: radial Laplacian rows with identity wall row
   const double* Luc;   // (1-d_im)/(2 Re) * Lu (explicit part of the Laplacian, pre-scaled)

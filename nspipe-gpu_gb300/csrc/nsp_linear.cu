@@ -134,6 +134,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   __shared__ double2 dvs[LM];
   __shared__ unsigned long long wnum[NTH / 32], wden[NTH / 32];
   __shared__ double skt[LM], skz[LM];  // k_theta, k_z of the block's modes
+  __shared__ double snkz2[LM], snkt2[LM], shdk[LM];  // -k_z^2, -k_theta^2, -c_ex k_theta (predictor)
   __shared__ int spar[LM];             // |m| mod 2 (selects the parity tables)
   __shared__ int bad;
   // (selects instead of indexing the parameter arrays by a run-time value, which
@@ -158,9 +159,13 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   if (tid == 0) bad = 0;
   if (tid < LM) {  // wavenumbers once per block instead of per point (the FP64 pipe is the bound)
     int k = k0 + tid, it = k / NZ, l = k - it * NZ, m = it < NT / 2 ? it : it - NT;
-    skt[tid] = tb.kts * (double)m;
-    skz[tid] = tb.kzs * (double)l;
+    const double kt = tb.kts * (double)m, kz = tb.kzs * (double)l;
+    skt[tid] = kt;
+    skz[tid] = kz;
     spar[tid] = abs(m) % 2;
+    snkz2[tid] = -kz * kz;
+    snkt2[tid] = -kt * kt;
+    shdk[tid] = -(0.5 * c_ex) * (2.0 * kt);
   }
   __syncthreads();
 
@@ -189,14 +194,14 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
         for (int c = 0; c < 3; c++) R[c * LN + p] = c2(0, 0);
         continue;
       }
-      double kt = skt[mm], kz = skz[mm];
       int par_m = spar[mm];
       int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
-      double ir2 = tb.rinv2[i];
-      double base = -kz * kz - kt * kt * ir2;
-      double hs = hc * (base - ir2) + hidt;  // s/2
-      double hd = -hc * (2.0 * kt * ir2);    // d/2
-      double hz = hc * base + hidt;          // diagonal of the u_z line / 2
+      // the diagonals from the per-mode tables: 4 FP64 operations per point
+      const double ir2 = tb.rinv2[i];
+      const double base = fma(snkt2[mm], ir2, snkz2[mm]);  // -k_z^2 - k_theta^2 / r^2
+      const double hz = fma(hc, base, hidt);                // diagonal of the u_z line / 2
+      const double hs = fma(-hc, ir2, hz);                  // s/2 = hc (base - 1/r^2) + 1/(2 dt)
+      const double hd = shdk[mm] * ir2;                     // d/2 = -hc 2 k_theta / r^2
       const double* Lo = Luc + (1 - par_m) * STEN * NR + STEN * i + i0;  // u_r, u_theta (odd flag)
       const double* Le = Luc + par_m * STEN * NR + STEN * i + i0;        // u_z
       double2 lr = c2(0, 0), lt = c2(0, 0), lz = c2(0, 0);
@@ -259,7 +264,8 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       double kt = skt[mm], kz = skz[mm];
       int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
       int tab = 1 - spar[mm];
-      const double* Dr = tb.D + tab * STEN * NR + STEN * i + i0;
+      // d_r u_r + u_r / r in one stencil: Ddiv is D with 1/r_i added to the centre weight
+      const double* Dr = tb.Ddiv + tab * STEN * NR + STEN * i + i0;
       double sx = 0.0, sy = 0.0;
       for (int j = 0; j < len; j++) {
         double de = __ldg(Dr + j);
@@ -267,9 +273,8 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
         sx += de * a.x;
         sy += de * a.y;
       }
-      double ri = tb.rinv[i], kti = kt * ri;
-      double2 rr = R[p], rt = R[LN + p], rz = R[2 * LN + p];
-      sx += rr.x * ri; sy += rr.y * ri;
+      double kti = kt * tb.rinv[i];
+      double2 rt = R[LN + p], rz = R[2 * LN + p];
       sx -= kti * rt.y; sy += kti * rt.x;
       sx -= kz * rz.y; sy += kz * rz.x;
       d = c2(sx, sy);
