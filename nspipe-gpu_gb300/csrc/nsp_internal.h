@@ -154,15 +154,14 @@ void remesh_shape(const nsp_remesh* p, int* old3, int* new3);
 int remesh_device(const nsp_remesh* p);
 
 // Host-side operator construction (nsp_setup.cpp).
+// Radial tables of one shape (radial_fd) and, in a group, its first parameter set's
+// flux response (flux_response).
 struct HostOps {
   int NR;
   std::vector<double> r, rdr, D, D2, Lu, Lp, dr0;
-  std::vector<double> fac;     // [4][NR][7][NTNZ]
-  std::vector<double2> V;      // [3][NR][NTNZ]
   std::vector<double> uc;
   double Qc;
 };
-void build_operators(const nsp_params& p, HostOps& out);
 void radial_fd(int NR, HostOps& out);
 // One parameter set's mode tables on the host: fac [4][NR][NFAC][NT*NZ], V [3][NR][NT*NZ].
 void mode_tables(const nsp_params& p, const HostOps& o, double* fac, double2* V);

@@ -194,12 +194,4 @@ void flux_response(const nsp_params& p, const HostOps& o, std::vector<double>& u
   Qc = Q;
 }
 
-void build_operators(const nsp_params& p, HostOps& o) {
-  radial_fd(p.NR, o);
-  o.fac.assign((size_t)4 * p.NR * NFAC * p.NT * p.NZ, 0.0);
-  o.V.assign((size_t)3 * p.NR * p.NT * p.NZ, double2{0.0, 0.0});
-  mode_tables(p, o, o.fac.data(), o.V.data());
-  flux_response(p, o, o.uc, o.Qc);
-}
-
 }  // namespace nsp
