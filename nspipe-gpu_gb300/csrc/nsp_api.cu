@@ -924,14 +924,26 @@ int nsp_step_host(nsp_ctx* c, int nsteps, const double* in, double* out, int* it
   }
   // Member chunks (internal order), each with its own step graph: the first step copies
   // chunk k+1 in while chunk k steps, the last step copies chunk k out while chunk k+1 steps.
-  int K = nm >= 16 ? 4 : (nm >= 4 ? 2 : 1);
-  if (const char* ke = getenv("NSP_HOST_CHUNKS")) K = std::max(1, std::min(nm, atoi(ke)));  // tuning override
-  if ((int)c->chunk_lo.size() != K + 1) {
+  // Chunk weights: with 16 or more members the first and last chunks are half-size
+  // (1:2:2:2:1), so that the exposed first copy in and last copy out are short.
+  std::vector<int> wts = nm >= 16 ? std::vector<int>{1, 2, 2, 2, 1} : (nm >= 4 ? std::vector<int>{1, 1} : std::vector<int>{1});
+  if (const char* ke = getenv("NSP_HOST_CHUNKS"))  // tuning override: that many equal chunks
+    wts.assign(std::max(1, std::min(nm, atoi(ke))), 1);
+  const int K = (int)wts.size();
+  std::vector<int> lo(K + 1, 0);
+  {
+    int wsum = 0, acc = 0;
+    for (int w : wts) wsum += w;
+    for (int k = 0; k < K; k++) {
+      acc += wts[k];
+      lo[k + 1] = (int)((long long)acc * nm / wsum);
+    }
+  }
+  if (c->chunk_lo != lo) {
     for (cudaGraphExec_t x : c->chunk_exec)
       if (x) cudaGraphExecDestroy(x);
     c->chunk_exec.assign(K, nullptr);
-    c->chunk_lo.resize(K + 1);
-    for (int k = 0; k <= K; k++) c->chunk_lo[k] = (int)((long long)k * nm / K);
+    c->chunk_lo = lo;
     if (c->use_graph)
       for (int k = 0; k < K; k++)
         if (int rc = build_graph_range(c, c->chunk_lo[k], c->chunk_lo[k + 1], &c->chunk_exec[k])) return rc;
