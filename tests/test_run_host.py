@@ -141,3 +141,28 @@ def test_checkpoint_info_resolution_and_validation(nsp, tmp_path):
     d = make_checkpoint(str(tmp_path / "one"), 5)
     assert sorted(x for x in os.listdir(d) if x.endswith(".bin")) == ["ur_s.bin", "ut_s.bin", "uz_s.bin"]
     assert nsp.checkpoint_info(d)[1] == d
+
+
+@pytest.mark.parametrize("text", ['{"format": "nspipe-gb300 checkpoint", "version": 1, "members": [',
+                                  'not json at all',
+                                  '{"format": "nspipe-gb300 checkpoint", "version": "1", "members": []}',
+                                  '{"format": "nspipe-gb300 checkpoint", "version": 1, "members": [{"dir": "."}]}',
+                                  '{"format": "nspipe-gb300 checkpoint", "version": 1, "members": [{"dir": ".", '
+                                  '"state": [{"file": "ur_s.bin"}, {}, {}]}]}',
+                                  '[1, 2, 3]', ''])
+def test_checkpoint_info_rejects_malformed_sidecars(nsp, tmp_path, text):
+    d = tmp_path / "step_0000000001"
+    d.mkdir()
+    (d / "checkpoint.json").write_text(text)
+    with pytest.raises(nsp.NspError) as e:
+        nsp.checkpoint_info(str(d))
+    assert e.value.code == nsp.NSP_ERR_IO
+    assert str(d) in nsp.host_error() or "checkpoint" in nsp.host_error()
+
+
+def test_checkpoint_info_buffer_too_small(nsp, tmp_path):
+    import ctypes
+    d = make_checkpoint(str(tmp_path), 2)
+    small = ctypes.create_string_buffer(8)
+    rc = nsp.lib().nsp_checkpoint_info(d.encode(), small, len(small), None, 0)
+    assert rc == nsp.NSP_ERR_ARG
