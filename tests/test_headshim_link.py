@@ -28,3 +28,22 @@ def test_reference_main_links_against_shim(tmp_path, monkeypatch):
     monkeypatch.setattr(build_ref, "REF_SRC_DEFAULT", str(tmp_path / "absent"))
     exe = build_ref.build_shim("s2", 20)
     assert os.path.exists(exe) and os.access(exe, os.X_OK)
+
+
+def test_integration_example_compiles(tmp_path):
+    """The hand-written binding shown in INTEGRATION.md compiles against the reference's
+    head.h (its macros share the C ABI's field names; the example shows the way round)."""
+    import re
+    import subprocess
+    if not os.path.exists(os.path.join(SRC, "head.h")):
+        pytest.skip("reference sources not staged (oracle/_ref/src)")
+    if not shutil.which("nvcc"):
+        pytest.skip("nvcc not found")
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    code = [b for b in re.findall(r"```cpp\n(.*?)```", text, re.S) if "integrate_gb300(vfield u)" in b][0]
+    src = tmp_path / "example.cu"
+    src.write_text(code)
+    p = subprocess.run(["nvcc", "-std=c++17", "-gencode", "arch=compute_103a,code=sm_103a", "-I", SRC, "-I",
+                        os.path.join(ROOT, "include"), "-c", str(src), "-o", str(tmp_path / "example.o")],
+                       capture_output=True, text=True)
+    assert p.returncode == 0, p.stdout + p.stderr
