@@ -25,10 +25,12 @@
 // columns, one line per lane, so the epilogue's stores are coalesced along l.
 // Persistent CTAs (one per SM) copy the DFT image once with a bulk async copy and
 // pipeline over tiles: tile j's operands (loaded into registers during the previous
-// iteration) go to shared memory -> fence -> one thread issues 3 K/8 MMAs into TMEM
-// accumulator j % 2 and commits to an mbarrier -> tile j+1's global loads are
-// issued -> tile j-1's accumulator drains to global memory while tile j is on the
-// tensor cores and tile j+1's loads are in flight.  Every wait is bounded: a CTA whose wait runs out records a fault in the
+// iteration) go to shared memory -> fence -> one thread of warp 0 issues 3 K/8 MMAs
+// into TMEM accumulator j % 2 and commits to an mbarrier -> tile j+1's global loads
+// are issued -> warps 1-15 each wait (bounded) for tile j-1's MMAs and drain its
+// accumulator to global memory while tile j is on the tensor cores and tile j+1's
+// loads are in flight.  Warp 0 takes no part in the drain, so the serial MMA issue is
+// off the other warps' path.  Every wait is bounded: a CTA whose wait runs out records a fault in the
 // control block, waits (bounded) for its MMAs and still frees its TMEM.
 #include <algorithm>
 #include <cmath>
@@ -47,7 +49,7 @@ namespace nsp {
 namespace {
 
 constexpr int TM = 128;             // lines per tile (the MMA's M)
-constexpr int TC_THREADS = 512;     // 16 warps: fill by all, epilogue 4 lane quarters x 4 column parts
+constexpr int TC_THREADS = 512;     // 16 warps: fill by all; warp 0 issues the MMAs, warps 1-15 drain
 constexpr int WAIT_LIMIT = 1 << 22; // try_wait polls before a wait is abandoned
 
 // Issue lo*Bhi + hi*Blo + hi*Bhi over K (8 per instruction) and commit to bar.
@@ -78,6 +80,23 @@ __device__ __forceinline__ void put_split(unsigned char* ah, unsigned char* al, 
 }
 
 }  // namespace
+
+// Accumulator drain: warps 1..15 (warp 0 issues the MMAs meanwhile).  A warp may read
+// TMEM lane quarter warp % 4 only; quarter 0 has three draining warps (4, 8, 12), the
+// others four (q, q+4, q+8, q+12), and each takes a contiguous share of the N columns in
+// units of 8: [c0, c0 + nc).  False for warp 0.
+template <int N>
+__device__ __forceinline__ bool drain_share(int warp, int* q, int* c0, int* nc) {
+  if (warp == 0) return false;
+  *q = warp & 3;
+  const int P = *q == 0 ? 3 : 4, p = *q == 0 ? (warp >> 2) - 1 : (warp >> 2);
+  constexpr int U = N / 8;
+  const int u0 = p * U / P, u1 = (p + 1) * U / P;
+  *c0 = 8 * u0;
+  *nc = 8 * (u1 - u0);
+  return true;
+}
+template <int N> constexpr int drain_max() { return 8 * ((N / 8 + 2) / 3); }  // the largest share
 
 // ------------------------------------------------------------------ tile jobs
 // Inverse: line (f, level i, l) of a member, f = u_r, u_t, u_z, d_r u_r.., (i m / r) u_r..;
@@ -168,23 +187,26 @@ template <int NT, int NTP> struct InvJob {
     }
   }
 
-  // Warp w reads TMEM lanes 32 (w % 4).. (its lines) and columns [part CPP, +CPP).
+  // A draining warp reads TMEM lanes 32 q.. (its lines) and columns [c0, c0 + nc).
   __device__ static void epilogue(const Tables& tb, const Bufs& bf, const Ctl*, int mloc, int t, const double2*,
                                   double2*, uint32_t tacc) {
-    constexpr int CPP = N / 4;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int q = warp & 3, part = warp >> 2, col = q * 32 + lane;
-    float v[CPP];
+    int q, c0, nc;
+    if (!drain_share<N>(threadIdx.x >> 5, &q, &c0, &nc)) return;
+    constexpr int CM = drain_max<N>();
+    const int col = q * 32 + (threadIdx.x & 31);
+    float v[CM];
 #pragma unroll
-    for (int c8 = 0; c8 < CPP; c8 += 8) tc::tmem_ld8(tacc + ((uint32_t)(q * 32) << 16) + (uint32_t)(part * CPP + c8), v + c8);
+    for (int c8 = 0; c8 < CM; c8 += 8)
+      if (c8 < nc) tc::tmem_ld8(tacc + ((uint32_t)(q * 32) << 16) + (uint32_t)(c0 + c8), v + c8);
     tc::tmem_wait_ld();
     const int NR = tb.NR, NZ = tb.NZ, g = t * TM + col;
     if (g >= columns(tb)) return;
     const int i = g / (9 * NZ), rem = g - i * 9 * NZ, f = rem / NZ, l = rem - f * NZ;
     cpx<float>* G = reinterpret_cast<cpx<float>*>(bf.G) + (size_t)mloc * 9 * NR * NTP * NZ;
-    cpx<float>* Gl = G + (((size_t)f * NR + i) * NTP + (size_t)part * (CPP / 2)) * NZ + l;
+    cpx<float>* Gl = G + (((size_t)f * NR + i) * NTP + (size_t)(c0 / 2)) * NZ + l;
 #pragma unroll
-    for (int j = 0; j < CPP / 2; j++) Gl[(size_t)j * NZ] = mk<float>(v[2 * j], v[2 * j + 1]);
+    for (int j = 0; j < CM / 2; j++)
+      if (2 * j < nc) Gl[(size_t)j * NZ] = mk<float>(v[2 * j], v[2 * j + 1]);
   }
 };
 
@@ -231,12 +253,14 @@ template <int NT, int NTP> struct FwdJob {
 
   __device__ static void epilogue(const Tables& tb, const Bufs& bf, const Ctl* ctl, int mloc, int t,
                                   const double2* src, double2* dst, uint32_t tacc) {
-    constexpr int CPP = N / 4;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int q = warp & 3, part = warp >> 2, col = q * 32 + lane;
-    float v[CPP];
+    int q, c0, nc;
+    if (!drain_share<N>(threadIdx.x >> 5, &q, &c0, &nc)) return;
+    constexpr int CM = drain_max<N>();
+    const int col = q * 32 + (threadIdx.x & 31);
+    float v[CM];
 #pragma unroll
-    for (int c8 = 0; c8 < CPP; c8 += 8) tc::tmem_ld8(tacc + ((uint32_t)(q * 32) << 16) + (uint32_t)(part * CPP + c8), v + c8);
+    for (int c8 = 0; c8 < CM; c8 += 8)
+      if (c8 < nc) tc::tmem_ld8(tacc + ((uint32_t)(q * 32) << 16) + (uint32_t)(c0 + c8), v + c8);
     tc::tmem_wait_ld();
     const int NR = tb.NR, NZ = tb.NZ, NTNZ = tb.NTNZ, g = t * TM + col;
     const long long S = tb.S;
@@ -244,7 +268,7 @@ template <int NT, int NTP> struct FwdJob {
     const int c = g / (NR * NZ), rem = g - c * NR * NZ, i = rem / NZ, l = rem - i * NZ;
     // Wall derivative of u_z(0,0) for the mean forcing (pressGrad_k, mod_radialFD.cu:100-111).
     double dwall = 0.0;
-    if (c == 2 && l == 0 && part == 0) {
+    if (c == 2 && l == 0 && c0 == 0) {
       bool skip;
       const double2* U = member_source(tb, bf, ctl, mloc, src, skip);
       const double* Dw = tb.D + STEN * (NR - 1) + IW;
@@ -252,8 +276,9 @@ template <int NT, int NTP> struct FwdJob {
     }
     double2* Nout = (dst ? dst : bf.N + (size_t)mloc * 3 * S) + c * S + (size_t)i * NTNZ + l;
 #pragma unroll
-    for (int j = 0; j < CPP / 2; j++) {
-      const int it = part * (CPP / 2) + j;
+    for (int j = 0; j < CM / 2; j++) {
+      if (2 * j >= nc) break;
+      const int it = c0 / 2 + j;
       double2 o = make_double2(f32_to_f64(v[2 * j]), f32_to_f64(v[2 * j + 1]));  // exact, integer pipe
       if (it == NT / 2 || l == NZ - 1) o = make_double2(0.0, 0.0);  // padBackward_k's dropped modes
       if (c == 2 && it == 0 && l == 0) o.x -= tb.sscal[4 * member_set(tb, mloc) + 1] * dwall;  // 2/Re
@@ -341,16 +366,22 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // Next tile's loads now, so that they are in flight while the previous tile drains.
     const int nxt = next_tile(tile + gridDim.x);
     if (nxt < total) JOB::load(tb, bf, ctl, nxt / T, nxt % T, src, src32, rg);
-    if (j > 0) {  // drain the previous tile while this one is on the tensor cores
+    if (j > 0) {  // warps 1-15 drain the previous tile while warp 0 issues this one's MMAs
+      bool ok = true;
       if (drained < j) {
-        if (!wait_batch(j - 1)) { fault = true; break; }
+        if (warp != 0) ok = tc::mbar_wait(&bar_mma[(j - 1) % ST], (uint32_t)(((j - 1) / ST) & 1), limit);
+        if (!ok) s_fault = 1;  // made block-uniform after the barrier below
         drained = j;
       }
       tc::fence_after_sync();
-      JOB::epilogue(tb, bf, ctl, prev_m, prev_t, src, dst, tmem + (uint32_t)(((j - 1) & 1) * ACC));
+      if (ok) JOB::epilogue(tb, bf, ctl, prev_m, prev_t, src, dst, tmem + (uint32_t)(((j - 1) & 1) * ACC));
     }
     tc::fence_before_sync();
     __syncthreads();
+    if (s_fault) {
+      fault = true;
+      break;
+    }
     prev_m = mloc;
     prev_t = t;
     tile = nxt;
