@@ -60,13 +60,13 @@ __device__ __forceinline__ void issue_3xtf32(uint32_t tmem, const unsigned char*
   constexpr uint32_t ID = tc::idesc_tf32(TM, N);
   const uint32_t a_h = tc::saddr(ah), a_l = tc::saddr(al), b_h = tc::saddr(bh), b_l = tc::saddr(bl);
   tc::fence_after_sync();
-#pragma unroll 1
+#pragma unroll
   for (int s = 0; s < K / 8; s++)
     tc::mma_tf32(tmem, tc::desc(a_l + 256 * s, tc::LBO, SBO), tc::desc(b_h + 256 * s, tc::LBO, SBO), ID, s > 0);
-#pragma unroll 1
+#pragma unroll
   for (int s = 0; s < K / 8; s++)
     tc::mma_tf32(tmem, tc::desc(a_h + 256 * s, tc::LBO, SBO), tc::desc(b_l + 256 * s, tc::LBO, SBO), ID, 1);
-#pragma unroll 1
+#pragma unroll
   for (int s = 0; s < K / 8; s++)
     tc::mma_tf32(tmem, tc::desc(a_h + 256 * s, tc::LBO, SBO), tc::desc(b_h + 256 * s, tc::LBO, SBO), ID, 1);
   tc::commit(bar);
