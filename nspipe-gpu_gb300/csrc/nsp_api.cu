@@ -168,6 +168,7 @@ Tables member_view(const Group& g, int slot) {
   t.fac += (size_t)ps * 4 * t.NR * NFAC * t.NTNZ;
   t.V += (size_t)ps * 3 * t.S;
   t.Luc += (size_t)ps * 2 * STEN * t.NR;
+  t.Luc32 += (size_t)ps * 2 * STEN * t.NR;
   t.uc += (size_t)ps * t.NR;
   t.sscal += (size_t)4 * ps;
   t.nsets = 1;
@@ -589,6 +590,7 @@ int nsp_setup(nsp_ctx* c) {
     std::vector<float> D32(o.D.size());
     for (int i = 0; i < p.NR; i++) { rinv[i] = 1.0 / o.r[i]; rinv2[i] = 1.0 / (o.r[i] * o.r[i]); }
     for (size_t e = 0; e < o.D.size(); e++) D32[e] = (float)o.D[e];
+    std::vector<float> Luc32(Luc_all.begin(), Luc_all.end());
     std::vector<double> Ddiv(o.D);  // stored row i holds columns left.. at offset i0; column i is the centre
     for (int tab = 0; tab < 2; tab++)
       for (int i = 0; i < p.NR; i++) {
@@ -599,6 +601,7 @@ int nsp_setup(nsp_ctx* c) {
     if ((rc = upload(c, &tb.r, o.r)) || (rc = upload(c, &tb.rinv, rinv)) || (rc = upload(c, &tb.rinv2, rinv2)) ||
         (rc = upload(c, &tb.rdr, o.rdr)) || (rc = upload(c, &tb.uc, uc_all)) || (rc = upload(c, &tb.D, o.D)) ||
         (rc = upload(c, &tb.D32, D32)) || (rc = upload(c, &tb.Ddiv, Ddiv)) || (rc = upload(c, &tb.Lu, o.Lu)) || (rc = upload(c, &tb.Luc, Luc_all)) ||
+        (rc = upload(c, &tb.Luc32, Luc32)) ||
         (rc = upload(c, &tb.sscal, sscal)) || (rc = upload(c, &tb.mset, g.mset)))
       return rc;
     // Factors and correction profiles of every (set, mode): on the device by default,

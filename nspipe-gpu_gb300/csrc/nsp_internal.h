@@ -44,6 +44,7 @@ struct Tables {
   const float* D32;    // the same in FP32 (mixed-form transforms)
   const double* Lu;    // [2][NR][7]: radial Laplacian rows with identity wall row
   const double* Luc;   // (1-d_im)/(2 Re) * Lu (explicit part of the Laplacian, pre-scaled)
+  const float* Luc32;  // the same in FP32 (mixed form: the explicit stencil runs on the FP32 mirror)
   const double* fac;   // [4][NR][7][NTNZ]: banded LU factors of u+, u-, u_z, p
   const double2* V;    // [3][NR][NTNZ]: influence-matrix correction profiles (+, -, z)
   const double2* tw_t; // [NTP] exp(-2 pi i e/NTP), FP64

@@ -188,6 +188,9 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     // read straight from global memory (the stencil's rows are served by L1).
     // Then, at half scale: rhs = N + e, rhsw' = (1-d_im) N + e.
     const double hc = 0.5 * c_ex, hidt = 0.5 * tb.inv_dt, hw = 0.5 * tb.one_m_dim;
+    const float2* U32n = par ? bf.U32[1] : bf.U32[0];
+    const float2* Un32 = U32n ? U32n + (size_t)mloc * 3 * S : nullptr;  // mixed form: FP32 mirror of u^n
+    const float* Luc32 = tb.Luc32 + (size_t)ps * 2 * STEN * NR;
     for (int p = tid; p < LN; p += nth) {
       int i = p / LM, mm = p - i * LM, k = k0 + mm;
       if (k >= NTNZ) {
@@ -202,16 +205,34 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       const double hz = fma(hc, base, hidt);                // diagonal of the u_z line / 2
       const double hs = fma(-hc, ir2, hz);                  // s/2 = hc (base - 1/r^2) + 1/(2 dt)
       const double hd = shdk[mm] * ir2;                     // d/2 = -hc 2 k_theta / r^2
-      const double* Lo = Luc + (1 - par_m) * STEN * NR + STEN * i + i0;  // u_r, u_theta (odd flag)
-      const double* Le = Luc + par_m * STEN * NR + STEN * i + i0;        // u_z
-      double2 lr = c2(0, 0), lt = c2(0, 0), lz = c2(0, 0);
-      for (int j = 0; j < len; j++) {
-        double a = __ldg(Lo + j), b = __ldg(Le + j);
-        size_t hj = (size_t)(left + j) * NTNZ + k;
-        double2 vr = Un[hj], vt = Un[S + hj], vz = Un[2 * S + hj];
-        lr.x += a * vr.x; lr.y += a * vr.y;
-        lt.x += a * vt.x; lt.y += a * vt.y;
-        lz.x += b * vz.x; lz.y += b * vz.y;
+      const int lo = (1 - par_m) * STEN * NR + STEN * i + i0;  // u_r, u_theta rows (odd flag)
+      const int le = par_m * STEN * NR + STEN * i + i0;        // u_z rows
+      double2 lr, lt, lz;
+      if (Un32 && k != 0) {
+        // mixed form: the stencil sums in FP32 on the FP32 mirror of u^n.  The sums are
+        // (1-d_im)/Re times the radial Laplacian, a small fraction of the u^n/dt term
+        // that the diagonal below adds in FP64.  The mean mode (k = 0) stays in FP64:
+        // its Laplacian is steady, so FP32 rounding there would add up step after step.
+        float2 fr = make_float2(0.f, 0.f), ft = fr, fz = fr;
+        for (int j = 0; j < len; j++) {
+          const float a = __ldg(Luc32 + lo + j), b = __ldg(Luc32 + le + j);
+          const size_t hj = (size_t)(left + j) * NTNZ + k;
+          const float2 vr = __ldg(Un32 + hj), vt = __ldg(Un32 + S + hj), vz = __ldg(Un32 + 2 * S + hj);
+          fr.x = fmaf(a, vr.x, fr.x); fr.y = fmaf(a, vr.y, fr.y);
+          ft.x = fmaf(a, vt.x, ft.x); ft.y = fmaf(a, vt.y, ft.y);
+          fz.x = fmaf(b, vz.x, fz.x); fz.y = fmaf(b, vz.y, fz.y);
+        }
+        lr = c2(fr.x, fr.y); lt = c2(ft.x, ft.y); lz = c2(fz.x, fz.y);
+      } else {
+        lr = c2(0, 0); lt = c2(0, 0); lz = c2(0, 0);
+        for (int j = 0; j < len; j++) {
+          double a = __ldg(Luc + lo + j), b = __ldg(Luc + le + j);
+          size_t hj = (size_t)(left + j) * NTNZ + k;
+          double2 vr = Un[hj], vt = Un[S + hj], vz = Un[2 * S + hj];
+          lr.x += a * vr.x; lr.y += a * vr.y;
+          lt.x += a * vt.x; lt.y += a * vt.y;
+          lz.x += b * vz.x; lz.y += b * vz.y;
+        }
       }
       size_t h = (size_t)i * NTNZ + k;
       double2 ur = Un[h], ut = Un[S + h], uz = Un[2 * S + h];
