@@ -78,6 +78,12 @@ struct nsp_ctx {
   std::vector<cudaGraphExec_t> chunk_exec;  // step graphs of the member chunks
   std::vector<int> chunk_lo;                // their internal member bounds (K+1 values)
   long long Smax = 0;
+  // Mixed form: U32/DR32[parity] hold the FP32 mirror of U[parity] (kept current by the
+  // linear pass; cleared by every call that writes the state from outside).
+  bool mirror_ok = false;
+  // Pinned host copy of the step history, then the members' status words, then the
+  // fault flag: read back after the steps with asynchronous copies and one synchronisation.
+  int* pin = nullptr;
   std::vector<void*> allocs;
   std::string err;
 };
@@ -552,6 +558,7 @@ int nsp_create(const nsp_params* members, int n_members, int precision, int devi
   CK(cudaMemset(h.err, 0, sizeof(double) * n_members));
   if ((rc = dalloc(c, &c->dctl, sizeof(Ctl)))) return rc;
   CK(cudaMemcpy(c->dctl, &h, sizeof(Ctl), cudaMemcpyHostToDevice));
+  CK(cudaMallocHost(&c->pin, sizeof(int) * ((size_t)(h.hist_cap + 1) * n_members + 1)));
   return NSP_OK;
 }
 
@@ -737,8 +744,10 @@ static int clear_status(nsp_ctx* c, int m) {
 
 static int copy_states(nsp_ctx* c, int m, double* const* host, bool to_device) {
   const int m0 = m < 0 ? 0 : m, mend = m < 0 ? c->nmem : m + 1;
-  if (to_device)
+  if (to_device) {
+    c->mirror_ok = false;
     if (int rc = clear_status(c, m)) return rc;
+  }
   size_t off = 0;  // doubles into each host component array
   for (int mm = m0; mm < mend;) {
     const int n = member_run(c, mm, mend);
@@ -784,6 +793,7 @@ int nsp_set_state_device(nsp_ctx* c, int m, const void* ur, const void* ut, cons
   if (!ur || !ut || !uz) return fail(c, NSP_ERR_ARG, "null state pointer");
   size_t bytes = sizeof(double2) * (size_t)c->groups[c->grp[m]].tb.S;
   const void* src[3] = {ur, ut, uz};
+  c->mirror_ok = false;
   if (int rc = clear_status(c, m)) return rc;
   for (int k = 0; k < 3; k++) CK(cudaMemcpyAsync(state_ptr(c, m, k), src[k], bytes, cudaMemcpyDeviceToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
@@ -867,6 +877,35 @@ static void mirror_range(nsp_ctx* c, int lo, int hi, int par) {
   }
 }
 
+// The step history of the last `batch` steps into the pinned buffer; with `final` also
+// the members' status words and the fault flag.  One synchronisation of the stream.
+static int read_control(nsp_ctx* c, int batch, bool final) {
+  const int nm = c->nmem;
+  const size_t tail = (size_t)c->hctl.hist_cap * nm;
+  if (batch > 0)
+    CK(cudaMemcpyAsync(c->pin, c->hctl.hist, sizeof(int) * (size_t)batch * nm, cudaMemcpyDeviceToHost, c->st));
+  if (final) {
+    CK(cudaMemcpyAsync(c->pin + tail, c->hctl.status, sizeof(int) * nm, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(c->pin + tail + nm, &c->dctl->fault, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  }
+  CK(cudaStreamSynchronize(c->st));
+  return NSP_OK;
+}
+
+// After a final read_control: a device-side wait that ran out, then non-finite members.
+static int control_verdict(nsp_ctx* c) {
+  const int nm = c->nmem;
+  const int* tail = c->pin + (size_t)c->hctl.hist_cap * nm;
+  if (tail[nm]) {
+    CK(cudaMemsetAsync(&c->dctl->fault, 0, sizeof(int), c->st));
+    return fail(c, NSP_ERR_DEVICE, "a device-side wait ran out; the call's results are invalid");
+  }
+  for (int m = 0; m < nm; m++)
+    if (tail[c->internal[m]] & NSP_ERR_NONFINITE)
+      return fail(c, NSP_ERR_NONFINITE, "member %d: non-finite velocity or convergence measure", m);
+  return NSP_OK;
+}
+
 int nsp_step(nsp_ctx* c, int nsteps, int* iters_out) {
   if (!c) return NSP_ERR_ARG;
   if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_step before nsp_setup");
@@ -876,21 +915,22 @@ int nsp_step(nsp_ctx* c, int nsteps, int* iters_out) {
   const int cap = c->hctl.hist_cap;
   long long launches = 0;
   const long long per_iter = 4LL * (long long)c->groups.size() + 1;
-  std::vector<int> hist;
   // Mixed form: the transforms read an FP32 mirror of the state and its radial
-  // derivative, kept current by the linear pass; refresh them here because the
-  // state may have been set from outside.
-  if (c->precision == NSP_MIXED && nsteps > 0)
+  // derivative, kept current by the linear pass; refresh them when the state was
+  // written from outside since.
+  if (c->precision == NSP_MIXED && nsteps > 0 && !c->mirror_ok)
     for (auto& g : c->groups) launch_mirror(g.tb, g.bf.U[c->parity], g.bf.U32[c->parity], g.bf.DR32[c->parity], c->st);
+  c->mirror_ok = false;
+  if (nsteps == 0)
+    if (int rc = read_control(c, 0, true)) return rc;
   for (int done = 0; done < nsteps;) {
     int chunk = std::min(cap, nsteps - done);
     CK(cudaMemsetAsync(&c->dctl->step, 0, sizeof(int), c->st));
     for (int s = 0; s < chunk; s++)
       if (int rc = run_step(c)) return rc;
     CK(cudaGetLastError());
-    hist.resize((size_t)chunk * nm);
-    CK(cudaMemcpyAsync(hist.data(), c->hctl.hist, sizeof(int) * hist.size(), cudaMemcpyDeviceToHost, c->st));
-    CK(cudaStreamSynchronize(c->st));
+    if (int rc = read_control(c, chunk, done + chunk == nsteps)) return rc;
+    const int* hist = c->pin;
     for (int s = 0; s < chunk; s++) {
       int mx = 0;
       for (int m = 0; m < nm; m++) mx = std::max(mx, hist[(size_t)s * nm + m]);
@@ -902,13 +942,9 @@ int nsp_step(nsp_ctx* c, int nsteps, int* iters_out) {
     done += chunk;
   }
   c->launches_last = launches;
-  if (int rc = check_fault(c)) return rc;
-  std::vector<int> status(nm);
-  CK(cudaMemcpy(status.data(), c->hctl.status, sizeof(int) * nm, cudaMemcpyDeviceToHost));
-  for (int m = 0; m < nm; m++)
-    if (status[c->internal[m]] & NSP_ERR_NONFINITE)
-      return fail(c, NSP_ERR_NONFINITE, "member %d: non-finite velocity or convergence measure", m);
-  return NSP_OK;
+  const int rc = control_verdict(c);
+  c->mirror_ok = rc == NSP_OK && nsteps > 0;
+  return rc;
 }
 
 int nsp_step_host(nsp_ctx* c, int nsteps, const double* in, double* out, int* iters_out) {
@@ -919,6 +955,7 @@ int nsp_step_host(nsp_ctx* c, int nsteps, const double* in, double* out, int* it
   CK(cudaSetDevice(c->device));
   const int nm = c->nmem;
   double* hin = const_cast<double*>(in);
+  c->mirror_ok = false;
   if (nsteps == 0) {
     if (int rc = copy_chunk(c, 0, nm, c->parity, hin, true, c->st)) return rc;
     if (int rc = copy_chunk(c, 0, nm, c->parity, out, false, c->st)) return rc;
@@ -927,21 +964,36 @@ int nsp_step_host(nsp_ctx* c, int nsteps, const double* in, double* out, int* it
   }
   // Member chunks (internal order), each with its own step graph: the first step copies
   // chunk k+1 in while chunk k steps, the last step copies chunk k out while chunk k+1 steps.
-  // Chunk weights: with 16 or more members the first and last chunks are half-size
-  // (1:2:2:2:1), so that the exposed first copy in and last copy out are short.
-  std::vector<int> wts = nm >= 16 ? std::vector<int>{1, 2, 2, 2, 1} : (nm >= 4 ? std::vector<int>{1, 1} : std::vector<int>{1});
-  if (const char* ke = getenv("NSP_HOST_CHUNKS"))  // tuning override: that many equal chunks
-    wts.assign(std::max(1, std::min(nm, atoi(ke))), 1);
-  const int K = (int)wts.size();
-  std::vector<int> lo(K + 1, 0);
+  // Chunk weights: with 16 or more members 1:4:3:1 -- short first and last chunks, whose
+  // copy in and copy out are the exposed ones, and two long middle chunks (every chunk
+  // step pays its kernels' fixed costs and partial last waves once).
+  std::vector<int> wts = nm >= 16 ? std::vector<int>{1, 4, 3, 1} : (nm >= 4 ? std::vector<int>{1, 1} : std::vector<int>{1});
+  if (const char* ke = getenv("NSP_HOST_CHUNKS")) {  // tuning override: "K" equal chunks, or weights "1:3:3:1"
+    if (strchr(ke, ':')) {
+      wts.clear();
+      for (const char* q = ke; *q;) {
+        const int w = atoi(q);
+        if (w > 0 && (int)wts.size() < nm) wts.push_back(w);
+        q = strchr(q, ':');
+        if (!q) break;
+        q++;
+      }
+      if (wts.empty()) wts.assign(1, 1);
+    } else {
+      wts.assign(std::max(1, std::min(nm, atoi(ke))), 1);
+    }
+  }
+  std::vector<int> lo(1, 0);  // chunk bounds; a chunk that rounds to no member is dropped
   {
     int wsum = 0, acc = 0;
     for (int w : wts) wsum += w;
-    for (int k = 0; k < K; k++) {
-      acc += wts[k];
-      lo[k + 1] = (int)((long long)acc * nm / wsum);
+    for (int w : wts) {
+      acc += w;
+      const int b = (int)((long long)acc * nm / wsum);
+      if (b > lo.back()) lo.push_back(b);
     }
   }
+  const int K = (int)lo.size() - 1;
   if (c->chunk_lo != lo) {
     for (cudaGraphExec_t x : c->chunk_exec)
       if (x) cudaGraphExecDestroy(x);
@@ -969,7 +1021,6 @@ int nsp_step_host(nsp_ctx* c, int nsteps, const double* in, double* out, int* it
   const int cap = c->hctl.hist_cap;
   const long long per_iter = 4LL * (long long)c->groups.size() + 1;
   long long launches = 0;
-  std::vector<int> hist;
   for (int done = 0; done < nsteps;) {
     const int batch = std::min(cap, nsteps - done);
     CK(cudaMemsetAsync(&c->dctl->step, 0, sizeof(int), c->st));
@@ -1018,11 +1069,9 @@ int nsp_step_host(nsp_ctx* c, int nsteps, const double* in, double* out, int* it
       CK(cudaGetLastError());
       c->parity ^= 1;
     }
-    hist.resize((size_t)batch * nm);
-    CK(cudaMemcpyAsync(hist.data(), c->hctl.hist, sizeof(int) * hist.size(), cudaMemcpyDeviceToHost, c->st));
-    CK(cudaStreamSynchronize(c->st));
+    if (int rc = read_control(c, batch, done + batch == nsteps)) return rc;
     for (int s = 0; s < batch; s++) {
-      const int* row = hist.data() + (size_t)s * nm;
+      const int* row = c->pin + (size_t)s * nm;
       if (chunked[s]) {
         for (int k = 0; k < K; k++)
           launches += (1 + *std::max_element(row + c->chunk_lo[k], row + c->chunk_lo[k + 1])) * per_iter;
@@ -1037,13 +1086,9 @@ int nsp_step_host(nsp_ctx* c, int nsteps, const double* in, double* out, int* it
   CK(cudaStreamSynchronize(c->cp_out));
   CK(cudaStreamSynchronize(c->cp_in));
   c->launches_last = launches;
-  if (int rc = check_fault(c)) return rc;
-  std::vector<int> status(nm);
-  CK(cudaMemcpy(status.data(), c->hctl.status, sizeof(int) * nm, cudaMemcpyDeviceToHost));
-  for (int m = 0; m < nm; m++)
-    if (status[c->internal[m]] & NSP_ERR_NONFINITE)
-      return fail(c, NSP_ERR_NONFINITE, "member %d: non-finite velocity or convergence measure", m);
-  return NSP_OK;
+  const int rc = control_verdict(c);
+  c->mirror_ok = rc == NSP_OK;
+  return rc;
 }
 
 int nsp_nonlinear(nsp_ctx* c, int m, const void* ur, const void* ut, const void* uz, void* nr, void* nt, void* nz) {
@@ -1496,6 +1541,7 @@ int nsp_remesh_members(nsp_remesh* rm, nsp_ctx* src, const int* src_members, nsp
     for (int q = 0; q < count; q++)
       if (sp[k] == dp[q]) return fail(dst, NSP_ERR_ARG, "a member is both a source and a destination");
   nsp_ctx* c = dst;  // CUDA failures are reported on the destination context
+  c->mirror_ok = false;
   CK(cudaSetDevice(dst->device));
   CK(cudaStreamSynchronize(src->st));
   int rc = remesh_launch(rm, count, sp.data(), dp.data(), dst->st);
@@ -1519,6 +1565,7 @@ int nsp_destroy(nsp_ctx* c) {
   for (cudaGraphExec_t x : c->chunk_exec)
     if (x) cudaGraphExecDestroy(x);
   if (c->own_st) cudaStreamDestroy(c->own_st);
+  if (c->pin) cudaFreeHost(c->pin);
   delete c;
   return NSP_OK;
 }

@@ -643,32 +643,45 @@ __global__ void to_f32_k(const double2* __restrict__ src, float2* __restrict__ d
 }
 
 // FP32 mirror U32 and its radial derivative DR32 of a group's state (step start):
-// the same conversion and stencil as the linear pass's stages I and J.
-__global__ void mirror_k(Tables tb, const double2* __restrict__ U, float2* __restrict__ U32, float2* __restrict__ DR32) {
-  const long long total = (long long)tb.nmem * 3 * tb.S;
+// the same conversion and stencil as the linear pass's stages I and J.  A block holds
+// a tile of MR levels x MK modes of one member component (line), plus IW levels on
+// either side, converted once into shared memory; the stencil reads the tile.  Lanes
+// run along the modes (coalesced); lines are S = NR*NT*NZ < 2^31 values.
+constexpr int MIR_K = 32, MIR_R = 24, MIR_T = 256;
+__global__ void __launch_bounds__(MIR_T) mirror_k(Tables tb, const double2* __restrict__ U, float2* __restrict__ U32,
+                                                  float2* __restrict__ DR32) {
+  __shared__ float2 tile[(MIR_R + 2 * IW) * MIR_K];
   const int NR = tb.NR, NT = tb.NT, NZ = tb.NZ, NTNZ = tb.NTNZ;
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total; q += (long long)gridDim.x * blockDim.x) {
-    const long long line = q / tb.S;  // member * 3 + component
-    const long long h = q - line * tb.S;
-    const int c = (int)(line % 3), i = (int)(h / NTNZ), k = (int)(h - (long long)i * NTNZ);
-    const int it = k / NZ, m = it < NT / 2 ? it : it - NT;
-    const double2* col = U + line * tb.S + k;
-    const double2 a = col[(size_t)i * NTNZ];
-    U32[q] = make_float2(f64_to_f32(a.x), f64_to_f32(a.y));
-    const int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
-    const int tab = abs((abs(m) % 2) - (c < 2 ? 1 : 0));
-    const float* Dr = tb.D32 + tab * STEN * NR + STEN * i + i0;
-    DR32[q] = dr32_line(Dr, left, len, [&](int row) {
-      const double2 b = col[(size_t)row * NTNZ];
-      return make_float2(f64_to_f32(b.x), f64_to_f32(b.y));
-    });
+  const int kx = threadIdx.x % MIR_K, ry = threadIdx.x / MIR_K;
+  constexpr int RY = MIR_T / MIR_K;
+  const int k = blockIdx.x * MIR_K + kx, r0 = blockIdx.y * MIR_R;
+  const int lo = max(0, r0 - IW), hi = min(NR, r0 + MIR_R + IW), r1 = min(NR, r0 + MIR_R);
+  const int it = k / NZ, m = it < NT / 2 ? it : it - NT, par_m = abs(m) % 2;
+  for (int line = blockIdx.z; line < 3 * tb.nmem; line += gridDim.z) {
+    const size_t base = (size_t)line * tb.S;
+    __syncthreads();  // the previous line's tile has been read
+    if (k < NTNZ)
+      for (int r = lo + ry; r < hi; r += RY) {
+        const double2 a = U[base + (size_t)r * NTNZ + k];
+        tile[(r - lo) * MIR_K + kx] = make_float2(f64_to_f32(a.x), f64_to_f32(a.y));
+      }
+    __syncthreads();
+    if (k >= NTNZ) continue;
+    const int tab = abs(par_m - (line % 3 < 2 ? 1 : 0));
+    for (int i = r0 + ry; i < r1; i += RY) {
+      const size_t h = base + (size_t)i * NTNZ + k;
+      U32[h] = tile[(i - lo) * MIR_K + kx];
+      const int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
+      const float* Dr = tb.D32 + tab * STEN * NR + STEN * i + i0;
+      DR32[h] = dr32_line(Dr, left, len, [&](int row) { return tile[(row - lo) * MIR_K + kx]; });
+    }
   }
 }
 
 void launch_mirror(const Tables& tb, const double2* U, float2* U32, float2* DR32, cudaStream_t st) {
-  const long long n = (long long)tb.nmem * 3 * tb.S;
-  const int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
-  mirror_k<<<blocks, 256, 0, st>>>(tb, U, U32, DR32);
+  const dim3 grid((unsigned)((tb.NTNZ + MIR_K - 1) / MIR_K), (unsigned)((tb.NR + MIR_R - 1) / MIR_R),
+                  (unsigned)std::min(3 * tb.nmem, 65535));
+  mirror_k<<<grid, MIR_T, 0, st>>>(tb, U, U32, DR32);
 }
 
 void launch_to_f32(const double2* src, float2* dst, long long n, cudaStream_t st) {

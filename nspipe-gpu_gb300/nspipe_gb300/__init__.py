@@ -161,6 +161,7 @@ class Stepper:
             params = [params]
         self.params = list(params)
         self.n = len(self.params)
+        self._total = sum(p.NR * p.NT * p.NZ for p in self.params)  # values per component, all members
         arr = (NspParams * self.n)(*self.params)
         self._h = ctypes.c_void_p()
         rc = lib().nsp_create(arr, self.n, precision, device, ctypes.byref(self._h))
@@ -213,7 +214,7 @@ class Stepper:
         return u
 
     def _all_size(self):
-        return sum(int(np.prod(self.shape(m))) for m in range(self.n))
+        return self._total
 
     def set_states_all(self, u_all):
         """All members at once: u_all[c] holds component c of every member back to back."""

@@ -137,6 +137,32 @@ def test_step_host_matches_step(nsp, precision, nsteps):
     b.close()
 
 
+@pytest.mark.parametrize("name", ["s1", "s2", "c0"])
+def test_mirror_refresh_matches_linear_pass(nsp, name):
+    """Mixed form: the FP32 mirror of the state and its d_r are kept current by the
+    linear pass between steps and rebuilt by their own kernel after the state is
+    written from outside (NR = 24, 32, 48: one, two partial and two full level tiles).
+    Both must give the same bits, so stepping on and re-setting the same state before
+    the next step agree exactly."""
+    NR, NT, NZ, LZ, Re, dt, _, _ = CFG[name]
+    prm = [nsp.make_params(NR, NT, NZ, Re * (1 + 0.1 * k), dt, LZ) for k in range(3)]
+    u0 = [init(nsp, name, k) for k in range(3)]
+    a = nsp.Stepper(prm, precision=nsp.NSP_MIXED)
+    b = nsp.Stepper(prm, precision=nsp.NSP_MIXED)
+    for k in range(3):
+        a.set_state(k, u0[k])
+        b.set_state(k, u0[k])
+    a.step(3)
+    b.step(1)
+    for k in range(3):
+        b.set_state(k, b.get_state(k))
+    b.step(2)
+    for k in range(3):
+        assert np.array_equal(np.stack(a.get_state(k)), np.stack(b.get_state(k))), k
+    a.close()
+    b.close()
+
+
 def test_batched_diagnostics_equal_per_member(nsp):
     """nsp_diag_all / nsp_mean_profile_all / nsp_cross_sections_all (one launch per group
     and kernel) give each member's per-member values bit for bit."""
