@@ -866,14 +866,14 @@ static int copy_chunk(nsp_ctx* c, int lo, int hi, int par, double* host, bool to
 }
 
 // Mixed form: the FP32 mirror of the state for the members with internal index in [lo, hi).
-static void mirror_range(nsp_ctx* c, int lo, int hi, int par) {
+static void mirror_range(nsp_ctx* c, int lo, int hi, int par, cudaStream_t st) {
   for (auto& g : c->groups) {
     const int a = std::max(lo, g.tb.mem0), b = std::min(hi, g.tb.mem0 + g.tb.nmem);
     if (a >= b) continue;
     Tables t = g.tb;
     t.nmem = b - a;
     const size_t o = (size_t)(a - g.tb.mem0) * 3 * g.tb.S;
-    launch_mirror(t, g.bf.U[par] + o, g.bf.U32[par] + o, g.bf.DR32[par] + o, c->st);
+    launch_mirror(t, g.bf.U[par] + o, g.bf.U32[par] + o, g.bf.DR32[par] + o, st);
   }
 }
 
@@ -1046,10 +1046,12 @@ int nsp_step_host(nsp_ctx* c, int nsteps, const double* in, double* out, int* it
         for (int k = 0; k < K; k++) {
           const int lo = c->chunk_lo[k], hi = c->chunk_lo[k + 1];
           if (first) {
+            // The chunk's copy in and its FP32 mirror run on the copy stream, beside the
+            // previous chunk's step (other members' buffers).
             if (int rc = copy_chunk(c, lo, hi, p, hin, true, c->cp_in)) return rc;
+            if (c->precision == NSP_MIXED) mirror_range(c, lo, hi, p, c->cp_in);
             CK(cudaEventRecord(c->ev_in[k], c->cp_in));
             CK(cudaStreamWaitEvent(c->st, c->ev_in[k], 0));
-            if (c->precision == NSP_MIXED) mirror_range(c, lo, hi, p);
           }
           CK(cudaMemsetAsync(c->hctl.phase, 0xFF, sizeof(int) * nm, c->st));  // -1: sits this chunk out
           CK(cudaMemsetAsync(c->hctl.phase + lo, 0, sizeof(int) * (hi - lo), c->st));
