@@ -222,7 +222,10 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
           ft.x = fmaf(a, vt.x, ft.x); ft.y = fmaf(a, vt.y, ft.y);
           fz.x = fmaf(b, vz.x, fz.x); fz.y = fmaf(b, vz.y, fz.y);
         }
-        lr = c2(fr.x, fr.y); lt = c2(ft.x, ft.y); lz = c2(fz.x, fz.y);
+        // exact widening on the integer pipe (the hardware conversion issues on the FP64 pipe)
+        lr = c2(f32_to_f64(fr.x), f32_to_f64(fr.y));
+        lt = c2(f32_to_f64(ft.x), f32_to_f64(ft.y));
+        lz = c2(f32_to_f64(fz.x), f32_to_f64(fz.y));
       } else {
         lr = c2(0, 0); lt = c2(0, 0); lz = c2(0, 0);
         for (int j = 0; j < len; j++) {
