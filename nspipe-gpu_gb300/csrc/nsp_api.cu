@@ -597,7 +597,7 @@ int nsp_setup(nsp_ctx* c) {
     std::vector<float> D32(o.D.size());
     for (int i = 0; i < p.NR; i++) { rinv[i] = 1.0 / o.r[i]; rinv2[i] = 1.0 / (o.r[i] * o.r[i]); }
     for (size_t e = 0; e < o.D.size(); e++) D32[e] = (float)o.D[e];
-    std::vector<float> Luc32(Luc_all.begin(), Luc_all.end());
+    std::vector<float> Luc32(Luc_all.begin(), Luc_all.end()), rinv32(rinv.begin(), rinv.end());
     std::vector<double> Ddiv(o.D);  // stored row i holds columns left.. at offset i0; column i is the centre
     for (int tab = 0; tab < 2; tab++)
       for (int i = 0; i < p.NR; i++) {
@@ -607,8 +607,9 @@ int nsp_setup(nsp_ctx* c) {
     int rc;
     if ((rc = upload(c, &tb.r, o.r)) || (rc = upload(c, &tb.rinv, rinv)) || (rc = upload(c, &tb.rinv2, rinv2)) ||
         (rc = upload(c, &tb.rdr, o.rdr)) || (rc = upload(c, &tb.uc, uc_all)) || (rc = upload(c, &tb.D, o.D)) ||
-        (rc = upload(c, &tb.D32, D32)) || (rc = upload(c, &tb.Ddiv, Ddiv)) || (rc = upload(c, &tb.Lu, o.Lu)) || (rc = upload(c, &tb.Luc, Luc_all)) ||
-        (rc = upload(c, &tb.Luc32, Luc32)) ||
+        (rc = upload(c, &tb.D32, D32)) || (rc = upload(c, &tb.Ddiv, Ddiv)) ||
+        (rc = upload(c, &tb.Ddiv32, std::vector<float>(Ddiv.begin(), Ddiv.end()))) || (rc = upload(c, &tb.Lu, o.Lu)) || (rc = upload(c, &tb.Luc, Luc_all)) ||
+        (rc = upload(c, &tb.Luc32, Luc32)) || (rc = upload(c, &tb.rinv32, rinv32)) ||
         (rc = upload(c, &tb.sscal, sscal)) || (rc = upload(c, &tb.mset, g.mset)))
       return rc;
     // Factors and correction profiles of every (set, mode): on the device by default,
@@ -657,6 +658,9 @@ int nsp_setup(nsp_ctx* c) {
     tb.Qdes = p.Qdes;
     tb.Qc = sscal[2];
     tb.inv_norm = 1.0 / ((double)tb.NTP * (double)tb.NZR);
+    tb.kts32 = (float)tb.kts;
+    tb.kzs32 = (float)tb.kzs;
+    tb.inv_norm32 = (float)tb.inv_norm;
     // Mixed form: theta transforms as tensor-core DFT GEMMs where the length has a
     // compiled tile shape (NSP_THETA_TC=0 keeps the FFT kernels).
     int dev_sms = 0;
@@ -877,6 +881,13 @@ static void mirror_range(nsp_ctx* c, int lo, int hi, int par, cudaStream_t st) {
   }
 }
 
+// Kernels launched per predictor or corrector pass: per group the three transform
+// kernels and the linear pass (two kernels in the mixed form: the full pass for the
+// predictor, the increment pass for the correctors), then converge_k.
+static long long kernels_per_pass(const nsp_ctx* c) {
+  return (c->precision == NSP_MIXED ? 5LL : 4LL) * (long long)c->groups.size() + 1;
+}
+
 // The step history of the last `batch` steps into the pinned buffer; with `final` also
 // the members' status words and the fault flag.  One synchronisation of the stream.
 static int read_control(nsp_ctx* c, int batch, bool final) {
@@ -914,7 +925,7 @@ int nsp_step(nsp_ctx* c, int nsteps, int* iters_out) {
   const int nm = c->nmem;
   const int cap = c->hctl.hist_cap;
   long long launches = 0;
-  const long long per_iter = 4LL * (long long)c->groups.size() + 1;
+  const long long per_iter = kernels_per_pass(c);
   // Mixed form: the transforms read an FP32 mirror of the state and its radial
   // derivative, kept current by the linear pass; refresh them when the state was
   // written from outside since.
@@ -1019,7 +1030,7 @@ int nsp_step_host(nsp_ctx* c, int nsteps, const double* in, double* out, int* it
   CK(cudaEventRecord(c->ev_done[0], c->st));
   CK(cudaStreamWaitEvent(c->cp_in, c->ev_done[0], 0));
   const int cap = c->hctl.hist_cap;
-  const long long per_iter = 4LL * (long long)c->groups.size() + 1;
+  const long long per_iter = kernels_per_pass(c);
   long long launches = 0;
   for (int done = 0; done < nsteps;) {
     const int batch = std::min(cap, nsteps - done);

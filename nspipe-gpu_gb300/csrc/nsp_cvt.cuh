@@ -50,6 +50,19 @@ __device__ __forceinline__ double f32_to_f64(float x) {
   const uint64_t r = f32_to_f64_bits(__float_as_uint(x), fb);
   return fb ? (double)x : __longlong_as_double((long long)r);
 }
+
+// The same for arithmetic whose inputs and results below 2^-126 may be taken as zero:
+// those flush to a signed zero instead of taking the hardware conversion.
+__device__ __forceinline__ float f64_to_f32_ftz(double x) {
+  const uint32_t hi = (uint32_t)__double2hiint(x);
+  if (((hi >> 20) & 0x7FFu) < 897u) return __uint_as_float(hi & 0x80000000u);
+  return f64_to_f32(x);
+}
+__device__ __forceinline__ double f32_to_f64_ftz(float x) {
+  const uint32_t u = __float_as_uint(x);
+  if (((u >> 23) & 0xFFu) == 0u) return __longlong_as_double((long long)((uint64_t)(u & 0x80000000u) << 32));
+  return f32_to_f64(x);
+}
 #endif
 
 }  // namespace nsp

@@ -34,13 +34,18 @@ struct Tables {
   int mem0;            // global index of the group's first member
   double kts, kzs;     // 2pi/LT, 2pi/LZ (wavenumber scales, mod_deriv.cu:17,31)
   double inv_dt, c_ex, d_im, one_m_dim, two_re, Qdes, Qc, inv_norm;
+  // FP32 copies for the FP32 transform kernels (a conversion from FP64 issues on the slow
+  // FP64 pipe, so the kernels read these instead of converting per thread)
+  float kts32, kzs32, inv_norm32;
   const double* r;
   const double* rinv;
+  const float* rinv32;
   const double* rinv2;  // 1/(r*r)
   const double* rdr;
   const double* uc;
   const double* D;     // [2][NR][7]: first derivative, parity tables (0 even-extended, 1 odd)
   const double* Ddiv;  // D with 1/r_i added to row i's centre weight: d_r u + u / r in one stencil
+  const float* Ddiv32; // the same in FP32 (mixed form, corrector increment passes)
   const float* D32;    // the same in FP32 (mixed-form transforms)
   const double* Lu;    // [2][NR][7]: radial Laplacian rows with identity wall row
   const double* Luc;   // (1-d_im)/(2 Re) * Lu (explicit part of the Laplacian, pre-scaled)

@@ -114,15 +114,31 @@ __device__ __forceinline__ void solve_line(V* X, int ld, const double* __restric
   }
 }
 
+// The low half of a line slot holds an FP32 pair in the increment passes.
+__device__ __forceinline__ float2& f32slot(double2* a, int e) { return reinterpret_cast<float2*>(a)[2 * e]; }
+
 // At least 1024 threads per SM resident (4 radial lines of 48 points x 16 modes
 // is 49 KB of shared memory, so four 256-thread blocks fit): 64 registers.
-template <int LM, int NTH>
+//
+// INC (mixed form, corrector passes): the pass is affine in its right-hand side, so
+// iterate i+1 is iterate i plus the linear part of the pass applied to
+// (d_im/2) (N_i - N_{i-1}):
+//   u_{i+1} = u_i + (d_im/2) L(N_i - N_{i-1}),
+// L = divergence, pressure solve, gradient, Helmholtz solves, influence correction
+// and the flux correction without its Qdes term (equal to the full pass in exact
+// arithmetic).  The increment is small next to u, so the divergence and gradient
+// stencils run in FP32 on it; the banded solves, the influence correction and the
+// update of u stay in FP64.  N_{i-1} is kept in RHSW (the predictor stores N(u^n)
+// there in the mixed form).  Without INC the kernel is the full pass, and in the
+// mixed form it takes only the predictor.
+template <int LM, int NTH, bool INC>
 __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 : (1024 / NTH)))
     linear_k(Tables tb, Bufs bf, Ctl* ctl) {
   const int mloc = blockIdx.y, gm = tb.mem0 + mloc;
   const int ph = ctl->phase[gm];
   if (ph < 0) return;
-  const bool pred = (ph == 0);
+  if (INC ? ph == 0 : (ph > 0 && bf.U32[0] != nullptr)) return;  // the other kernel's pass
+  const bool pred = !INC && ph == 0;
   const int par = ctl->parity;
   const int NR = tb.NR, NT = tb.NT, NZ = tb.NZ, NTNZ = tb.NTNZ;
   const long long S = tb.S;
@@ -136,6 +152,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   __shared__ double skt[LM], skz[LM];  // k_theta, k_z of the block's modes
   __shared__ double snkz2[LM], snkt2[LM], shdk[LM];  // -k_z^2, -k_theta^2, -c_ex k_theta (predictor)
   __shared__ int spar[LM];             // |m| mod 2 (selects the parity tables)
+  __shared__ float skt32[LM], skz32[LM];  // k_theta, k_z in FP32 (increment passes)
   __shared__ int bad;
   // (selects instead of indexing the parameter arrays by a run-time value, which
   // would copy them to local memory)
@@ -166,6 +183,8 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     snkz2[tid] = -kz * kz;
     snkt2[tid] = -kt * kt;
     shdk[tid] = -(0.5 * c_ex) * (2.0 * kt);
+    skt32[tid] = f64_to_f32(kt);
+    skz32[tid] = f64_to_f32(kz);
   }
   __syncthreads();
 
@@ -246,9 +265,37 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       R[p] = c2(0.5 * nr.x + er.x, 0.5 * nr.y + er.y);
       R[LN + p] = c2(0.5 * nt.x + et.x, 0.5 * nt.y + et.y);
       R[2 * LN + p] = c2(0.5 * nz.x + ez.x, 0.5 * nz.y + ez.y);
-      Rw[h] = c2(hw * nr.x + er.x, hw * nr.y + er.y);
-      Rw[S + h] = c2(hw * nt.x + et.x, hw * nt.y + et.y);
-      Rw[2 * S + h] = c2(hw * nz.x + ez.x, hw * nz.y + ez.y);
+      if (Un32) {  // mixed form: N(u^n) for the first increment pass
+        Rw[h] = nr; Rw[S + h] = nt; Rw[2 * S + h] = nz;
+      } else {
+        Rw[h] = c2(hw * nr.x + er.x, hw * nr.y + er.y);
+        Rw[S + h] = c2(hw * nt.x + et.x, hw * nt.y + et.y);
+        Rw[2 * S + h] = c2(hw * nz.x + ez.x, hw * nz.y + ez.y);
+      }
+    }
+  } else if constexpr (INC) {
+    // B'. N_i - N_{i-1} in FP32 (the FP32 transforms' values are exact in FP32; the
+    // u_z line of mode (0,0) carries the FP64 wall forcing, so its difference is taken
+    // in FP64), into the FP32 halves of the line slots; RHSW takes N_i.
+    for (int p = tid; p < LN; p += nth) {
+      const int i = p / LM, mm = p - i * LM, k = k0 + mm;
+      if (k >= NTNZ) {
+        for (int c = 0; c < 3; c++) f32slot(R, c * LN + p) = make_float2(0.f, 0.f);
+        continue;
+      }
+      const size_t h = (size_t)i * NTNZ + k;
+#pragma unroll
+      for (int c = 0; c < 3; c++) {
+        const double2 n = Nn[c * S + h], q = Rw[c * S + h];
+        Rw[c * S + h] = n;
+        float2 d;
+        if (c == 2 && k == 0) {
+          d = make_float2(f64_to_f32_ftz(n.x - q.x), f64_to_f32_ftz(n.y - q.y));
+        } else {
+          d = make_float2(f64_to_f32_ftz(n.x) - f64_to_f32_ftz(q.x), f64_to_f32_ftz(n.y) - f64_to_f32_ftz(q.y));
+        }
+        f32slot(R, c * LN + p) = d;
+      }
     }
   } else {
     // A+B. rhs/2 = (d_im/2) N(u_i) + rhsw'/2, straight in r/theta form.  U points per
@@ -284,7 +331,24 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   for (int p = tid; p < LN; p += nth) {
     int i = p / LM, mm = p - i * LM, k = k0 + mm;
     double2 d = c2(0, 0);
-    if (k < NTNZ && i < NR - 1) {
+    if constexpr (INC) {  // FP32 on the increment, widened for the FP64 solve
+      if (k < NTNZ && i < NR - 1) {
+        const int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
+        const float* Dr = tb.Ddiv32 + (1 - spar[mm]) * STEN * NR + STEN * i + i0;
+        float sx = 0.f, sy = 0.f;
+        for (int j = 0; j < len; j++) {
+          const float de = __ldg(Dr + j);
+          const float2 a = f32slot(R, (left + j) * LM + mm);
+          sx = fmaf(de, a.x, sx);
+          sy = fmaf(de, a.y, sy);
+        }
+        const float kti = skt32[mm] * tb.rinv32[i], kz = skz32[mm];
+        const float2 rt = f32slot(R, LN + p), rz = f32slot(R, 2 * LN + p);
+        sx -= kti * rt.y; sy += kti * rt.x;
+        sx -= kz * rz.y; sy += kz * rz.x;
+        d = c2(f32_to_f64_ftz(sx), f32_to_f64_ftz(sy));
+      }
+    } else if (k < NTNZ && i < NR - 1) {
       double kt = skt[mm], kz = skz[mm];
       int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
       int tab = 1 - spar[mm];
@@ -316,13 +380,40 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
                  NTNZ, NR);
   }
   __syncthreads();
+  if constexpr (INC) {  // the pressure increment to FP32, in place (each slot by its own thread)
+    for (int p = tid; p < LN; p += nth) {
+      const double2 a = P[p];
+      f32slot(P, p) = make_float2(f64_to_f32_ftz(a.x), f64_to_f32_ftz(a.y));
+    }
+    __syncthreads();
+  }
 
   // E. rhs -= grad p, r/theta -> +/-, wall rows = 0.
   for (int p = tid; p < LN; p += nth) {
     int i = p / LM, mm = p - i * LM, k = k0 + mm;
     if (k >= NTNZ) continue;
     double2 up = c2(0, 0), um = c2(0, 0), rz = c2(0, 0);
-    if (i < NR - 1) {
+    if constexpr (INC) {  // FP32 on the increment; each thread reads its own slots and the P taps
+      if (i < NR - 1) {
+        const int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
+        const float* Dr = tb.D32 + spar[mm] * STEN * NR + STEN * i + i0;
+        float2 rr = f32slot(R, p);
+        for (int j = 0; j < len; j++) {
+          const float de = __ldg(Dr + j);
+          const float2 a = f32slot(P, (left + j) * LM + mm);
+          rr.x = fmaf(-de, a.x, rr.x);
+          rr.y = fmaf(-de, a.y, rr.y);
+        }
+        const float kti = skt32[mm] * tb.rinv32[i], kz = skz32[mm];
+        const float2 pp = f32slot(P, p);
+        float2 rt = f32slot(R, LN + p), fz = f32slot(R, 2 * LN + p);
+        rt.x += kti * pp.y; rt.y -= kti * pp.x;
+        fz.x += kz * pp.y; fz.y -= kz * pp.x;
+        up = c2(f32_to_f64_ftz(rr.x - rt.y), f32_to_f64_ftz(rr.y + rt.x));
+        um = c2(f32_to_f64_ftz(rr.x + rt.y), f32_to_f64_ftz(rr.y - rt.x));
+        rz = c2(f32_to_f64_ftz(fz.x), f32_to_f64_ftz(fz.y));
+      }
+    } else if (i < NR - 1) {
       double kt = skt[mm], kz = skz[mm];
       int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
       int tab = spar[mm];
@@ -407,7 +498,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   if (k0 == 0 && tid == 0) {
     double Q = 0.0;
     for (int i = 0; i < NR; i++) Q += tb.rdr[i] * R[2 * LN + i * LM].x;
-    double corr = (tb.Qdes - Q) / Qc;
+    double corr = ((INC ? 0.0 : tb.Qdes) - Q) / Qc;
     for (int i = 0; i < NR; i++) R[2 * LN + i * LM].x += corr * ucp[i];
   }
   __syncthreads();
@@ -417,6 +508,8 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   // as unsigned integers, which order like the values, and the finiteness test reads
   // the exponent field: both on the integer pipe.
   unsigned long long lnum = 0ull, lden = 0ull;
+  unsigned lnum32 = 0u, lden32 = 0u;  // increment passes: the same maxima as FP32 bits
+  const double hdi = 0.5 * tb.d_im;   // increment passes: u_{i+1} = u_i + hdi * (the pass's result)
   bool nonfin = false;
   constexpr int UI = 2;  // points per thread whose previous-iterate loads are issued together
   for (int pb = tid; pb < LN; pb += UI * nth) {
@@ -439,7 +532,14 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
 #pragma unroll
       for (int c = 0; c < 3; c++) {
         double2 v = R[c * LN + p];
-        if (!pred) {
+        if constexpr (INC) {
+          // |increment|^2 and |u_i|^2 in FP32 (the measure only decides err > tol)
+          const float fx = f64_to_f32_ftz(v.x), fy = f64_to_f32_ftz(v.y);
+          const float ox = f64_to_f32_ftz(o[u][c].x), oy = f64_to_f32_ftz(o[u][c].y);
+          lnum32 = max(lnum32, __float_as_uint(fmaf(fx, fx, fy * fy)));
+          lden32 = max(lden32, __float_as_uint(fmaf(ox, ox, oy * oy)));
+          v = c2(fma(hdi, v.x, o[u][c].x), fma(hdi, v.y, o[u][c].y));
+        } else if (!pred) {
           const double ex = o[u][c].x - v.x, ey = o[u][c].y - v.y;
           lnum = max(lnum, (unsigned long long)__double_as_longlong(ex * ex + ey * ey));
           lden = max(lden, (unsigned long long)__double_as_longlong(o[u][c].x * o[u][c].x + o[u][c].y * o[u][c].y));
@@ -456,6 +556,10 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     }
   }
   if (nonfin) bad = 1;
+  if constexpr (INC) {  // float -> double is exact and monotonic; the increment is hdi x the pass's result
+    lnum = (unsigned long long)__double_as_longlong(f32_to_f64(__uint_as_float(lnum32)) * (hdi * hdi));
+    lden = (unsigned long long)__double_as_longlong(f32_to_f64(__uint_as_float(lden32)));
+  }
   if (!pred) {
     for (int o = 16; o > 0; o >>= 1) {
       lnum = max(lnum, __shfl_xor_sync(0xffffffffu, lnum, o));
@@ -712,7 +816,9 @@ bool linear_variant_fits(int v, int NR) {
 
 void configure_linear_kernels() {
   const int big = 200 * 1024;
-#define NSP_LIN_CFG(v, lm, nth) cudaFuncSetAttribute(linear_k<lm, nth>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+#define NSP_LIN_CFG(v, lm, nth)                                                                        \
+  cudaFuncSetAttribute(linear_k<lm, nth, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big); \
+  cudaFuncSetAttribute(linear_k<lm, nth, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   NSP_LIN_SHAPES(NSP_LIN_CFG)
 #undef NSP_LIN_CFG
 }
@@ -722,9 +828,13 @@ void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st)
   const LinShape s = kLinShapes[v];
   dim3 grid((tb.NTNZ + s.LM - 1) / s.LM, tb.nmem);
   size_t smem = sizeof(double2) * 4 * (size_t)tb.NR * s.LM;
+  const bool inc = bf.U32[0] != nullptr;  // mixed form: correctors take the increment pass
   switch (v) {
-#define NSP_LIN_CASE(v, lm, nth) \
-  case v: linear_k<lm, nth><<<grid, nth, smem, st>>>(tb, bf, dctl); break;
+#define NSP_LIN_CASE(v, lm, nth)                                                         \
+  case v:                                                                               \
+    linear_k<lm, nth, false><<<grid, nth, smem, st>>>(tb, bf, dctl);                    \
+    if (inc) linear_k<lm, nth, true><<<grid, nth, smem, st>>>(tb, bf, dctl);            \
+    break;
     NSP_LIN_SHAPES(NSP_LIN_CASE)
 #undef NSP_LIN_CASE
     default: break;

@@ -19,6 +19,20 @@ __device__ __forceinline__ const double2* member_source(const Tables& tb, const 
   return (which ? bf.U[1] : bf.U[0]) + (size_t)mloc * 3 * tb.S;  // (a select keeps bf out of local memory)
 }
 
+// Scalars and 1/r of the tables in the working precision (FP32 copies for T = float).
+template <typename T> __device__ __forceinline__ T tb_kts(const Tables& tb) {
+  if constexpr (sizeof(T) == 4) return tb.kts32; else return tb.kts;
+}
+template <typename T> __device__ __forceinline__ T tb_kzs(const Tables& tb) {
+  if constexpr (sizeof(T) == 4) return tb.kzs32; else return tb.kzs;
+}
+template <typename T> __device__ __forceinline__ T tb_inv_norm(const Tables& tb) {
+  if constexpr (sizeof(T) == 4) return tb.inv_norm32; else return tb.inv_norm;
+}
+template <typename T> __device__ __forceinline__ T tb_rinv(const Tables& tb, int i) {
+  if constexpr (sizeof(T) == 4) return tb.rinv32[i]; else return tb.rinv[i];
+}
+
 // Transform input in the working precision: the FP64 state, or its FP32 mirror.
 template <typename T> struct StateIn;
 template <> struct StateIn<double> {

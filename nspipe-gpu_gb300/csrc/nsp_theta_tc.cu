@@ -161,7 +161,7 @@ template <int NT, int NTP> struct InvJob {
           }
         }
       } else {  // derivt_k (mod_deriv.cu:10-21) divided by r
-        const float ktsf = (float)tb.kts, ri = (float)tb.rinv[i];
+        const float ktsf = tb.kts32, ri = tb.rinv32[i];
 #pragma unroll
         for (int j = 0; j < J; j++) {
           const int it = mq + 4 * j, m = it < NT / 2 ? it : it - NT;

@@ -82,8 +82,8 @@ __global__ void __launch_bounds__(TTH) nl_theta_inv(Tables tb, Bufs bf, const Ct
   __syncthreads();
   const int left = max(0, i - IW), right = min(i + IW, NR - 1);
   const int len = right + 1 - left, i0 = i + IW - right;
-  const T rinv = (T)tb.rinv[i];
-  const T ktsT = (T)tb.kts;
+  const T rinv = tb_rinv<T>(tb, i);
+  const T ktsT = tb_kts<T>(tb);
   for (int idx = threadIdx.x; idx < NTP * LC; idx += TTH) {
     int p = idx / LC, lc = idx % LC;
     int f = colf[lc];
@@ -138,7 +138,7 @@ __global__ void __launch_bounds__(ZTH) nl_z(Tables tb, Bufs bf, const Ctl* ctl, 
   const int NZR = NZRC > 0 ? NZRC : tb.NZR;
   const cpx<T>* G = reinterpret_cast<const cpx<T>*>(bf.G) + (size_t)mloc * 9 * NR * NTP * NZ;
   cpx<T>* H = reinterpret_cast<cpx<T>*>(bf.H) + (size_t)mloc * 3 * NR * NTP * NZ;
-  const T kzs = (T)tb.kzs;
+  const T kzs = tb_kzs<T>(tb);
   // Hermitian-extended spectra, two real fields per complex transform.
   for (int idx = threadIdx.x; idx < RPB * 6 * NZR; idx += ZTH) {
     int q = idx % NZR, t = (idx / NZR) % 6, rr = idx / (6 * NZR);
@@ -172,7 +172,7 @@ __global__ void __launch_bounds__(ZTH) nl_z(Tables tb, Bufs bf, const Ctl* ctl, 
   else fft_batch<T, +1, MAXR, false>(Z, tb.pz, RPB * 6, 1, NZR, tw_z<T>(tb));
   // -(u.grad)u (calcNonlinear_k), packed for the forward transforms:
   // RPB 2: slot0 = (Nr0, Nt0), slot1 = (Nr1, Nt1), slot2 = (Nz0, Nz1); RPB 1: slot0 = (Nr, Nt), slot1 = (Nz, 0).
-  const T rinv = (T)tb.rinv[i];
+  const T rinv = tb_rinv<T>(tb, i);
   for (int n = threadIdx.x; n < NZR; n += ZTH) {
     T nr[RPB], nt[RPB], nz[RPB];
 #pragma unroll
@@ -313,7 +313,7 @@ __global__ void __launch_bounds__(ZTH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl,
   const int NR = tb.NR, NTP = tb.NTP;
   const cpx<T>* G = reinterpret_cast<const cpx<T>*>(bf.G) + (size_t)mloc * 9 * NR * NTP * NZ;
   cpx<T>* H = reinterpret_cast<cpx<T>*>(bf.H) + (size_t)mloc * 3 * NR * NTP * NZ;
-  const T kzs = (T)tb.kzs;
+  const T kzs = tb_kzs<T>(tb);
   const auto* twz = tw_z<T>(tb);  // exp(-2 pi i e / NZR)
   const size_t fstride = (size_t)NR * NTP * NZ;
 
@@ -364,7 +364,7 @@ __global__ void __launch_bounds__(ZTH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl,
   // 3. -(u.grad)u (calcNonlinear_k, mod_io_nonlinear.cu:142-170).  Pairs: (u_r,u_t) (u_z,dr u_r)
   // (dr u_t,dr u_z) (dt u_r,dt u_t) (dt u_z,dz u_r) (dz u_t,dz u_z).  Written back as
   // pair 0 = (N_r, N_t), pair 1 .x = N_z.
-  const T rinv = (T)tb.rinv[i];
+  const T rinv = tb_rinv<T>(tb, i);
   for (int task = threadIdx.x; task < R * NZRC; task += ZTH) {
     const int z = task % NZRC, r = task / NZRC;
     cpx<T>* p = Ph + r * 6 * PS + z;
@@ -464,7 +464,7 @@ __global__ void __launch_bounds__(TTH) nl_theta_fwd(Tables tb, Bufs bf, const Ct
     const double* Dw = tb.D + STEN * (NR - 1) + IW;
     for (int j = 0; j <= IW; j++) dwall += Dw[j] * U[2 * S + (size_t)(NR - 1 - IW + j) * NTNZ].x;
   }
-  const T scale = (T)tb.inv_norm;
+  const T scale = tb_inv_norm<T>(tb);
   for (int idx = threadIdx.x; idx < NT * LC; idx += TTH) {
     int it = idx / LC, lc = idx % LC;
     int c = colc[lc], l = coll[lc];
