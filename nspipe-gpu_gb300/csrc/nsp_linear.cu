@@ -290,9 +290,9 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
         Rw[c * S + h] = n;
         float2 d;
         if (c == 2 && k == 0) {
-          d = make_float2(f64_to_f32_ftz(n.x - q.x), f64_to_f32_ftz(n.y - q.y));
+          d = make_float2(f64_to_f32(n.x - q.x), f64_to_f32(n.y - q.y));
         } else {
-          d = make_float2(f64_to_f32_ftz(n.x) - f64_to_f32_ftz(q.x), f64_to_f32_ftz(n.y) - f64_to_f32_ftz(q.y));
+          d = make_float2(f64_to_f32(n.x) - f64_to_f32(q.x), f64_to_f32(n.y) - f64_to_f32(q.y));
         }
         f32slot(R, c * LN + p) = d;
       }
@@ -346,7 +346,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
         const float2 rt = f32slot(R, LN + p), rz = f32slot(R, 2 * LN + p);
         sx -= kti * rt.y; sy += kti * rt.x;
         sx -= kz * rz.y; sy += kz * rz.x;
-        d = c2(f32_to_f64_ftz(sx), f32_to_f64_ftz(sy));
+        d = c2(f32_to_f64(sx), f32_to_f64(sy));
       }
     } else if (k < NTNZ && i < NR - 1) {
       double kt = skt[mm], kz = skz[mm];
@@ -383,7 +383,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   if constexpr (INC) {  // the pressure increment to FP32, in place (each slot by its own thread)
     for (int p = tid; p < LN; p += nth) {
       const double2 a = P[p];
-      f32slot(P, p) = make_float2(f64_to_f32_ftz(a.x), f64_to_f32_ftz(a.y));
+      f32slot(P, p) = make_float2(f64_to_f32(a.x), f64_to_f32(a.y));
     }
     __syncthreads();
   }
@@ -409,9 +409,9 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
         float2 rt = f32slot(R, LN + p), fz = f32slot(R, 2 * LN + p);
         rt.x += kti * pp.y; rt.y -= kti * pp.x;
         fz.x += kz * pp.y; fz.y -= kz * pp.x;
-        up = c2(f32_to_f64_ftz(rr.x - rt.y), f32_to_f64_ftz(rr.y + rt.x));
-        um = c2(f32_to_f64_ftz(rr.x + rt.y), f32_to_f64_ftz(rr.y - rt.x));
-        rz = c2(f32_to_f64_ftz(fz.x), f32_to_f64_ftz(fz.y));
+        up = c2(f32_to_f64(rr.x - rt.y), f32_to_f64(rr.y + rt.x));
+        um = c2(f32_to_f64(rr.x + rt.y), f32_to_f64(rr.y - rt.x));
+        rz = c2(f32_to_f64(fz.x), f32_to_f64(fz.y));
       }
     } else if (i < NR - 1) {
       double kt = skt[mm], kz = skz[mm];
@@ -534,8 +534,8 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
         double2 v = R[c * LN + p];
         if constexpr (INC) {
           // |increment|^2 and |u_i|^2 in FP32 (the measure only decides err > tol)
-          const float fx = f64_to_f32_ftz(v.x), fy = f64_to_f32_ftz(v.y);
-          const float ox = f64_to_f32_ftz(o[u][c].x), oy = f64_to_f32_ftz(o[u][c].y);
+          const float fx = f64_to_f32(v.x), fy = f64_to_f32(v.y);
+          const float ox = f64_to_f32(o[u][c].x), oy = f64_to_f32(o[u][c].y);
           lnum32 = max(lnum32, __float_as_uint(fmaf(fx, fx, fy * fy)));
           lden32 = max(lden32, __float_as_uint(fmaf(ox, ox, oy * oy)));
           v = c2(fma(hdi, v.x, o[u][c].x), fma(hdi, v.y, o[u][c].y));
