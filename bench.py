@@ -341,7 +341,10 @@ def main():
         M * (3 * S * 16 + 9 * NR * NTP * NZ * csz),           # read u (stencil counted once), write G
         M * (9 * NR * NTP * NZ * csz + 3 * NR * NTP * (NZ - 1) * csz),  # read G, write H
         M * (3 * NR * NTP * (NZ - 1) * csz + 3 * S * 16),     # read H, write N
-        M * 15 * S * 16,                                       # corrector: read N, rhsw', u_i, V; write u_i
+        # predictor pass (the one timed): read u^n, N, V, write u_1 and RHSW (16 bytes per
+        # value, 3 components); the mixed form also reads u^n's FP32 mirror for the explicit
+        # stencil and writes the new FP32 mirror and its d_r (8 bytes per value)
+        M * S * (15 * 16 + (9 * 8 if prec == nsp.NSP_MIXED else 0)),
         M * 64,
     ]
     dom = int(np.argmax(stage_ms[:4]))
@@ -358,13 +361,14 @@ def main():
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                 "algorithmic_bytes_per_launch": alg_bytes[dom], "launch_ms": stage_ms[dom],
                 "stage_ms": dict(zip(names, [float(x) for x in stage_ms]))}
-    # The linear pass is FP64-bound on GB300 (FP64 ~1/60 of FP32): its FP64 roofline,
-    # with ~272 algorithmic FP64 flops per grid point in a corrector pass (divergence
-    # and gradient stencils, four banded solves, influence-matrix correction, +/-
-    # changes of variable, right-hand-side blend, convergence measure).
+    # The linear pass is FP64-bound on GB300 (FP64 ~1/60 of FP32): its FP64 roofline.
+    # FP64 flops per grid point of the timed predictor pass: explicit Laplacian 84 (FP32
+    # in the mixed form), coefficients 7, right-hand sides 20 + 12, step-invariant part
+    # 12 (not in the mixed form), divergence 37, pressure solve 26, gradient and +/- 41,
+    # three Helmholtz solves 78, influence correction and r/theta 30: 347, mixed 251.
     if names[dom] == "linear_k":
         fp64_peak = st.fp64_peak_tflops()
-        fl = 272.0 * S * M
+        fl = (251.0 if prec == nsp.NSP_MIXED else 347.0) * S * M
         ach = fl / (stage_ms[dom] * 1e-3) / 1e12
         roofline["compute_bound"] = "fp64"
         roofline["fp64"] = {"achieved_tflops": ach, "peak_tflops": fp64_peak, "frac": ach / fp64_peak,
