@@ -296,7 +296,7 @@ int reset_control(nsp_ctx* c) {
 }
 
 int autotune(nsp_ctx* c) {
-  for (auto& g : c->groups) g.tb.lin_variant = linear_default_variant(g.tb.NR);
+  for (auto& g : c->groups) g.tb.lin_variant = g.tb.lin_variant_inc = linear_default_variant(g.tb.NR);
   const char* ev = getenv("NSP_AUTOTUNE");
   if (ev && ev[0] == '0') return NSP_OK;
   std::map<std::string, int> cache = tune_load();
@@ -309,18 +309,24 @@ int autotune(nsp_ctx* c) {
   for (auto& g : c->groups) {
     char key[128];
     snprintf(key, sizeof key, "v2:%dx%dx%d:m%d:p%d", g.tb.NR, g.tb.NT, g.tb.NZ, g.tb.nmem, c->precision);
-    auto it = cache.find(key);
-    if (it != cache.end() && linear_variant_fits(it->second, g.tb.NR)) {
+    const std::string key_inc = std::string(key) + ":inc";
+    auto it = cache.find(key), it_inc = cache.find(key_inc);
+    const bool mixed = c->precision == NSP_MIXED;
+    if (it != cache.end() && linear_variant_fits(it->second, g.tb.NR) &&
+        (!mixed || (it_inc != cache.end() && linear_variant_fits(it_inc->second, g.tb.NR)))) {
       g.tb.lin_variant = it->second;
+      if (mixed) g.tb.lin_variant_inc = it_inc->second;
       continue;
     }
     // A step is one predictor pass (phase 0) and usually one or two corrector passes
-    // (phase 1): each candidate is scored by predictor + corrector time.
-    float best = 1e30f;
+    // (phase 1): in the FP64 form one kernel takes both and each candidate is scored by
+    // predictor + corrector time; in the mixed form the corrector is its own kernel
+    // (the increment pass) and the two passes are tuned separately.
+    float best = 1e30f, best_p[2] = {1e30f, 1e30f};
     for (int v = 0; v < LIN_VARIANTS; v++) {
       if (!linear_variant_fits(v, g.tb.NR)) continue;
       Tables tv = g.tb;
-      tv.lin_variant = v;
+      tv.lin_variant = tv.lin_variant_inc = v;
       float score = 0.f;
       for (int phase = 0; phase < 2; phase++) {
         const std::vector<int>& ph = phase ? ones : zeros;
@@ -337,11 +343,16 @@ int autotune(nsp_ctx* c) {
           t = std::min(t, ms);
         }
         score += t;
+        if (mixed && t < best_p[phase]) {
+          best_p[phase] = t;
+          (phase ? g.tb.lin_variant_inc : g.tb.lin_variant) = v;
+        }
       }
       CK(cudaGetLastError());
-      if (score < best) { best = score; g.tb.lin_variant = v; }
+      if (!mixed && score < best) { best = score; g.tb.lin_variant = v; }
     }
     cache[key] = g.tb.lin_variant;
+    if (mixed) cache[key_inc] = g.tb.lin_variant_inc;
     dirty = true;
   }
   cudaEventDestroy(e0);
@@ -1402,13 +1413,17 @@ int nsp_describe(nsp_ctx* c, char* buf, int cap) {
   for (size_t k = 0; k < c->groups.size(); k++) {
     const Tables& tb = c->groups[k].tb;
     int v = linear_variant_fits(tb.lin_variant, tb.NR) ? tb.lin_variant : linear_default_variant(tb.NR);
-    int LM = 0, NTH = 0;
+    int vi = linear_variant_fits(tb.lin_variant_inc, tb.NR) ? tb.lin_variant_inc : linear_default_variant(tb.NR);
+    int LM = 0, NTH = 0, LMi = 0, NTHi = 0;
     linear_shape(v, &LM, &NTH);
-    char g[384];
+    linear_shape(vi, &LMi, &NTHi);
+    char inc[64] = "";
+    if (c->precision == NSP_MIXED) snprintf(inc, sizeof inc, ", \"linear_block_corrector\": [%d, %d]", LMi, NTHi);
+    char g[448];
     snprintf(g, sizeof(g),
-             "%s{\"shape\": [%d, %d, %d], \"members\": %d, \"parameter_sets\": %d, \"linear_block\": [%d, %d], "
+             "%s{\"shape\": [%d, %d, %d], \"members\": %d, \"parameter_sets\": %d, \"linear_block\": [%d, %d]%s, "
              "\"theta\": \"%s\", \"setup\": \"%s\"}",
-             k ? ", " : "", tb.NR, tb.NT, tb.NZ, tb.nmem, tb.nsets, LM, NTH,
+             k ? ", " : "", tb.NR, tb.NT, tb.NZ, tb.nmem, tb.nsets, LM, NTH, inc,
              c->precision != NSP_MIXED ? "fft-fp64" : (tb.tc_theta ? "tcgen05-3xtf32" : "fft-fp32"),
              c->groups[k].device_setup ? "device" : "host");
     s += g;

@@ -58,6 +58,7 @@ struct Tables {
   const float2* tw_z32;
   FftPlan pt, pz;
   int lin_variant;     // block shape of the linear pass (autotuned at setup)
+  int lin_variant_inc; // mixed form: block shape of the increment (corrector) pass
   int nsets;           // operator parameter sets (distinct Re) of the group
   const int* mset;     // [nmem] parameter set of each member
   const double* sscal; // [nsets][4]: (1-d_im)/Re, 2/Re, Qc, Re

@@ -824,20 +824,24 @@ void configure_linear_kernels() {
 }
 
 void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st) {
-  int v = linear_variant_fits(tb.lin_variant, tb.NR) ? tb.lin_variant : linear_default_variant(tb.NR);
-  const LinShape s = kLinShapes[v];
-  dim3 grid((tb.NTNZ + s.LM - 1) / s.LM, tb.nmem);
-  size_t smem = sizeof(double2) * 4 * (size_t)tb.NR * s.LM;
-  const bool inc = bf.U32[0] != nullptr;  // mixed form: correctors take the increment pass
-  switch (v) {
-#define NSP_LIN_CASE(v, lm, nth)                                                         \
-  case v:                                                                               \
-    linear_k<lm, nth, false><<<grid, nth, smem, st>>>(tb, bf, dctl);                    \
-    if (inc) linear_k<lm, nth, true><<<grid, nth, smem, st>>>(tb, bf, dctl);            \
+  // The full pass, then in the mixed form the increment pass (correctors), each with
+  // its own block shape; each returns at once in the other's passes.
+  for (int pass = 0; pass < (bf.U32[0] != nullptr ? 2 : 1); pass++) {
+    const int want = pass ? tb.lin_variant_inc : tb.lin_variant;
+    const int v = linear_variant_fits(want, tb.NR) ? want : linear_default_variant(tb.NR);
+    const LinShape s = kLinShapes[v];
+    const dim3 grid((tb.NTNZ + s.LM - 1) / s.LM, tb.nmem);
+    const size_t smem = sizeof(double2) * 4 * (size_t)tb.NR * s.LM;
+    switch (v) {
+#define NSP_LIN_CASE(v, lm, nth)                                                          \
+  case v:                                                                                \
+    if (pass) linear_k<lm, nth, true><<<grid, nth, smem, st>>>(tb, bf, dctl);            \
+    else linear_k<lm, nth, false><<<grid, nth, smem, st>>>(tb, bf, dctl);                \
     break;
-    NSP_LIN_SHAPES(NSP_LIN_CASE)
+      NSP_LIN_SHAPES(NSP_LIN_CASE)
 #undef NSP_LIN_CASE
-    default: break;
+      default: break;
+    }
   }
 }
 
