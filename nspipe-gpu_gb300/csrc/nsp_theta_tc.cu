@@ -72,11 +72,16 @@ __device__ __forceinline__ void issue_3xtf32(uint32_t tmem, const unsigned char*
   tc::commit(bar);
 }
 
-__device__ __forceinline__ void put_split(unsigned char* ah, unsigned char* al, uint32_t off, float x) {
-  float h, l;
-  tc::split_tf32(x, h, l);
-  *reinterpret_cast<float*>(ah + off) = h;
-  *reinterpret_cast<float*>(al + off) = l;
+// Four consecutive K entries of one operand row (16 bytes at a 16-byte aligned core
+// matrix offset): their TF32 hi and lo parts as two vector stores.
+__device__ __forceinline__ void put_split4(unsigned char* ah, unsigned char* al, uint32_t off, const float* x) {
+  float4 h, l;
+  tc::split_tf32(x[0], h.x, l.x);
+  tc::split_tf32(x[1], h.y, l.y);
+  tc::split_tf32(x[2], h.z, l.z);
+  tc::split_tf32(x[3], h.w, l.w);
+  *reinterpret_cast<float4*>(ah + off) = h;
+  *reinterpret_cast<float4*>(al + off) = l;
 }
 
 }  // namespace
@@ -104,13 +109,17 @@ template <int N> constexpr int drain_max() { return 8 * ((N / 8 + 2) / 3); }  //
 template <int NT, int NTP> struct InvJob {
   static constexpr int K = 2 * NT, N = 2 * NTP, STAGES = 2;
   static constexpr int J = NT / 4;  // modes per thread in the fill
+  static_assert(NT % 16 == 0, "the fill takes blocks of 4 modes, 4 blocks per round");
   __device__ static int columns(const Tables& tb) { return 9 * tb.NR * tb.NZ; }
   __device__ static const float* image(const Tables& tb) { return tb.dft_inv; }
 
-  // Warp w fills lines 8w..8w+7; lane = line (lane % 8) x mode quarter (lane / 8), so
-  // a warp's 32 stores of one K index hit 32 different banks.  Every load of a
+  // Warp w fills lines 8w..8w+7; lane = line (lane % 8) x mode quarter (lane / 8); a
+  // thread takes the blocks of 4 consecutive modes q, q+4, ... (q = its quarter), so
+  // that each block is one 16-byte row of a core matrix (vector stores; a warp's
+  // stores of one block cover 4 core matrices, conflict-free).  Every load of a
   // thread is independent of the others (one line, J modes, up to 7 levels).
   struct Regs { float vx[J], vy[J]; };  // one thread's share of a tile (line col, J modes)
+  __device__ static int mode_of(int mq, int j) { return 4 * (mq + 4 * (j / 4)) + (j % 4); }
 
   // Global -> registers; the loop issues this for the next tile before draining the
   // previous one, so the loads are in flight during the epilogue.
@@ -134,27 +143,29 @@ template <int NT, int NTP> struct InvJob {
       if (f >= 3 && f < 6 && DR) {  // d_r u from the mirror the linear pass wrote
 #pragma unroll
         for (int j = 0; j < J; j++) {
-          const float2 a = __ldg(DR + (size_t)i * NTNZ + base + (size_t)(mq + 4 * j) * NZ);
+          const float2 a = __ldg(DR + (size_t)i * NTNZ + base + (size_t)mode_of(mq, j) * NZ);
           vx[j] = a.x; vy[j] = a.y;
         }
       } else if (f < 3) {
 #pragma unroll
         for (int j = 0; j < J; j++) {
-          cpx<float> a = U.ld((size_t)i * NTNZ + base + (size_t)(mq + 4 * j) * NZ);
+          cpx<float> a = U.ld((size_t)i * NTNZ + base + (size_t)mode_of(mq, j) * NZ);
           vx[j] = a.x; vy[j] = a.y;
         }
-      } else if (f < 6) {  // derivr_k (mod_radialFD.cu:10-30); |m| mod 2 = it mod 2 = mq mod 2 here
+      } else if (f < 6) {  // derivr_k (mod_radialFD.cu:10-30); |m| mod 2 = it mod 2 = j mod 2 here
         const int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
-        const int tab = abs((mq & 1) - (comp < 2 ? 1 : 0));
-        const float* Dr = tb.D32 + tab * STEN * NR + STEN * i + i0;
+        const int odd = comp < 2 ? 1 : 0;  // u_r, u_theta take the odd table for even |m|
+        const float* Dr0 = tb.D32 + abs(0 - odd) * STEN * NR + STEN * i + i0;  // even |m|
+        const float* Dr1 = tb.D32 + abs(1 - odd) * STEN * NR + STEN * i + i0;  // odd |m|
 #pragma unroll
         for (int r = 0; r < STEN; r++) {
           if (r < len) {
-            const float de = __ldg(Dr + r);
+            const float de0 = __ldg(Dr0 + r), de1 = __ldg(Dr1 + r);
             const size_t row = (size_t)(left + r) * NTNZ + base;
 #pragma unroll
             for (int j = 0; j < J; j++) {
-              cpx<float> a = U.ld(row + (size_t)(mq + 4 * j) * NZ);
+              const float de = (j & 1) ? de1 : de0;
+              cpx<float> a = U.ld(row + (size_t)mode_of(mq, j) * NZ);
               vx[j] += de * a.x;
               vy[j] += de * a.y;
             }
@@ -164,7 +175,7 @@ template <int NT, int NTP> struct InvJob {
         const float ktsf = tb.kts32, ri = tb.rinv32[i];
 #pragma unroll
         for (int j = 0; j < J; j++) {
-          const int it = mq + 4 * j, m = it < NT / 2 ? it : it - NT;
+          const int it = mode_of(mq, j), m = it < NT / 2 ? it : it - NT;
           const float kt = (float)m * ktsf;
           cpx<float> a = U.ld((size_t)i * NTNZ + base + (size_t)it * NZ);
           vx[j] = -kt * a.y * ri;
@@ -180,10 +191,10 @@ template <int NT, int NTP> struct InvJob {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int col = warp * 8 + (lane & 7), mq = lane >> 3;
 #pragma unroll
-    for (int j = 0; j < J; j++) {
-      const int it = mq + 4 * j;
-      put_split(ah, al, tc::koff(col, it, SBO), rg.vx[j]);
-      put_split(ah, al, tc::koff(col, NT + it, SBO), rg.vy[j]);
+    for (int j = 0; j < J; j += 4) {
+      const int it = mode_of(mq, j);  // first of 4 consecutive modes
+      put_split4(ah, al, tc::koff(col, it, SBO), rg.vx + j);
+      put_split4(ah, al, tc::koff(col, NT + it, SBO), rg.vy + j);
     }
   }
 
@@ -215,10 +226,13 @@ template <int NT, int NTP> struct InvJob {
 template <int NT, int NTP> struct FwdJob {
   static constexpr int K = 2 * NTP, N = 2 * NT, STAGES = 1;
   static constexpr int J = NTP / 4;
+  static_assert(NTP % 16 == 0, "the fill takes blocks of 4 points, 4 blocks per round");
   __device__ static int columns(const Tables& tb) { return 3 * tb.NR * tb.NZ; }
   __device__ static const float* image(const Tables& tb) { return tb.dft_fwd; }
 
   struct Regs { cpx<float> h[J]; };
+  // blocks of 4 consecutive points per thread, as the inverse's modes
+  __device__ static int point_of(int pq, int j) { return 4 * (pq + 4 * (j / 4)) + (j % 4); }
 
   __device__ static void load(const Tables& tb, const Bufs& bf, const Ctl*, int mloc, int t, const double2*,
                               const float2*, Regs& rg) {
@@ -234,7 +248,7 @@ template <int NT, int NTP> struct FwdJob {
         const cpx<float>* H = reinterpret_cast<const cpx<float>*>(bf.H) + (size_t)mloc * 3 * NR * NTP * NZ +
                               ((size_t)c * NR + i) * NTP * NZ + l;
 #pragma unroll
-        for (int j = 0; j < J; j++) h[j] = H[(size_t)(pq + 4 * j) * NZ];
+        for (int j = 0; j < J; j++) h[j] = H[(size_t)point_of(pq, j) * NZ];
       }
     }
   }
@@ -244,10 +258,12 @@ template <int NT, int NTP> struct FwdJob {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int col = warp * 8 + (lane & 7), pq = lane >> 3;
 #pragma unroll
-    for (int j = 0; j < J; j++) {
-      const int p = pq + 4 * j;
-      put_split(ah, al, tc::koff(col, p, SBO), rg.h[j].x);
-      put_split(ah, al, tc::koff(col, NTP + p, SBO), rg.h[j].y);
+    for (int j = 0; j < J; j += 4) {
+      const int p = point_of(pq, j);  // first of 4 consecutive points
+      const float re[4] = {rg.h[j].x, rg.h[j + 1].x, rg.h[j + 2].x, rg.h[j + 3].x};
+      const float im[4] = {rg.h[j].y, rg.h[j + 1].y, rg.h[j + 2].y, rg.h[j + 3].y};
+      put_split4(ah, al, tc::koff(col, p, SBO), re);
+      put_split4(ah, al, tc::koff(col, NTP + p, SBO), im);
     }
   }
 
