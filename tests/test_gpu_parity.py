@@ -117,6 +117,26 @@ def test_mixed_steps_close_to_fp64(nsp, orc):
     st.close()
 
 
+def test_mixed_increment_correctors_follow_fp64(nsp):
+    """The mixed form's correctors advance by increments (d_im/2) L(N_i - N_{i-1}), with
+    the previous pass's N kept between passes.  With tol = 1e-14 every step takes
+    several corrector passes, so the chain of increments runs past the first
+    corrector; the states and iteration counts follow the FP64 form's full passes."""
+    NR, NT, NZ, LZ, Re, dt, _, _ = CFG["c0"]
+    res, its = {}, {}
+    for prec in (nsp.NSP_FP64, nsp.NSP_MIXED):
+        st = nsp.Stepper([nsp.make_params(NR, NT, NZ, Re, dt, LZ, tol=1e-14) for _ in range(2)], precision=prec)
+        for m in range(2):
+            st.set_state(m, init(nsp, "c0", m))
+        its[prec] = st.step(20)
+        res[prec] = [np.stack(st.get_state(m)) for m in range(2)]
+        st.close()
+    assert its[nsp.NSP_FP64].min() >= 2, its[nsp.NSP_FP64]
+    assert np.array_equal(its[nsp.NSP_MIXED], its[nsp.NSP_FP64]), (its[nsp.NSP_MIXED], its[nsp.NSP_FP64])
+    for m in range(2):
+        assert rel(res[nsp.NSP_MIXED][m], res[nsp.NSP_FP64][m]) < 1e-6
+
+
 def test_ensemble_members_independent(nsp):
     """A batched context gives each member the result of a single-member context."""
     name, M, nsteps = "s2", 5, 3
