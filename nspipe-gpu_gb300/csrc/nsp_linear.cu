@@ -277,24 +277,38 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     // B'. N_i - N_{i-1} in FP32 (the FP32 transforms' values are exact in FP32; the
     // u_z line of mode (0,0) carries the FP64 wall forcing, so its difference is taken
     // in FP64), into the FP32 halves of the line slots; RHSW takes N_i.
-    for (int p = tid; p < LN; p += nth) {
-      const int i = p / LM, mm = p - i * LM, k = k0 + mm;
-      if (k >= NTNZ) {
-        for (int c = 0; c < 3; c++) f32slot(R, c * LN + p) = make_float2(0.f, 0.f);
-        continue;
-      }
-      const size_t h = (size_t)i * NTNZ + k;
+    constexpr int UB = 2;  // points per thread whose loads are issued together (RHSW is also stored)
+    for (int pb = tid; pb < LN; pb += UB * nth) {
+      double2 n[UB][3], q[UB][3];
 #pragma unroll
-      for (int c = 0; c < 3; c++) {
-        const double2 n = Nn[c * S + h], q = Rw[c * S + h];
-        Rw[c * S + h] = n;
-        float2 d;
-        if (c == 2 && k == 0) {
-          d = make_float2(f64_to_f32(n.x - q.x), f64_to_f32(n.y - q.y));
-        } else {
-          d = make_float2(f64_to_f32(n.x) - f64_to_f32(q.x), f64_to_f32(n.y) - f64_to_f32(q.y));
+      for (int u = 0; u < UB; u++) {
+        const int p = pb + u * nth, i = p / LM, k = k0 + p - i * LM;
+        const bool ok = p < LN && k < NTNZ;
+        const size_t h = ok ? (size_t)i * NTNZ + k : 0;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          n[u][c] = ok ? Nn[c * S + h] : c2(0, 0);
+          q[u][c] = ok ? Rw[c * S + h] : c2(0, 0);
         }
-        f32slot(R, c * LN + p) = d;
+      }
+#pragma unroll
+      for (int u = 0; u < UB; u++) {
+        const int p = pb + u * nth, i = p / LM, k = k0 + p - i * LM;
+        if (p >= LN) continue;
+        const bool ok = k < NTNZ;
+        const size_t h = (size_t)i * NTNZ + k;
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          if (ok) Rw[c * S + h] = n[u][c];
+          float2 d;
+          if (c == 2 && k == 0) {
+            d = make_float2(f64_to_f32(n[u][c].x - q[u][c].x), f64_to_f32(n[u][c].y - q[u][c].y));
+          } else {
+            d = make_float2(f64_to_f32(n[u][c].x) - f64_to_f32(q[u][c].x),
+                            f64_to_f32(n[u][c].y) - f64_to_f32(q[u][c].y));
+          }
+          f32slot(R, c * LN + p) = d;  // zero where k >= NTNZ
+        }
       }
     }
   } else {
