@@ -40,6 +40,7 @@ constexpr int MAXR = 4;   // register rounds of the run-time FFT
 constexpr int LC = 16;    // theta columns per block
 constexpr int TTH = 256;  // threads of the theta kernels
 constexpr int ZTH = 256;  // threads of the z kernel
+constexpr int Z2TH = 192; // threads of the two-pass z kernel (its passes run 192, 144, 384, 48, 36, 384 tasks)
 
 template <typename T> __device__ __forceinline__ const typename vec2<T>::type* tw_t(const Tables& tb);
 template <> __device__ __forceinline__ const double2* tw_t<double>(const Tables& tb) { return tb.tw_t; }
@@ -297,7 +298,7 @@ __device__ __forceinline__ cpx<T> z_pair_spec_in(const cpx<T>* Ga, const cpx<T>*
 }
 
 template <typename T, int NZRC, int N1, int N2, int R>
-__global__ void __launch_bounds__(ZTH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl, int standalone) {
+__global__ void __launch_bounds__(Z2TH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl, int standalone) {
   static_assert(N1 * N2 == NZRC && R % 2 == 0 && NZRC % 3 == 0, "z split");
   constexpr int NZ = NZRC / 3 + 1;    // NZR = 3 (NZ - 1) (3/2 rule)
   constexpr int NQ = NZ - 1;          // retained z modes of the output
@@ -318,7 +319,7 @@ __global__ void __launch_bounds__(ZTH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl,
   const size_t fstride = (size_t)NR * NTP * NZ;
 
   // 1. inverse, pass A (spectra gathered from G)
-  for (int task = threadIdx.x; task < R * 6 * N1; task += ZTH) {
+  for (int task = threadIdx.x; task < R * 6 * N1; task += Z2TH) {
     const int n1 = task % N1, t = (task / N1) % 6, r = task / (6 * N1);
     const cpx<T>* Gi = G + ((size_t)i * NTP + j0 + r) * NZ;
     const int fa = 2 * t, fb = 2 * t + 1;  // d_z u_c (fields 9-11) comes from the u_c columns
@@ -349,7 +350,7 @@ __global__ void __launch_bounds__(ZTH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl,
   }
   __syncthreads();
   // 2. inverse, pass B -> physical point z = N2 k1 + k2 of the pair (2t, 2t+1)
-  for (int task = threadIdx.x; task < R * 6 * N2; task += ZTH) {
+  for (int task = threadIdx.x; task < R * 6 * N2; task += Z2TH) {
     const int k2 = task % N2, t = (task / N2) % 6, r = task / (6 * N2);
     cpx<T> y[N1];
     const cpx<T>* Yt = Y + (r * 6 + t) * YT + k2 * YP;
@@ -365,7 +366,7 @@ __global__ void __launch_bounds__(ZTH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl,
   // (dr u_t,dr u_z) (dt u_r,dt u_t) (dt u_z,dz u_r) (dz u_t,dz u_z).  Written back as
   // pair 0 = (N_r, N_t), pair 1 .x = N_z.
   const T rinv = tb_rinv<T>(tb, i);
-  for (int task = threadIdx.x; task < R * NZRC; task += ZTH) {
+  for (int task = threadIdx.x; task < R * NZRC; task += Z2TH) {
     const int z = task % NZRC, r = task / NZRC;
     cpx<T>* p = Ph + r * 6 * PS + z;
     const cpx<T> a0 = p[0], a1 = p[PS], a2 = p[2 * PS], a3 = p[3 * PS], a4 = p[4 * PS], a5 = p[5 * PS];
@@ -377,7 +378,7 @@ __global__ void __launch_bounds__(ZTH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl,
   }
   __syncthreads();
   // 4. forward, pass A: transform t < R is (N_r, N_t) of row t; t >= R packs N_z of rows 2(t-R), 2(t-R)+1.
-  for (int task = threadIdx.x; task < NF * N1; task += ZTH) {
+  for (int task = threadIdx.x; task < NF * N1; task += Z2TH) {
     const int n1 = task % N1, t = task / N1;
     cpx<T> x[N2];
     if (t < R) {
@@ -405,7 +406,7 @@ __global__ void __launch_bounds__(ZTH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl,
   __syncthreads();
   // 5. forward, pass B -> spectrum X[N2 k1 + k2] (natural order, over the physical buffer)
   cpx<T>* Xs = Ph;
-  for (int task = threadIdx.x; task < NF * N2; task += ZTH) {
+  for (int task = threadIdx.x; task < NF * N2; task += Z2TH) {
     const int k2 = task % N2, t = task / N2;
     cpx<T> y[N1];
     const cpx<T>* Yt = Y + t * YT + k2 * YP;
@@ -417,7 +418,7 @@ __global__ void __launch_bounds__(ZTH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl,
   }
   __syncthreads();
   // 6. unpack x = a + i b: A_q = (X_q + conj X_-q)/2, B_q = (X_q - conj X_-q)/(2i); keep q < NZ-1.
-  for (int task = threadIdx.x; task < R * 3 * NQ; task += ZTH) {
+  for (int task = threadIdx.x; task < R * 3 * NQ; task += Z2TH) {
     const int q = task % NQ, c = (task / NQ) % 3, r = task / (3 * NQ), j = j0 + r;
     const int slot = c < 2 ? r : R + r / 2;
     const bool takeB = c < 2 ? (c == 1) : (r & 1);
@@ -512,7 +513,7 @@ static constexpr size_t z2_smem() {
 template <typename T, int NZRC, int N1, int N2, int R>
 static void launch_z2(const Tables& tb, const Bufs& bf, Ctl* dctl, bool standalone, cudaStream_t st, int nm) {
   dim3 g((tb.NTP + R - 1) / R, tb.NR, nm);
-  nl_z2<T, NZRC, N1, N2, R><<<g, ZTH, z2_smem<T, NZRC, N1, N2, R>(), st>>>(tb, bf, dctl, standalone ? 1 : 0);
+  nl_z2<T, NZRC, N1, N2, R><<<g, Z2TH, z2_smem<T, NZRC, N1, N2, R>(), st>>>(tb, bf, dctl, standalone ? 1 : 0);
 }
 
 #define NSP_NTP_LIST(X) X(12) X(24) X(48) X(72) X(96) X(144) X(192)
