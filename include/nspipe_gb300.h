@@ -188,8 +188,9 @@ long long nsp_kernel_launches(nsp_ctx* ctx);
 /* Introspection (no reference counterpart): writes a JSON object describing the
  * context's execution choices -- precision, whether the step is a CUDA graph, and
  * per member group its shape, member count, the autotuned linear-pass block
- * (modes, threads) and the theta-transform path ("fft-fp64", "fft-fp32" or
- * "tcgen05-3xtf32") -- into buf (NUL-terminated).  NSP_ERR_ARG if cap is too small. */
+ * (modes, threads; in the mixed form also the corrector's increment pass, as
+ * "linear_block_corrector") and the theta-transform path ("fft-fp64", "fft-fp32"
+ * or "tcgen05-3xtf32") -- into buf (NUL-terminated).  NSP_ERR_ARG if cap is too small. */
 int nsp_describe(nsp_ctx* ctx, char* buf, int cap);
 
 /* Makes the context launch its work on `stream` (a cudaStream_t of the context's
