@@ -153,6 +153,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   __shared__ double snkz2[LM], snkt2[LM], shdk[LM];  // -k_z^2, -k_theta^2, -c_ex k_theta (predictor)
   __shared__ int spar[LM];             // |m| mod 2 (selects the parity tables)
   __shared__ float skt32[LM], skz32[LM];  // k_theta, k_z in FP32 (increment passes)
+  __shared__ float snkz2_32[LM], snkt2_32[LM], shdk32[LM];  // FP32 copies (mixed predictor)
   __shared__ int bad;
   // (selects instead of indexing the parameter arrays by a run-time value, which
   // would copy them to local memory)
@@ -185,6 +186,9 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     shdk[tid] = -(0.5 * c_ex) * (2.0 * kt);
     skt32[tid] = f64_to_f32(kt);
     skz32[tid] = f64_to_f32(kz);
+    snkz2_32[tid] = f64_to_f32(snkz2[tid]);
+    snkt2_32[tid] = f64_to_f32(snkt2[tid]);
+    shdk32[tid] = f64_to_f32(shdk[tid]);
   }
   __syncthreads();
 
@@ -218,20 +222,15 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       }
       int par_m = spar[mm];
       int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
-      // the diagonals from the per-mode tables: 4 FP64 operations per point
-      const double ir2 = tb.rinv2[i];
-      const double base = fma(snkt2[mm], ir2, snkz2[mm]);  // -k_z^2 - k_theta^2 / r^2
-      const double hz = fma(hc, base, hidt);                // diagonal of the u_z line / 2
-      const double hs = fma(-hc, ir2, hz);                  // s/2 = hc (base - 1/r^2) + 1/(2 dt)
-      const double hd = shdk[mm] * ir2;                     // d/2 = -hc 2 k_theta / r^2
       const int lo = (1 - par_m) * STEN * NR + STEN * i + i0;  // u_r, u_theta rows (odd flag)
       const int le = par_m * STEN * NR + STEN * i + i0;        // u_z rows
-      double2 lr, lt, lz;
+      const size_t h = (size_t)i * NTNZ + k;
       if (Un32 && k != 0) {
-        // mixed form: the stencil sums in FP32 on the FP32 mirror of u^n.  The sums are
-        // (1-d_im)/Re times the radial Laplacian, a small fraction of the u^n/dt term
-        // that the diagonal below adds in FP64.  The mean mode (k = 0) stays in FP64:
-        // its Laplacian is steady, so FP32 rounding there would add up step after step.
+        // mixed form: everything but u^n/dt in FP32 on the FP32 mirror of u^n -- the
+        // stencil sums and the diagonal terms ((1-d_im)/Re times the Laplacian) and N/2
+        // (exact in FP32: the FP32 transforms' values) -- then one FP64 multiply-add
+        // per value adds u^n/dt.  The mean mode (k = 0) stays in FP64: its Laplacian is
+        // steady, so FP32 rounding there would add up step after step.
         float2 fr = make_float2(0.f, 0.f), ft = fr, fz = fr;
         for (int j = 0; j < len; j++) {
           const float a = __ldg(Luc32 + lo + j), b = __ldg(Luc32 + le + j);
@@ -241,27 +240,49 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
           ft.x = fmaf(a, vt.x, ft.x); ft.y = fmaf(a, vt.y, ft.y);
           fz.x = fmaf(b, vz.x, fz.x); fz.y = fmaf(b, vz.y, fz.y);
         }
-        // exact widening on the integer pipe (the hardware conversion issues on the FP64 pipe)
-        lr = c2(f32_to_f64(fr.x), f32_to_f64(fr.y));
-        lt = c2(f32_to_f64(ft.x), f32_to_f64(ft.y));
-        lz = c2(f32_to_f64(fz.x), f32_to_f64(fz.y));
-      } else {
-        lr = c2(0, 0); lt = c2(0, 0); lz = c2(0, 0);
-        for (int j = 0; j < len; j++) {
-          double a = __ldg(Luc + lo + j), b = __ldg(Luc + le + j);
-          size_t hj = (size_t)(left + j) * NTNZ + k;
-          double2 vr = Un[hj], vt = Un[S + hj], vz = Un[2 * S + hj];
-          lr.x += a * vr.x; lr.y += a * vr.y;
-          lt.x += a * vt.x; lt.y += a * vt.y;
-          lz.x += b * vz.x; lz.y += b * vz.y;
+        const float ri = tb.rinv32[i], ir2f = ri * ri, hcf = f64_to_f32(hc);
+        const float basef = fmaf(snkt2_32[mm], ir2f, snkz2_32[mm]);  // -k_z^2 - k_theta^2 / r^2
+        const float hzf = hcf * basef, hsf = hcf * (basef - ir2f), hdf = shdk32[mm] * ir2f;
+        {
+          const float2 fur = __ldg(Un32 + h), fut = __ldg(Un32 + S + h), fuz = __ldg(Un32 + 2 * S + h);
+          fr.x += fmaf(hsf, fur.x, -hdf * fut.y);
+          fr.y += fmaf(hsf, fur.y, hdf * fut.x);
+          ft.x += fmaf(hsf, fut.x, hdf * fur.y);
+          ft.y += fmaf(hsf, fut.y, -hdf * fur.x);
+          fz.x += hzf * fuz.x;
+          fz.y += hzf * fuz.y;
         }
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          const double2 n = Nn[c * S + h], u = Un[c * S + h];
+          Rw[c * S + h] = n;  // N(u^n) for the first increment pass
+          const float2 f = c == 0 ? fr : (c == 1 ? ft : fz);
+          const float gx = fmaf(0.5f, f64_to_f32(n.x), f.x), gy = fmaf(0.5f, f64_to_f32(n.y), f.y);
+          // widening on the integer pipe (the hardware conversion issues on the FP64 pipe)
+          R[c * LN + p] = c2(fma(hidt, u.x, f32_to_f64(gx)), fma(hidt, u.y, f32_to_f64(gy)));
+        }
+        continue;
       }
-      size_t h = (size_t)i * NTNZ + k;
-      double2 ur = Un[h], ut = Un[S + h], uz = Un[2 * S + h];
+      // the diagonals from the per-mode tables: 4 FP64 operations per point
+      const double ir2 = tb.rinv2[i];
+      const double base = fma(snkt2[mm], ir2, snkz2[mm]);  // -k_z^2 - k_theta^2 / r^2
+      const double hz = fma(hc, base, hidt);                // diagonal of the u_z line / 2
+      const double hs = fma(-hc, ir2, hz);                  // s/2 = hc (base - 1/r^2) + 1/(2 dt)
+      const double hd = shdk[mm] * ir2;                     // d/2 = -hc 2 k_theta / r^2
+      double2 lr = c2(0, 0), lt = c2(0, 0), lz = c2(0, 0);
+      for (int j = 0; j < len; j++) {
+        double a = __ldg(Luc + lo + j), b = __ldg(Luc + le + j);
+        size_t hj = (size_t)(left + j) * NTNZ + k;
+        double2 vr = Un[hj], vt = Un[S + hj], vz = Un[2 * S + hj];
+        lr.x += a * vr.x; lr.y += a * vr.y;
+        lt.x += a * vt.x; lt.y += a * vt.y;
+        lz.x += b * vz.x; lz.y += b * vz.y;
+      }
+      const double2 ur = Un[h], ut = Un[S + h], uz = Un[2 * S + h];
       double2 er = c2(lr.x + hs * ur.x - hd * ut.y, lr.y + hs * ur.y + hd * ut.x);
       double2 et = c2(lt.x + hs * ut.x + hd * ur.y, lt.y + hs * ut.y - hd * ur.x);
       double2 ez = c2(lz.x + hz * uz.x, lz.y + hz * uz.y);
-      double2 nr = Nn[h], nt = Nn[S + h], nz = Nn[2 * S + h];
+      const double2 nr = Nn[h], nt = Nn[S + h], nz = Nn[2 * S + h];
       R[p] = c2(0.5 * nr.x + er.x, 0.5 * nr.y + er.y);
       R[LN + p] = c2(0.5 * nt.x + et.x, 0.5 * nt.y + et.y);
       R[2 * LN + p] = c2(0.5 * nz.x + ez.x, 0.5 * nz.y + ez.y);
