@@ -163,6 +163,48 @@ def test_mirror_refresh_matches_linear_pass(nsp, name):
     b.close()
 
 
+def test_mirror_refreshed_after_device_writes(nsp):
+    """A state written device to device (nsp_set_state_device) also marks the FP32
+    mirror stale: stepping on from it equals stepping a context that never had the
+    member's other state."""
+    import torch
+    NR, NT, NZ, LZ, Re, dt, _, _ = CFG["c0"]
+    prm = [nsp.make_params(NR, NT, NZ, Re, dt, LZ) for _ in range(2)]
+    u0, u1 = init(nsp, "c0", 0), init(nsp, "c0", 1)
+    a = nsp.Stepper(prm, precision=nsp.NSP_MIXED)
+    b = nsp.Stepper(prm, precision=nsp.NSP_MIXED)
+    for m in range(2):
+        a.set_state(m, u0)
+        b.set_state(m, u1 if m == 1 else u0)
+    a.step(1)  # a's mirror of member 1 is now the one the linear pass kept (u0's successor)
+    d = [torch.from_numpy(np.ascontiguousarray(x)).cuda() for x in u1]
+    a.set_state_device(1, *d)
+    a.step(2)
+    b.step(2)
+    assert np.array_equal(np.stack(a.get_state(1)), np.stack(b.get_state(1)))
+    a.close()
+    b.close()
+
+
+@pytest.mark.parametrize("weights", ["3:1", "1:0:2", "5", "2:3:3:2:9"])
+def test_step_host_chunk_weights(nsp, monkeypatch, weights):
+    """nsp_step_host's member chunks (the NSP_HOST_CHUNKS override: equal chunks or a
+    weight pattern; chunks that round to no member are dropped) change only the
+    overlap of copies and compute, never the results."""
+    from conftest import PI2
+    shapes = [(24, 8, 9) if k % 3 else (32, 16, 17) for k in range(11)]
+    prm = [nsp.make_params(*s, 1000.0 + 10 * k, 0.005, PI2) for k, s in enumerate(shapes)]
+    fields = [nsp.seeded_field(*s, PI2, 0.05, 90 + k) for k, s in enumerate(shapes)]
+    ref = nsp.Stepper(prm, precision=nsp.NSP_MIXED)
+    out_ref, it_ref = ref.step_host(2, ref.pack(fields))
+    ref.close()
+    monkeypatch.setenv("NSP_HOST_CHUNKS", weights)
+    st = nsp.Stepper(prm, precision=nsp.NSP_MIXED)
+    out, it = st.step_host(2, st.pack(fields))
+    st.close()
+    assert np.array_equal(out, out_ref) and np.array_equal(it, it_ref)
+
+
 def test_batched_diagnostics_equal_per_member(nsp):
     """nsp_diag_all / nsp_mean_profile_all / nsp_cross_sections_all (one launch per group
     and kernel) give each member's per-member values bit for bit."""
