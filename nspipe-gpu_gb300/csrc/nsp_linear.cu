@@ -201,7 +201,8 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   // corrector of a step.  The predictor computes it once and stores
   // rhsw' = (1-d_im) N(u^n) + e, in r/theta form and at half scale; a corrector's
   // right-hand side is then d_im N(u_i) + rhsw' (addRHS_k + addLaplacian), with no
-  // stencil, no +/- conversion and no read of u^n.
+  // stencil, no +/- conversion and no read of u^n.  (The mixed form's increment
+  // passes need no rhsw': its predictor stores N(u^n) there instead.)
   if (pred) {
     // e = u^n/dt + (1-d_im)/Re (L_r - k_z^2 - m^2/r^2 [-1/r^2 -+ 2m/r^2]) u^n on the +/- lines
     // (addLaplacian), evaluated in r/theta form: with dd+- the two diagonals,
