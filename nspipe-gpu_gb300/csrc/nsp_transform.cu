@@ -297,6 +297,11 @@ __device__ __forceinline__ cpx<T> z_pair_spec_in(const cpx<T>* Ga, const cpx<T>*
   return mk<T>(a.x - b.y, a.y + b.x);
 }
 
+// Pitch (complex values) of a physical row of the two-pass z stage: the smallest
+// value >= NZR that is 12 mod 16, so that the rows written by one warp in pass B
+// (12 lanes per transform, 8-byte values) fall on disjoint bank ranges.
+constexpr int z2_pitch(int nzr) { return nzr + (28 - nzr % 16) % 16; }
+
 template <typename T, int NZRC, int N1, int N2, int R>
 __global__ void __launch_bounds__(Z2TH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl, int standalone) {
   static_assert(N1 * N2 == NZRC && R % 2 == 0 && NZRC % 3 == 0, "z split");
@@ -304,7 +309,7 @@ __global__ void __launch_bounds__(Z2TH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl
   constexpr int NQ = NZ - 1;          // retained z modes of the output
   constexpr int YP = N1 + 1;          // padded transpose row
   constexpr int YT = N2 * YP;         // one transform in the transpose buffer
-  constexpr int PS = NZRC + 2;        // padded physical row (complex pairs)
+  constexpr int PS = z2_pitch(NZRC);  // padded physical row (complex pairs)
   constexpr int NF = R + R / 2;       // forward transforms: (N_r, N_t) per row, (N_z, N_z) per row pair
   const int mloc = blockIdx.z, i = blockIdx.y, j0 = blockIdx.x * R;  // NTP % R == 0 (host check)
   if (!standalone && ctl->phase[tb.mem0 + mloc] < 0) return;
@@ -507,7 +512,7 @@ static bool z2_enabled();
 
 template <typename T, int NZRC, int N1, int N2, int R>
 static constexpr size_t z2_smem() {
-  return sizeof(cpx<T>) * ((size_t)R * 6 * N2 * (N1 + 1) + (size_t)R * 6 * (NZRC + 2));
+  return sizeof(cpx<T>) * ((size_t)R * 6 * N2 * (N1 + 1) + (size_t)R * 6 * z2_pitch(NZRC));
 }
 
 template <typename T, int NZRC, int N1, int N2, int R>
