@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(Z2TH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl
     for (int n1 = 0; n1 < N1; n1++) y[n1] = Yt[n1];
     reg_fft<T, -1, N1>(y);
 #pragma unroll
-    for (int k1 = 0; k1 < N1; k1++) Xs[t * NZRC + N2 * k1 + k2] = y[k1];
+    for (int k1 = 0; k1 < N1; k1++) Xs[t * PS + N2 * k1 + k2] = y[k1];
   }
   __syncthreads();
   // 6. unpack x = a + i b: A_q = (X_q + conj X_-q)/2, B_q = (X_q - conj X_-q)/(2i); keep q < NZ-1.
@@ -427,7 +427,7 @@ __global__ void __launch_bounds__(Z2TH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl
     const int q = task % NQ, c = (task / NQ) % 3, r = task / (3 * NQ), j = j0 + r;
     const int slot = c < 2 ? r : R + r / 2;
     const bool takeB = c < 2 ? (c == 1) : (r & 1);
-    const cpx<T>* X = Xs + slot * NZRC;
+    const cpx<T>* X = Xs + slot * PS;
     const cpx<T> xq = X[q], xm = X[(NZRC - q) % NZRC];
     const cpx<T> v = takeB ? mk<T>((T)0.5 * (xq.y + xm.y), (T)-0.5 * (xq.x - xm.x))
                            : mk<T>((T)0.5 * (xq.x + xm.x), (T)0.5 * (xq.y - xm.y));
