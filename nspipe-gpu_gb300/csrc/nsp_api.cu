@@ -330,12 +330,13 @@ int autotune(nsp_ctx* c) {
       float score = 0.f;
       for (int phase = 0; phase < 2; phase++) {
         const std::vector<int>& ph = phase ? ones : zeros;
+        const int which = phase ? LIN_CORR : LIN_PRED;
         CK(cudaMemcpyAsync(c->hctl.phase, ph.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, c->st));
-        launch_linear(tv, g.bf, c->dctl, c->st);
+        launch_linear(tv, g.bf, c->dctl, c->st, which);
         float t = 1e30f;
         for (int r = 0; r < 3; r++) {
           CK(cudaEventRecord(e0, c->st));
-          launch_linear(tv, g.bf, c->dctl, c->st);
+          launch_linear(tv, g.bf, c->dctl, c->st, which);
           CK(cudaEventRecord(e1, c->st));
           CK(cudaEventSynchronize(e1));
           float ms = 0.f;
@@ -375,17 +376,9 @@ int build_graph_range(nsp_ctx* c, int lo, int hi, cudaGraphExec_t* out) {
     c->use_graph = false;
     return NSP_OK;
   }
-  cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
-  cp.type = cudaGraphNodeTypeConditional;
-  cp.conditional.handle = h;
-  cp.conditional.type = cudaGraphCondTypeWhile;
-  cp.conditional.size = 1;
-  cudaGraphNode_t node;
-  CK(cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &cp));
-  cudaGraph_t body = cp.conditional.phGraph_out[0];
   // Member groups (different shapes) are independent until the convergence
-  // bookkeeping: each group's four kernels form their own branch of the body graph
-  // so that groups run concurrently, then converge_k joins them.
+  // bookkeeping: each group's kernels form their own branch of a pass so that groups
+  // run concurrently, then converge_k joins them.
   const size_t ng = c->groups.size();
   if (c->side.size() + 1 < ng) {
     if (!c->ev_fork) CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
@@ -398,26 +391,49 @@ int build_graph_range(nsp_ctx* c, int lo, int hi, cudaGraphExec_t* out) {
       c->ev_join.push_back(e2);
     }
   }
-  CK(cudaStreamBeginCaptureToGraph(c->st, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-  if (ng > 1) CK(cudaEventRecord(c->ev_fork, c->st));
-  for (size_t k = 0; k < ng; k++) {
-    Group& gr = c->groups[k];
-    cudaStream_t sk = k == 0 ? c->st : c->side[k - 1];
-    if (k > 0) CK(cudaStreamWaitEvent(sk, c->ev_fork, 0));
-    const int a = std::max(lo, gr.tb.mem0) - gr.tb.mem0, b = std::min(hi, gr.tb.mem0 + gr.tb.nmem) - gr.tb.mem0;
-    if (a < b) {  // (an empty branch still forks and joins)
-      Tables t;
-      Bufs bf;
-      range_view(gr, c->precision == NSP_MIXED, a, b, &t, &bf);
-      launch_nonlinear(t, bf, c->dctl, c->precision == NSP_MIXED, nullptr, nullptr, sk);
-      launch_linear(t, bf, c->dctl, sk);
+  // One pass (the three transforms and the linear-pass kernel `which` per group, then
+  // converge_k, which sets the loop condition when `cond`) captured into `into`.
+  auto capture_pass = [&](cudaGraph_t into, int which, bool cond) -> int {
+    CK(cudaStreamBeginCaptureToGraph(c->st, into, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    if (ng > 1) CK(cudaEventRecord(c->ev_fork, c->st));
+    for (size_t k = 0; k < ng; k++) {
+      Group& gr = c->groups[k];
+      cudaStream_t sk = k == 0 ? c->st : c->side[k - 1];
+      if (k > 0) CK(cudaStreamWaitEvent(sk, c->ev_fork, 0));
+      const int a = std::max(lo, gr.tb.mem0) - gr.tb.mem0, b = std::min(hi, gr.tb.mem0 + gr.tb.nmem) - gr.tb.mem0;
+      if (a < b) {  // (an empty branch still forks and joins)
+        Tables t;
+        Bufs bf;
+        range_view(gr, c->precision == NSP_MIXED, a, b, &t, &bf);
+        launch_nonlinear(t, bf, c->dctl, c->precision == NSP_MIXED, nullptr, nullptr, sk);
+        launch_linear(t, bf, c->dctl, sk, which);
+      }
+      if (k > 0) CK(cudaEventRecord(c->ev_join[k - 1], sk));
     }
-    if (k > 0) CK(cudaEventRecord(c->ev_join[k - 1], sk));
-  }
-  for (size_t k = 1; k < ng; k++) CK(cudaStreamWaitEvent(c->st, c->ev_join[k - 1], 0));
-  launch_converge(c->dctl, c->nmem, (unsigned long long)h, 1, c->st);
-  cudaGraph_t cap = nullptr;
-  CK(cudaStreamEndCapture(c->st, &cap));
+    for (size_t k = 1; k < ng; k++) CK(cudaStreamWaitEvent(c->st, c->ev_join[k - 1], 0));
+    launch_converge(c->dctl, c->nmem, (unsigned long long)h, cond ? 1 : 0, c->st);
+    cudaGraph_t cap = nullptr;
+    CK(cudaStreamEndCapture(c->st, &cap));
+    return NSP_OK;
+  };
+  // The step: the predictor pass (a child graph), then the corrector passes in a
+  // conditional WHILE node whose condition converge_k sets; the condition's default
+  // value 1 makes at least one corrector pass, as in the reference.
+  cudaGraph_t gp = nullptr;
+  CK(cudaGraphCreate(&gp, 0));
+  if (int rc = capture_pass(gp, LIN_PRED, false)) { cudaGraphDestroy(gp); cudaGraphDestroy(g); return rc; }
+  cudaGraphNode_t pnode;
+  cudaError_t ec = cudaGraphAddChildGraphNode(&pnode, g, nullptr, 0, gp);  // (clones gp)
+  cudaGraphDestroy(gp);
+  CK(ec);
+  cudaGraphNodeParams cp = {cudaGraphNodeTypeConditional};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = cudaGraphCondTypeWhile;
+  cp.conditional.size = 1;
+  cudaGraphNode_t node;
+  CK(cudaGraphAddNode(&node, g, &pnode, nullptr, 1, &cp));
+  if (int rc = capture_pass(cp.conditional.phGraph_out[0], LIN_CORR, true)) { cudaGraphDestroy(g); return rc; }
   CK(cudaGraphInstantiate(out, g, 0));
   cudaGraphDestroy(g);
   c->use_graph = true;
@@ -893,10 +909,11 @@ static void mirror_range(nsp_ctx* c, int lo, int hi, int par, cudaStream_t st) {
 }
 
 // Kernels launched per predictor or corrector pass: per group the three transform
-// kernels and the linear pass (two kernels in the mixed form: the full pass for the
-// predictor, the increment pass for the correctors), then converge_k.
+// kernels and the linear pass, then converge_k.  The step graph launches the pass's
+// own linear kernel; the host-driven loop launches both of the mixed form's (the
+// full pass for the predictor, the increment pass for the correctors).
 static long long kernels_per_pass(const nsp_ctx* c) {
-  return (c->precision == NSP_MIXED ? 5LL : 4LL) * (long long)c->groups.size() + 1;
+  return (c->precision == NSP_MIXED && !c->use_graph ? 5LL : 4LL) * (long long)c->groups.size() + 1;
 }
 
 // The step history of the last `batch` steps into the pinned buffer; with `final` also
@@ -1456,7 +1473,7 @@ int nsp_profile_stages(nsp_ctx* c, int reps, double* ms_out) {
       if (stage < 3) {
         for (auto& g : c->groups) launch_nonlinear(g.tb, g.bf, c->dctl, mixed, nullptr, nullptr, c->st, 1 << stage);
       } else if (stage == 3) {
-        for (auto& g : c->groups) launch_linear(g.tb, g.bf, c->dctl, c->st);
+        for (auto& g : c->groups) launch_linear(g.tb, g.bf, c->dctl, c->st, LIN_PRED);  // phases are 0
       } else {
         launch_converge(c->dctl, nm, 0ull, 0, c->st);
       }

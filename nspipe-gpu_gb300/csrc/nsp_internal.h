@@ -120,7 +120,12 @@ struct Ctl {
 // src32_override: FP32 copy of src_override (mixed form, explicit-field calls only).
 void launch_nonlinear(const Tables& tb, const Bufs& bf, Ctl* dctl, bool mixed, const double2* src_override,
                       double2* dst_override, cudaStream_t st, int mask = 7, const float2* src32_override = nullptr);
-void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st);
+// Which linear-pass kernels a launch issues: the predictor's (the full pass), the
+// correctors' (the mixed form's increment pass; the full pass again in the FP64 form)
+// or both (each returns at once in the other's passes; the FP64 form launches its one
+// kernel once).
+enum { LIN_PRED = 1, LIN_CORR = 2, LIN_BOTH = 3 };
+void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st, int which = LIN_BOTH);
 void launch_converge(Ctl* dctl, int nmem, unsigned long long cond_handle, int use_cond, cudaStream_t st);
 // Completes a step taken in member chunks: parity flip and step count (converge_k's
 // completion work, held back while the chunks ran).

@@ -859,10 +859,12 @@ void configure_linear_kernels() {
 #undef NSP_LIN_CFG
 }
 
-void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st) {
+void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st, int which) {
   // The full pass, then in the mixed form the increment pass (correctors), each with
   // its own block shape; each returns at once in the other's passes.
-  for (int pass = 0; pass < (bf.U32[0] != nullptr ? 2 : 1); pass++) {
+  const bool mixed = bf.U32[0] != nullptr;
+  for (int pass = 0; pass < 2; pass++) {
+    if (mixed ? !(which & (pass ? LIN_CORR : LIN_PRED)) : (pass == 1 || which == 0)) continue;
     const int want = pass ? tb.lin_variant_inc : tb.lin_variant;
     const int v = linear_variant_fits(want, tb.NR) ? want : linear_default_variant(tb.NR);
     const LinShape s = kLinShapes[v];
