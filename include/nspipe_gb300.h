@@ -39,6 +39,9 @@ extern "C" {
 #define NSP_ERR_NOMEM 6      /* device allocation failed                           */
 #define NSP_ERR_DEVICE 7     /* a bounded device-side wait ran out (a tensor-core
                                 tile pipeline did not complete); results invalid   */
+#define NSP_ERR_MAXIT 8      /* strict mode only (nsp_set_strict): a member's corrector
+                                loop stopped at maxit with err > tol; the steps were
+                                taken as the reference takes them                   */
 
 #define NSP_FP64 0  /* plain form: every operation in FP64 (matches the reference)         */
 #define NSP_MIXED 1 /* transforms + nonlinear product in FP32; solves, BCs, state in FP64 */
@@ -69,6 +72,9 @@ typedef struct nsp_diag_out {
   double div_max;     /* max |div u| over the interior rows (div_k, mod_radialFD.cu:67-96) */
   double div_wall;    /* max |div u| on the wall row, the quantity the influence-matrix
                          correction drives to zero (divWall_k, mod_radialFD.cu:34-63)     */
+  int unconverged_steps; /* steps of the last nsp_step / nsp_step_host call whose corrector
+                            loop stopped at maxit with err > tol (the reference moves on
+                            silently, mod_integrate.cu:120)                               */
 } nsp_diag_out;
 
 typedef struct nsp_ctx nsp_ctx;
@@ -113,7 +119,11 @@ int nsp_get_state_device(nsp_ctx* ctx, int member, void* ur, void* ut, void* uz)
  * own iteration count.  One CUDA graph per step; the corrector loop is a device-side
  * conditional node.  iters_out (optional) receives nsteps*n_members counts,
  * step-major.  Returns NSP_ERR_NONFINITE if any member's convergence measure became
- * NaN/Inf (the other members are still advanced). */
+ * NaN/Inf (the other members are still advanced).  A step whose corrector loop stops
+ * at maxit with err > tol is taken as in the reference, which continues silently
+ * (mod_integrate.cu:120); it is counted per member (nsp_diag_out.unconverged_steps)
+ * and, in strict mode (nsp_set_strict), makes the call return NSP_ERR_MAXIT after all
+ * nsteps steps. */
 int nsp_step(nsp_ctx* ctx, int nsteps, int* iters_out);
 
 /* Host-resident form of integrate() over the whole ensemble: the states in `in` are
@@ -124,7 +134,7 @@ int nsp_step(nsp_ctx* ctx, int nsteps, int* iters_out);
  * stepped in chunks, each with its own step graph, so that the first step's copies in
  * and the last step's copies out overlap the other chunks' compute; the host arrays
  * should be pinned (cudaHostAlloc / cudaHostRegister) for the copies to overlap.
- * iters_out as nsp_step. */
+ * iters_out and the status codes as nsp_step. */
 int nsp_step_host(nsp_ctx* ctx, int nsteps, const double* in, double* out, int* iters_out);
 
 /* The nonlinear term -(u.grad)u of one member's field (r/theta form), 3/2-dealiased,
@@ -147,8 +157,10 @@ int nsp_nonlinear(nsp_ctx* ctx, int member, const void* ur, const void* ut, cons
  * NSP_ERR_ARG.  The first call on a device looks up the array's device address, so
  * make that first call before any stream capture.  The array is shared by every
  * call: calls that overlap on the GPU (other threads, other contexts on the same
- * device) race on it.  Nothing in it needs to start at zero.  Synchronises the
- * context's stream. */
+ * device) race on it.  Nothing in it needs to start at zero.  u3 and n3 must not
+ * overlap (NSP_ERR_ARG).  The cached address belongs to the device's primary context:
+ * do not call this on a device after cudaDeviceReset of that device.  Synchronises the
+ * context's stream; NSP_ERR_DEVICE as nsp_nonlinear if a tensor-core wait ran out. */
 int nsp_nonlinear_static(nsp_ctx* ctx, int member, const void* u3, void* n3);
 
 /* One banded solve on one member's operators (LUsolve_u flag 0/1/2 and LUsolve_p,
@@ -197,6 +209,13 @@ int nsp_describe(nsp_ctx* ctx, char* buf, int cap);
  * device); NULL restores the context's own stream.  The reference runs on the
  * legacy default stream (no equivalent entry point). */
 int nsp_set_stream(nsp_ctx* ctx, void* stream);
+
+/* Strict convergence (no reference counterpart; the reference's integrate() moves on
+ * silently at maxit, mod_integrate.cu:120): with strict != 0, nsp_step, nsp_step_host
+ * and nsp_run_advance return NSP_ERR_MAXIT when a member's corrector loop stopped at
+ * maxit with err > tol in one of the call's steps (NSP_ERR_NONFINITE takes precedence).
+ * The states are those of the non-strict call.  Default 0. */
+int nsp_set_strict(nsp_ctx* ctx, int strict);
 
 /* Measurement hook (no reference counterpart): average device time in ms of one
  * launch of each kernel of the step, over `reps` back-to-back launches timed with
@@ -285,7 +304,9 @@ int nsp_run_resume(nsp_ctx* ctx, const nsp_run_opts* o, const char* ckpt, nsp_ru
  * periodic checkpoint is due), writing rows and checkpoints on the way.  iters_out
  * (optional): nsteps * n_members corrector iteration counts, step-major.  A member
  * whose field becomes non-finite ends the call with NSP_ERR_NONFINITE after the rows
- * of that chunk are written, and no checkpoint is written for that state. */
+ * of that chunk are written, and no checkpoint is written for that state; in strict
+ * mode (nsp_set_strict) a step that stopped at maxit without convergence ends the call
+ * the same way with NSP_ERR_MAXIT. */
 int nsp_run_advance(nsp_run* run, int nsteps, int* iters_out);
 
 /* Writes a checkpoint of the current state now (pending rows are written first). */

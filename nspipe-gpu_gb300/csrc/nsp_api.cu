@@ -81,8 +81,12 @@ struct nsp_ctx {
   // Mixed form: U32/DR32[parity] hold the FP32 mirror of U[parity] (kept current by the
   // linear pass; cleared by every call that writes the state from outside).
   bool mirror_ok = false;
-  // Pinned host copy of the step history, then the members' status words, then the
-  // fault flag: read back after the steps with asynchronous copies and one synchronisation.
+  // nsp_set_strict: a step whose corrector loop stopped at maxit with err > tol makes
+  // nsp_step / nsp_step_host return NSP_ERR_MAXIT.
+  bool strict = false;
+  // Pinned host copy of the step history, then the members' status words, the fault
+  // flag and the members' unconverged-step counts: read back after the steps with
+  // asynchronous copies and one synchronisation.
   int* pin = nullptr;
   std::vector<void*> allocs;
   std::string err;
@@ -368,10 +372,13 @@ int build_graph_range(nsp_ctx* c, int lo, int hi, cudaGraphExec_t* out) {
   if (*out) { cudaGraphExecDestroy(*out); *out = nullptr; }
   cudaGraph_t g = nullptr;
   CK(cudaGraphCreate(&g, 0));
+  struct GraphOwner {  // destroys the step graph on every return path (instantiation copies it)
+    cudaGraph_t g;
+    ~GraphOwner() { cudaGraphDestroy(g); }
+  } owner{g};
   cudaGraphConditionalHandle h;
   cudaError_t e = cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault);
   if (e != cudaSuccess) {
-    cudaGraphDestroy(g);
     cudaGetLastError();
     c->use_graph = false;
     return NSP_OK;
@@ -393,8 +400,9 @@ int build_graph_range(nsp_ctx* c, int lo, int hi, cudaGraphExec_t* out) {
   }
   // One pass (the three transforms and the linear-pass kernel `which` per group, then
   // converge_k, which sets the loop condition when `cond`) captured into `into`.
-  auto capture_pass = [&](cudaGraph_t into, int which, bool cond) -> int {
-    CK(cudaStreamBeginCaptureToGraph(c->st, into, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  // A failure inside the capture still ends it, so that the context's stream is not
+  // left capturing; the partial graph belongs to `into`, which the caller destroys.
+  auto capture_body = [&](int which, bool cond) -> int {
     if (ng > 1) CK(cudaEventRecord(c->ev_fork, c->st));
     for (size_t k = 0; k < ng; k++) {
       Group& gr = c->groups[k];
@@ -412,8 +420,18 @@ int build_graph_range(nsp_ctx* c, int lo, int hi, cudaGraphExec_t* out) {
     }
     for (size_t k = 1; k < ng; k++) CK(cudaStreamWaitEvent(c->st, c->ev_join[k - 1], 0));
     launch_converge(c->dctl, c->nmem, (unsigned long long)h, cond ? 1 : 0, c->st);
+    return NSP_OK;
+  };
+  auto capture_pass = [&](cudaGraph_t into, int which, bool cond) -> int {
+    CK(cudaStreamBeginCaptureToGraph(c->st, into, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    const int rc = capture_body(which, cond);
     cudaGraph_t cap = nullptr;
-    CK(cudaStreamEndCapture(c->st, &cap));
+    const cudaError_t e_end = cudaStreamEndCapture(c->st, &cap);
+    if (rc) {
+      cudaGetLastError();  // (an invalidated capture also fails to end)
+      return rc;
+    }
+    CK(e_end);
     return NSP_OK;
   };
   // The step: the predictor pass (a child graph), then the corrector passes in a
@@ -421,7 +439,7 @@ int build_graph_range(nsp_ctx* c, int lo, int hi, cudaGraphExec_t* out) {
   // value 1 makes at least one corrector pass, as in the reference.
   cudaGraph_t gp = nullptr;
   CK(cudaGraphCreate(&gp, 0));
-  if (int rc = capture_pass(gp, LIN_PRED, false)) { cudaGraphDestroy(gp); cudaGraphDestroy(g); return rc; }
+  if (int rc = capture_pass(gp, LIN_PRED, false)) { cudaGraphDestroy(gp); return rc; }
   cudaGraphNode_t pnode;
   cudaError_t ec = cudaGraphAddChildGraphNode(&pnode, g, nullptr, 0, gp);  // (clones gp)
   cudaGraphDestroy(gp);
@@ -433,9 +451,8 @@ int build_graph_range(nsp_ctx* c, int lo, int hi, cudaGraphExec_t* out) {
   cp.conditional.size = 1;
   cudaGraphNode_t node;
   CK(cudaGraphAddNode(&node, g, &pnode, nullptr, 1, &cp));
-  if (int rc = capture_pass(cp.conditional.phGraph_out[0], LIN_CORR, true)) { cudaGraphDestroy(g); return rc; }
+  if (int rc = capture_pass(cp.conditional.phGraph_out[0], LIN_CORR, true)) return rc;
   CK(cudaGraphInstantiate(out, g, 0));
-  cudaGraphDestroy(g);
   c->use_graph = true;
   return NSP_OK;
 }
@@ -577,6 +594,8 @@ int nsp_create(const nsp_params* members, int n_members, int precision, int devi
   if ((rc = dalloc(c, &h.den, sizeof(unsigned long long) * n_members))) return rc;
   if ((rc = dalloc(c, &h.err, sizeof(double) * n_members))) return rc;
   if ((rc = dalloc(c, &h.hist, sizeof(int) * n_members * (size_t)h.hist_cap))) return rc;
+  if ((rc = dalloc(c, &h.unconv, sizeof(int) * n_members))) return rc;
+  CK(cudaMemset(h.unconv, 0, sizeof(int) * n_members));
   CK(cudaMemset(h.phase, 0, sizeof(int) * n_members));
   CK(cudaMemset(h.ite, 0, sizeof(int) * n_members));
   CK(cudaMemset(h.status, 0, sizeof(int) * n_members));
@@ -585,7 +604,7 @@ int nsp_create(const nsp_params* members, int n_members, int precision, int devi
   CK(cudaMemset(h.err, 0, sizeof(double) * n_members));
   if ((rc = dalloc(c, &c->dctl, sizeof(Ctl)))) return rc;
   CK(cudaMemcpy(c->dctl, &h, sizeof(Ctl), cudaMemcpyHostToDevice));
-  CK(cudaMallocHost(&c->pin, sizeof(int) * ((size_t)(h.hist_cap + 1) * n_members + 1)));
+  CK(cudaMallocHost(&c->pin, sizeof(int) * ((size_t)(h.hist_cap + 2) * n_members + 1)));
   return NSP_OK;
 }
 
@@ -917,7 +936,8 @@ static long long kernels_per_pass(const nsp_ctx* c) {
 }
 
 // The step history of the last `batch` steps into the pinned buffer; with `final` also
-// the members' status words and the fault flag.  One synchronisation of the stream.
+// the members' status words, the fault flag and the unconverged-step counts.  One
+// synchronisation of the stream.
 static int read_control(nsp_ctx* c, int batch, bool final) {
   const int nm = c->nmem;
   const size_t tail = (size_t)c->hctl.hist_cap * nm;
@@ -926,6 +946,7 @@ static int read_control(nsp_ctx* c, int batch, bool final) {
   if (final) {
     CK(cudaMemcpyAsync(c->pin + tail, c->hctl.status, sizeof(int) * nm, cudaMemcpyDeviceToHost, c->st));
     CK(cudaMemcpyAsync(c->pin + tail + nm, &c->dctl->fault, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(c->pin + tail + nm + 1, c->hctl.unconv, sizeof(int) * nm, cudaMemcpyDeviceToHost, c->st));
   }
   CK(cudaStreamSynchronize(c->st));
   return NSP_OK;
@@ -942,6 +963,11 @@ static int control_verdict(nsp_ctx* c) {
   for (int m = 0; m < nm; m++)
     if (tail[c->internal[m]] & NSP_ERR_NONFINITE)
       return fail(c, NSP_ERR_NONFINITE, "member %d: non-finite velocity or convergence measure", m);
+  if (c->strict)
+    for (int m = 0; m < nm; m++)
+      if (const int n = tail[nm + 1 + c->internal[m]])
+        return fail(c, NSP_ERR_MAXIT, "member %d: %d step(s) stopped at maxit = %d without convergence", m, n,
+                    c->hctl.maxit);
   return NSP_OK;
 }
 
@@ -960,6 +986,7 @@ int nsp_step(nsp_ctx* c, int nsteps, int* iters_out) {
   if (c->precision == NSP_MIXED && nsteps > 0 && !c->mirror_ok)
     for (auto& g : c->groups) launch_mirror(g.tb, g.bf.U[c->parity], g.bf.U32[c->parity], g.bf.DR32[c->parity], c->st);
   c->mirror_ok = false;
+  if (nsteps > 0) CK(cudaMemsetAsync(c->hctl.unconv, 0, sizeof(int) * nm, c->st));
   if (nsteps == 0)
     if (int rc = read_control(c, 0, true)) return rc;
   for (int done = 0; done < nsteps;) {
@@ -1054,6 +1081,7 @@ int nsp_step_host(nsp_ctx* c, int nsteps, const double* in, double* out, int* it
     c->ev_done.push_back(e2);
   }
   if (int rc = clear_status(c, NSP_ALL_MEMBERS)) return rc;  // every state comes from `in`
+  CK(cudaMemsetAsync(c->hctl.unconv, 0, sizeof(int) * nm, c->st));
   // Copies in may start only once earlier work on the state is done.
   CK(cudaEventRecord(c->ev_done[0], c->st));
   CK(cudaStreamWaitEvent(c->cp_in, c->ev_done[0], 0));
@@ -1157,6 +1185,11 @@ int nsp_nonlinear_static(nsp_ctx* c, int m, const void* u3, void* n3) {
   if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_nonlinear_static before nsp_setup");
   if (!u3 || !n3) return fail(c, NSP_ERR_ARG, "null field pointer");
   Group& g = c->groups[c->grp[m]];
+  {  // the transforms read u3 until the last kernel writes n3 (the wall forcing reads u_z)
+    const char *a = (const char*)u3, *b = (const char*)n3;
+    const size_t fb = 3 * sizeof(double2) * (size_t)g.tb.S;
+    if (a < b + fb && b < a + fb) return fail(c, NSP_ERR_ARG, "nsp_nonlinear_static: u3 and n3 overlap");
+  }
   const bool mixed = c->precision == NSP_MIXED;
   const size_t csz = mixed ? sizeof(float2) : sizeof(double2);
   auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
@@ -1180,7 +1213,7 @@ int nsp_nonlinear_static(nsp_ctx* c, int m, const void* u3, void* n3) {
   launch_nonlinear(tv, b, c->dctl, mixed, (const double2*)u3, (double2*)n3, c->st, 7, in32);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->st));
-  return NSP_OK;
+  return check_fault(c);  // a tensor-core wait that ran out leaves n3 invalid
 }
 
 int nsp_lusolve(nsp_ctx* c, int m, int kind, const void* rhs, void* sol) {
@@ -1240,8 +1273,9 @@ int nsp_diag(nsp_ctx* c, int m, nsp_diag_out* out) {
   int status = 0;
   CK(cudaMemcpyAsync(&err, c->hctl.err + mi, sizeof(double), cudaMemcpyDeviceToHost, c->st));
   CK(cudaMemcpyAsync(&status, c->hctl.status + mi, sizeof(int), cudaMemcpyDeviceToHost, c->st));
-  int ite = 0;
+  int ite = 0, unconv = 0;
   CK(cudaMemcpyAsync(&ite, c->hctl.ite + mi, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(&unconv, c->hctl.unconv + mi, sizeof(int), cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   std::vector<double> uz0(NR);
   for (int i = 0; i < NR; i++) uz0[i] = uz[i].x;
@@ -1249,6 +1283,7 @@ int nsp_diag(nsp_ctx* c, int m, nsp_diag_out* out) {
   out->last_err = err;
   out->last_iters = ite;
   out->status = (status & NSP_ERR_NONFINITE) ? NSP_ERR_NONFINITE : NSP_OK;
+  out->unconverged_steps = unconv;
   // Divergence of the state on the device.
   if (int rc = ensure_diagbuf(c)) return rc;
   CK(cudaMemsetAsync(c->diagbuf, 0, 2 * sizeof(unsigned long long), c->st));
@@ -1297,8 +1332,9 @@ int nsp_diag_all(nsp_ctx* c, nsp_diag_out* out) {
   CK(cudaGetLastError());
   std::vector<unsigned long long> bits(2 * (size_t)nm);
   std::vector<double> err(nm);
-  std::vector<int> status(nm), ite(nm);
+  std::vector<int> status(nm), ite(nm), unconv(nm);
   CK(cudaMemcpyAsync(bits.data(), c->diagbuf, sizeof(unsigned long long) * bits.size(), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaMemcpyAsync(unconv.data(), c->hctl.unconv, sizeof(int) * nm, cudaMemcpyDeviceToHost, c->st));
   CK(cudaMemcpyAsync(err.data(), c->hctl.err, sizeof(double) * nm, cudaMemcpyDeviceToHost, c->st));
   CK(cudaMemcpyAsync(status.data(), c->hctl.status, sizeof(int) * nm, cudaMemcpyDeviceToHost, c->st));
   CK(cudaMemcpyAsync(ite.data(), c->hctl.ite, sizeof(int) * nm, cudaMemcpyDeviceToHost, c->st));
@@ -1312,6 +1348,7 @@ int nsp_diag_all(nsp_ctx* c, nsp_diag_out* out) {
     out[m].last_err = err[mi];
     out[m].last_iters = ite[mi];
     out[m].status = (status[mi] & NSP_ERR_NONFINITE) ? NSP_ERR_NONFINITE : NSP_OK;
+    out[m].unconverged_steps = unconv[mi];
     double dv[2];
     memcpy(dv, bits.data() + 2 * (size_t)mi, sizeof dv);
     out[m].div_max = dv[0];
@@ -1455,6 +1492,12 @@ int nsp_set_stream(nsp_ctx* c, void* stream) {
   if (!c) return NSP_ERR_ARG;
   CK(cudaStreamSynchronize(c->st));
   c->st = stream ? (cudaStream_t)stream : c->own_st;
+  return NSP_OK;
+}
+
+int nsp_set_strict(nsp_ctx* c, int strict) {
+  if (!c) return NSP_ERR_ARG;
+  c->strict = strict != 0;
   return NSP_OK;
 }
 

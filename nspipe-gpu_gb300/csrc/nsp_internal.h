@@ -106,6 +106,8 @@ struct Ctl {
   unsigned long long* den;  // max |u_i|^2
   double* err;
   int* hist;           // [cap][nmem]: iterations of each step of the call
+  int* unconv;         // [nmem]: steps of the current call whose corrector loop stopped at
+                       // maxit with err > tol (the reference moves on silently)
   int hist_cap;
   int fault;           // nonzero: a device-side wait ran out and a kernel abandoned its work
   int hold;            // nonzero: a completed step keeps parity and step count (chunked

@@ -655,6 +655,7 @@ __global__ void converge_k(Ctl* ctl, cudaGraphConditionalHandle h, int use_cond)
       bool more = (it < ctl->maxit) && (err > ctl->tol);
       if (!more) {
         if (ctl->step < ctl->hist_cap) ctl->hist[(size_t)ctl->step * nm + m] = it;
+        if (err > ctl->tol) ctl->unconv[m] += 1;  // stopped by maxit, not converged (one thread per m)
         ph = -1;
       } else {
         ph = ph + 1;

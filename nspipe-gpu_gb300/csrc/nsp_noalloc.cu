@@ -14,7 +14,10 @@
 // holds NOALLOC_SCRATCH_BYTES on each GPU it uses until it exits.  In host code
 // the symbol's name is only a host-side stand-in, so its device address is looked
 // up once per device with cudaGetSymbolAddress (with that device current) and
-// cached; the first call on a device does this set-up.
+// cached; the first call on a device does this set-up.  The cached address belongs
+// to the device's primary context: after cudaDeviceReset on that device the module
+// is loaded again (possibly elsewhere), so a process that resets a device must not
+// call the allocation-free entry point on it afterwards.
 #include <mutex>
 #include <string>
 

@@ -779,7 +779,7 @@ int nsp_run_advance(nsp_run* r, int nsteps, int* iters_out) {
     if (r->o.ckpt_every > 0) k = (int)std::min<long long>(k, r->o.ckpt_every - r->step % r->o.ckpt_every);
     it.assign((size_t)k * n, 0);
     int rc = nsp_step(r->ctx, k, it.data());
-    if (rc != NSP_OK && rc != NSP_ERR_NONFINITE) return rc;
+    if (rc != NSP_OK && rc != NSP_ERR_NONFINITE && rc != NSP_ERR_MAXIT) return rc;
     if (iters_out) std::copy(it.begin(), it.end(), iters_out + (size_t)done * n);
     r->step += k;
     done += k;
@@ -802,7 +802,7 @@ int nsp_run_advance(nsp_run* r, int nsteps, int* iters_out) {
       due[i][2] = due[i][2] && m.out[F_MNP].f;
     }
     if (int s = sample(r, due, target)) return s;
-    if (rc == NSP_ERR_NONFINITE) {
+    if (rc == NSP_ERR_NONFINITE || rc == NSP_ERR_MAXIT) {  // rows of the chunk, no checkpoint
       flush_all(r);
       return rc;
     }

@@ -17,7 +17,8 @@ from .initfield import PI2, radial_grid, read_state, seeded_field, write_state  
 _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(os.path.dirname(_HERE), "libnspipe_gb300.so")
 
-NSP_OK, NSP_ERR_ARG, NSP_ERR_CUDA, NSP_ERR_IO, NSP_ERR_NONFINITE, NSP_ERR_STATE, NSP_ERR_NOMEM, NSP_ERR_DEVICE = range(8)
+(NSP_OK, NSP_ERR_ARG, NSP_ERR_CUDA, NSP_ERR_IO, NSP_ERR_NONFINITE, NSP_ERR_STATE, NSP_ERR_NOMEM, NSP_ERR_DEVICE,
+ NSP_ERR_MAXIT) = range(9)
 NSP_FP64, NSP_MIXED = 0, 1
 
 EXPORTS = [
@@ -30,7 +31,7 @@ EXPORTS = [
     "nsp_run_checkpoint", "nsp_run_time", "nsp_run_close", "nsp_checkpoint_info", "nsp_output_schedule",
     "nsp_remesh_create", "nsp_remesh_matrix", "nsp_remesh_device", "nsp_remesh_members", "nsp_remesh_files",
     "nsp_remesh_destroy", "nsp_step_host", "nsp_diag_all", "nsp_mean_profile_all", "nsp_cross_sections_all",
-    "nsp_debug_inject",
+    "nsp_debug_inject", "nsp_set_strict",
 ]
 
 
@@ -49,6 +50,7 @@ class NspDiag(ctypes.Structure):
         ("u_centre", ctypes.c_double), ("u_tau", ctypes.c_double), ("flux", ctypes.c_double),
         ("last_err", ctypes.c_double), ("last_iters", ctypes.c_int), ("status", ctypes.c_int),
         ("re_tau", ctypes.c_double), ("div_max", ctypes.c_double), ("div_wall", ctypes.c_double),
+        ("unconverged_steps", ctypes.c_int),
     ]
 
 
@@ -124,6 +126,7 @@ def lib():
         L.nsp_remesh_files.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p]
         L.nsp_remesh_destroy.argtypes = [vp]
         L.nsp_debug_inject.argtypes = [vp, ip]
+        L.nsp_set_strict.argtypes = [vp, ip]
         L.nsp_last_error.argtypes = [vp]
         L.nsp_last_error.restype = ctypes.c_char_p
         L.nsp_destroy.argtypes = [vp]
@@ -365,6 +368,10 @@ class Stepper:
         t = ctypes.c_double()
         self._check(lib().nsp_measure_fp64_peak(self._h, ctypes.byref(t)))
         return t.value
+
+    def set_strict(self, strict=True):
+        """Strict convergence: steps that stop at maxit with err > tol raise NSP_ERR_MAXIT."""
+        self._check(lib().nsp_set_strict(self._h, int(bool(strict))))
 
     def debug_inject(self, flags):
         """Test hook of the device-side failure path (nsp_debug_inject)."""

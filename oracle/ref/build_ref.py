@@ -32,8 +32,10 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
 REF_OUT = os.path.join(ORACLE, "_ref")
-REF_SRC_DEFAULT = "/root/reference/Main_Code/src"
-REMESH_SRC_DEFAULT = "/root/reference/tools/Re_Mesh/src"
+# Checkout of the reference project: $NSP_REFERENCE_ROOT, else the container's read-only copy.
+REF_ROOT = os.environ.get("NSP_REFERENCE_ROOT") or "/root/reference"
+REF_SRC_DEFAULT = os.path.join(REF_ROOT, "Main_Code", "src")
+REMESH_SRC_DEFAULT = os.path.join(REF_ROOT, "tools", "Re_Mesh", "src")
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
 # name -> (NR, NT, NZ, LZ expression, Re, dt in code units)
@@ -42,13 +44,16 @@ CONFIGS = {
     "s2": (32, 16, 17, "(2.0*PI2)", 3000.0, 0.005),
     "c0": (48, 32, 65, "(2.0*PI2)", 2000.0, 0.01),
     "c1": (96, 128, 257, "(2.5*PI2)", 5300.0, 0.004),
+    # the turbulent shape with half its time step (0.001 R/U_b): a long run that stays stable
+    "c1h": (96, 128, 257, "(2.5*PI2)", 5300.0, 0.002),
     "c4b": (64, 48, 129, "(2.0*PI2)", 2700.0, 0.006),
     "c4c": (96, 96, 193, "(2.0*PI2)", 3500.0, 0.006),
 }
 
 
-def stage(src=REF_SRC_DEFAULT):
+def stage(src=None):
     """Copy the reference sources next to the build outputs (once, where the reference exists)."""
+    src = src or REF_SRC_DEFAULT
     dst = os.path.join(REF_OUT, "src")
     if not os.path.isdir(src):
         if os.path.isdir(dst):
@@ -180,8 +185,9 @@ def run_exe(exe, fields_dir, rundir):
 
 # ---- the Re_Mesh tool (tools/Re_Mesh/src): mod_remesh.cu + mod_io.cu + remesh_driver.cu
 
-def stage_remesh(src=REMESH_SRC_DEFAULT):
+def stage_remesh(src=None):
     """Copy the Re_Mesh sources to oracle/_ref/remesh_src (once, where the reference exists)."""
+    src = src or REMESH_SRC_DEFAULT
     dst = os.path.join(REF_OUT, "remesh_src")
     if not os.path.isdir(src):
         if os.path.isdir(dst):

@@ -13,8 +13,10 @@
 //                   nonlinear() calls minus one, counted through a linker
 //                   --wrap of nonlinear); writes ur_<s>.bin... after the steps
 //                   s in the comma-separated LIST.
-//   time  N       : build with nsteps=N; times one integrate() call with wall
-//                   clock and cudaDeviceSynchronize on both sides.
+//   time  N       : build with nsteps=N; one untimed integrate() call (module
+//                   loading, cuFFT/cuBLAS first use), the initial field put back,
+//                   then one integrate() call timed with wall clock and
+//                   cudaDeviceSynchronize on both sides.
 #include "head.h"
 #include <chrono>
 #include <cstring>
@@ -70,6 +72,16 @@ int main(int argc, const char* argv[]) {
     }
     fclose(f);
   } else {
+    // warm-up: the same integrate() call once, untimed, from a saved copy of u
+    vfield u0;
+    CHECK_CUDART(cudaMalloc(&u0.r, sz)); CHECK_CUDART(cudaMalloc(&u0.t, sz)); CHECK_CUDART(cudaMalloc(&u0.z, sz));
+    CHECK_CUDART(cudaMemcpy(u0.r, u.r, sz, cudaMemcpyDeviceToDevice));
+    CHECK_CUDART(cudaMemcpy(u0.t, u.t, sz, cudaMemcpyDeviceToDevice));
+    CHECK_CUDART(cudaMemcpy(u0.z, u.z, sz, cudaMemcpyDeviceToDevice));
+    integrate(u, rhs);
+    CHECK_CUDART(cudaMemcpy(u.r, u0.r, sz, cudaMemcpyDeviceToDevice));
+    CHECK_CUDART(cudaMemcpy(u.t, u0.t, sz, cudaMemcpyDeviceToDevice));
+    CHECK_CUDART(cudaMemcpy(u.z, u0.z, sz, cudaMemcpyDeviceToDevice));
     CHECK_CUDART(cudaDeviceSynchronize());
     long c0 = g_nl_calls;
     auto t0 = std::chrono::steady_clock::now();

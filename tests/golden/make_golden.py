@@ -10,7 +10,8 @@ in 'trace' mode (one integrate() call per step, corrector iteration counts
 recorded) and reduces the snapshots it writes to fixtures:
 
   * small configurations (s1, s2): full spectral fields at selected steps;
-  * c0 (NR=48, 32x64 modes) and c1 (NR=96, 128x256 modes): the low-mode block
+  * c0 (NR=48, 32x64 modes), c1 and c1h (NR=96, 128x256 modes; c1h with half
+    c1's time step, 500 steps), c4b (NR=64, 48x128) and c4c (NR=96, 96x192): the low-mode block
     |m| <= 4, l <= 5 at every radius, the mean profile u_z(0,0,r), the per-
     component L2 norms and 8 seeded random projections of every component
     (a checksum of the whole field).
@@ -49,6 +50,11 @@ RUNS = {
     "s2": (0.1, 12, 20, [1, 10, 20], True),
     "c0": (1e-3, 2000, 100, [1, 10, 50, 100], False),
     "c1": (0.1, 5300, 100, [1, 10, 50, 100], False),
+    "c1h": (0.1, 5300, 500, [1, 10, 50, 100, 200, 300, 400, 500], False),
+    # one member of each larger group of the uneven mixed batch (NR=64 x 48 x 128 modes,
+    # NR=96 x 96 x 192 modes; dt = 0.003 R/U_b, amplitude 0.05)
+    "c4b": (0.05, 4100, 100, [1, 10, 50, 100], False),
+    "c4c": (0.05, 4200, 100, [1, 10, 50, 100], False),
 }
 N_PROJ = 8
 

@@ -31,8 +31,9 @@ def test_reference_main_links_against_shim(tmp_path, monkeypatch):
 
 
 def test_integration_example_compiles(tmp_path):
-    """The hand-written binding shown in INTEGRATION.md compiles against the reference's
-    head.h (its macros share the C ABI's field names; the example shows the way round)."""
+    """The hand-written integrate() replacement in the integration notes (the ```cpp block
+    that defines integrate_gb300(vfield u)) compiles against the reference's head.h: its
+    macros share the C ABI's field names, and the example shows the way round them."""
     import re
     import subprocess
     if not os.path.exists(os.path.join(SRC, "head.h")):
