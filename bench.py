@@ -11,11 +11,14 @@ iterations to tol = 5e-8 as in the reference.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--precision mixed|fp64]
     python bench.py --impl reference ...   # the reference nsPipe-CUDA build, same workload
-    python bench.py --workload uneven      # supplementary: 28 pipes of three resolutions, mixed
+    python bench.py --workload uneven      # the uneven batch alone: 28 pipes of three resolutions, mixed
 
-Under torchrun each rank (one GPU) advances its own 64-member ensemble (weak
-scaling, no data-path collective); timing is bracketed by a barrier and
-synchronisation and the max over ranks is taken.  Rank 0 prints one JSON line.
+The headline line also carries the plain FP64 form on the same ensemble (device-timed
+and end to end) and the uneven batch as sub-objects.  Under torchrun each rank (one
+GPU) advances its own 64-member ensemble (weak scaling, no data-path collective), or
+with --split its shard of one 64-member ensemble (strong scaling); timing is bracketed
+by a barrier and synchronisation and the max over ranks is taken.  Rank 0 prints one
+JSON line.
 """
 import argparse
 import json
@@ -184,15 +187,19 @@ UNEVEN = [  # (members, NR, NT, NZ, Re low, Re high): 32x64, 48x128, 96x192 mode
 UNEVEN_DT, UNEVEN_AMP = 0.006, 0.05  # dt = 0.003 R/U_b
 
 
-def run_uneven(args):
+UNEVEN_WORKLOAD = ("uneven batch: 16 pipes NR=48 x 32 x 64 modes (Re 2000-2400), 8 NR=64 x 48 x 128 (Re 2400-3000), "
+                   "4 NR=96 x 96 x 192 (Re 3000-4000); dt=0.003R/U_b, L=4piR, amplitude 0.05")
+
+
+def measure_uneven(args, device=0, barrier=None, max_over_ranks=None):
     """Mixed-precision uneven batch: 28 pipes of three resolutions with Re spread
     within each; member-steps/s and ns/(step.dof) over the whole batch, the plain
     FP64 form on the same batch, and the execution choices (one group per shape,
-    one operator set per Re, groups as parallel graph branches)."""
-    import numpy as np
+    one operator set per Re, groups as parallel graph branches).  Returns a dict."""
     import torch
     import nspipe_gb300 as nsp
-    torch.cuda.set_device(0)
+    barrier = barrier or torch.cuda.synchronize
+    max_over_ranks = max_over_ranks or (lambda x: x)
     prm, fields, dof = [], [], 0
     k = 0
     for n, nr, nt, nz, lo, hi in UNEVEN:
@@ -205,7 +212,7 @@ def run_uneven(args):
 
     def timed(precision):
         t_setup = time.perf_counter()
-        st = nsp.Stepper(prm, precision=precision)  # operator tables of 28 parameter sets, autotune, graph
+        st = nsp.Stepper(prm, precision=precision, device=device)  # 28 parameter sets, autotune, graph
         t_setup = time.perf_counter() - t_setup
         for m, f in enumerate(fields):
             st.set_state(m, f)
@@ -213,17 +220,17 @@ def run_uneven(args):
         stream = torch.cuda.Stream()
         st.set_stream(stream.cuda_stream)
         st.step(args.warmup, check=False)
-        torch.cuda.synchronize()
+        barrier()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with ClockSampler(0) as clk:
+        with ClockSampler(device) as clk:
             with torch.cuda.stream(stream):
                 e0.record(stream)
                 iters = st.step(args.steps, check=False)
                 e1.record(stream)
-            torch.cuda.synchronize()
-        sec = e0.elapsed_time(e1) / 1e3
+            barrier()
+        sec = max_over_ranks(e0.elapsed_time(e1) / 1e3)
         launches = st.kernel_launches()
-        finite = all(d.status == 0 for d in (st.diag(m) for m in range(len(prm))))
+        finite = all(d.status == 0 for d in st.diag_all())
         st.set_stream(0)
         st.close()
         desc["setup_seconds"] = round(t_setup, 3)
@@ -231,20 +238,33 @@ def run_uneven(args):
 
     sec, iters, clocks, desc, launches, finite = timed(nsp.NSP_MIXED)
     n = len(prm)
-    value = n * args.steps / sec
-    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
-           "ms_per_step": 1e3 * sec / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": "f64+f32", "data": "synthetic: seeded divergence-free perturbations of Hagen-Poiseuille flow",
-           "config": {"workload": "uneven batch: 16 pipes NR=48 x 32 x 64 modes (Re 2000-2400), 8 NR=64 x 48 x 128 "
-                                  "(Re 2400-3000), 4 NR=96 x 96 x 192 (Re 3000-4000); dt=0.003R/U_b, L=4piR, "
-                                  "amplitude 0.05", "members_per_gpu": n, "precision": "mixed", "execution": desc},
+    out = {"value": n * args.steps / sec, "unit": UNIT, "ms_per_step": 1e3 * sec / args.steps,
            "ns_per_step_dof": 1e9 * sec / args.steps / dof, "iters_mean": float(iters.mean()),
-           "gpu_launches": int(launches), "clocks": clocks, "all_members_finite": finite}
+           "gpu_launches": int(launches), "clocks": clocks, "all_members_finite": finite,
+           "members": n, "workload": UNEVEN_WORKLOAD, "execution": desc}
     if not args.no_fp64_compare:
         sec64, it64, _, _, _, fin64 = timed(nsp.NSP_FP64)
         out["fp64_form"] = {"value": n * args.steps / sec64, "unit": UNIT, "ms_per_step": 1e3 * sec64 / args.steps,
                             "iters_mean": float(it64.mean()), "mixed_over_fp64": sec64 / sec,
                             "all_members_finite": fin64}
+    return out
+
+
+def run_uneven(args):
+    """The uneven batch as its own JSON line (--workload uneven)."""
+    import torch
+    torch.cuda.set_device(0)
+    u = measure_uneven(args)
+    out = {"metric": METRIC, "value": u["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": u["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64+f32",
+           "data": "synthetic: seeded divergence-free perturbations of Hagen-Poiseuille flow",
+           "config": {"workload": UNEVEN_WORKLOAD, "members_per_gpu": u["members"], "precision": "mixed",
+                      "execution": u["execution"]},
+           "ns_per_step_dof": u["ns_per_step_dof"], "iters_mean": u["iters_mean"], "gpu_launches": u["gpu_launches"],
+           "clocks": u["clocks"], "all_members_finite": u["all_members_finite"]}
+    if "fp64_form" in u:
+        out["fp64_form"] = u["fp64_form"]
     print(json.dumps(out))
     return 0
 
@@ -262,6 +282,10 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", default="ensemble", choices=["ensemble", "uneven"],
                     help="ensemble: the headline 64-member workload; uneven: the mixed three-resolution batch")
+    ap.add_argument("--split", action="store_true",
+                    help="strong scaling: shard one ensemble of --members pipes across the ranks "
+                         "(default: every rank advances its own --members pipes, weak scaling)")
+    ap.add_argument("--no-uneven", action="store_true", help="skip the uneven-batch sub-measurement")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
@@ -295,9 +319,16 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
-    M = args.members
     prec = nsp.NSP_MIXED if args.precision == "mixed" else nsp.NSP_FP64
-    fields = [member_fields(rank * M + m) for m in range(M)]
+    if args.split:  # one fixed ensemble, partitioned: this rank owns members [lo, hi)
+        from nspipe_gb300.ensemble import shard
+        lo, hi = shard(args.members, world, rank)
+        total_members = args.members
+    else:  # every rank its own ensemble of --members pipes
+        lo, hi = rank * args.members, (rank + 1) * args.members
+        total_members = args.members * world
+    M = hi - lo
+    fields = [member_fields(m) for m in range(lo, hi)]
 
     def make(precision):
         st = nsp.Stepper([nsp.make_params(NR, NT, NZ, RE, DT, LZ) for _ in range(M)], precision=precision, device=local)
@@ -329,7 +360,7 @@ def main():
     sec, iters, clocks = device_timed(st, args.steps, args.warmup)
     launches = st.kernel_launches()
     sec_max = max_over_ranks(sec)
-    total_member_steps = M * args.steps * world
+    total_member_steps = total_members * args.steps
     value = total_member_steps / sec_max
 
     # Roofline of the dominant kernel: CUDA-event timing of standalone launches.
@@ -375,7 +406,32 @@ def main():
         roofline["fp64"] = {"achieved_tflops": ach, "peak_tflops": fp64_peak, "frac": ach / fp64_peak,
                             "algorithmic_flops_per_launch": fl, "peak_source": "measured live (nsp_measure_fp64_peak)"}
 
-    # Plain FP64 form on the same ensemble (the metric's comparison).
+    # End to end through the C ABI with host buffers: every step is one nsp_step_host
+    # call -- H2D of all members' state from pinned memory, one step, D2H of all
+    # members' state into pinned memory (the members in chunks, so that the copies of
+    # one chunk overlap the compute of the others).  Wall clock, max over ranks.
+    def pinned(n):
+        return torch.zeros(n, dtype=torch.complex128).pin_memory().numpy()
+
+    def e2e_timed(stp):
+        host_in, host_out = pinned(3 * M * S), pinned(3 * M * S)  # member-major: u_r, u_t, u_z per member
+        host_in[:] = stp.pack(fields)
+        for _ in range(args.warmup):
+            stp.step_host(1, host_in, out=host_out)
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            stp.step_host(1, host_in, out=host_out)
+            host_in, host_out = host_out, host_in
+        barrier()
+        e2e_sec = max_over_ranks(time.perf_counter() - t0)
+        return {"value": total_member_steps / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": M * 3 * S * 16,
+                "d2h_bytes_per_step": M * 3 * S * 16}
+
+    e2e = e2e_timed(st)
+
+    # Plain FP64 form on the same ensemble (the metric's comparison; the drop-in form),
+    # device-timed and end to end.
     fp64 = None
     if prec == nsp.NSP_MIXED and not args.no_fp64_compare:
         st64 = make(nsp.NSP_FP64)
@@ -383,48 +439,41 @@ def main():
         sec64 = max_over_ranks(sec64)
         v64 = total_member_steps / sec64
         fp64 = {"value": v64, "unit": UNIT, "ms_per_step": 1e3 * sec64 / args.steps,
-                "iters_mean": float(it64.mean()), "mixed_over_fp64": value / v64}
+                "ns_per_step_dof": 1e9 * sec64 / args.steps / (total_members * DOF),
+                "iters_mean": float(it64.mean()), "mixed_over_fp64": value / v64, "e2e": e2e_timed(st64)}
         st64.close()
 
-    # End to end through the C ABI with host buffers: every step is one nsp_step_host
-    # call -- H2D of all members' state from pinned memory, one step, D2H of all
-    # members' state into pinned memory (the members in chunks, so that the copies of
-    # one chunk overlap the compute of the others).
-    def pinned(n):
-        return torch.zeros(n, dtype=torch.complex128).pin_memory().numpy()
-    host_in, host_out = pinned(3 * M * S), pinned(3 * M * S)  # member-major: u_r, u_t, u_z per member
-    host_in[:] = st.pack(fields)
-    for _ in range(args.warmup):
-        st.step_host(1, host_in, out=host_out)
-    barrier()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        st.step_host(1, host_in, out=host_out)
-        host_in, host_out = host_out, host_in
-    barrier()
-    e2e_sec = max_over_ranks(time.perf_counter() - t0)
-    e2e = {"value": total_member_steps / e2e_sec, "unit": UNIT, "h2d_bytes_per_step": M * 3 * S * 16,
-           "d2h_bytes_per_step": M * 3 * S * 16}
+    # The uneven mixed batch (three resolutions, Re spread), every rank its own batch.
+    uneven = None
+    if not args.no_uneven:
+        uneven = measure_uneven(args, device=local, barrier=barrier, max_over_ranks=max_over_ranks)
+        if world > 1:
+            uneven["value"] *= world
+            if "fp64_form" in uneven:
+                uneven["fp64_form"]["value"] *= world
 
     out = None
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1e3 * sec_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None,
+            "scaling": "strong" if args.split else "weak", "vs_baseline": None,
             "dtype": "f64+f32" if prec == nsp.NSP_MIXED else "f64",
             "data": "synthetic: seeded divergence-free perturbations of Hagen-Poiseuille flow",
             "config": {"workload": WORKLOAD, "members_per_gpu": M, "precision": args.precision,
-                       "parallelism": "ensemble members sharded per GPU (dp%d), no collective" % world,
+                       "parallelism": ("one ensemble of %d pipes sharded across %d GPUs" % (total_members, world)
+                                       if args.split else "every GPU its own ensemble (dp%d)" % world)
+                                      + ", no collective",
                        "l2": "inputs larger than L2: %.2f GB of member state per GPU" % (M * 9 * S * 16 / 1e9),
                        "execution": describe},
-            "ns_per_step_dof": 1e9 * sec_max / args.steps / (M * world * DOF),
+            "ns_per_step_dof": 1e9 * sec_max / args.steps / (total_members * DOF),
             "iters_mean": float(iters.mean()),
             "gpu_launches": int(launches),
             "clocks": clocks,
             "roofline": roofline,
             "fp64_form": fp64,
             "e2e": e2e,
+            "uneven": uneven,
         }
         if world == 1 and not args.no_cpu_baseline:
             out["cpu_baseline"] = cpu_baseline()

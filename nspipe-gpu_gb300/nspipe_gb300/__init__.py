@@ -312,6 +312,11 @@ class Stepper:
         self._check(lib().nsp_diag(self._h, m, ctypes.byref(d)))
         return d
 
+    def friction(self, m=0):
+        """(u_centre, u_tau) of member m (nsp_diag): the data of the friction file's rows."""
+        d = self.diag(m)
+        return d.u_centre, d.u_tau
+
     def mean_profile(self, m=0):
         """Re u_z(0,0)(r_i), i < NR (the data row of the reference's mean-profile file)."""
         out = np.zeros(self.params[m].NR)
