@@ -113,9 +113,11 @@ static inline int signed_mode(const orc_ctx* c, int it) { return it < c->NT / 2 
 static inline double kt_of(const orc_ctx* c, int m) { return (PI2 / c->p.LT) * (double)m; }
 static inline double kz_of(const orc_ctx* c, int l) { return (PI2 / c->p.LZ) * (double)l; }
 
+/* Each call sets its context's thread count (0: every processor), so that a context
+ * with an explicit count leaves no lasting setting for the others. */
 static void set_threads(const orc_ctx* c) {
 #ifdef _OPENMP
-  if (c->p.nthreads > 0) omp_set_num_threads(c->p.nthreads);
+  omp_set_num_threads(c->p.nthreads > 0 ? c->p.nthreads : omp_get_num_procs());
 #else
   (void)c;
 #endif
