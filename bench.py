@@ -405,6 +405,18 @@ def main():
         roofline["compute_bound"] = "fp64"
         roofline["fp64"] = {"achieved_tflops": ach, "peak_tflops": fp64_peak, "frac": ach / fp64_peak,
                             "algorithmic_flops_per_launch": fl, "peak_source": "measured live (nsp_measure_fp64_peak)"}
+        # The corrector pass.  Mixed form (the increment pass): about 150 FP64 flops per
+        # point (banded solves 104, influence correction 30, update 12; its stencils are
+        # FP32).  FP64 form: 242 (right-hand side 12, divergence 37, pressure solve 26,
+        # gradient and +/- 41, Helmholtz solves 78, correction 30, convergence measure 18).
+        # Bytes: read N, RHSW, V, u_i, write u_{i+1} (15 x 16 per point); mixed, also the
+        # RHSW update (3 x 16) and the FP32 mirror and its d_r (6 x 8).
+        lin = st.profile_linear(5)
+        fl_c = (150.0 if prec == nsp.NSP_MIXED else 242.0) * S * M
+        by_c = M * S * ((18 * 16 + 6 * 8) if prec == nsp.NSP_MIXED else 15 * 16)
+        roofline["corrector"] = {"launch_ms": float(lin[1]), "fp64_frac": fl_c / (lin[1] * 1e-3) / 1e12 / fp64_peak,
+                                 "hbm_frac": by_c / (lin[1] * 1e-3) / 1e9 / peak,
+                                 "algorithmic_flops_per_launch": fl_c, "algorithmic_bytes_per_launch": by_c}
 
     # End to end through the C ABI with host buffers: every step is one nsp_step_host
     # call -- H2D of all members' state from pinned memory, one step, D2H of all

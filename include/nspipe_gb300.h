@@ -217,6 +217,16 @@ int nsp_set_stream(nsp_ctx* ctx, void* stream);
  * The states are those of the non-strict call.  Default 0. */
 int nsp_set_strict(nsp_ctx* ctx, int strict);
 
+/* Bounds record (no reference counterpart; the reference's kernels are unchecked).  The
+ * library built with -DNSP_BOUNDS_CHECK (libnspipe_gb300_bc.so) checks every global
+ * index that its step kernels compute -- state, nonlinear term, right-hand side and
+ * correction slabs, transform intermediates, factor rows, stencil taps -- against the
+ * extent it addresses, skips an access outside it and records it.  out[0] the number
+ * of violations since the context was created, out[1] the first one's check site,
+ * out[2] its index, out[3] the extent, out[4] 1 in the bounds-checked build (0: the
+ * normal build, whose record stays 0).  Synchronises the context's stream. */
+int nsp_bounds_report(nsp_ctx* ctx, long long* out);
+
 /* Measurement hook (no reference counterpart): average device time in ms of one
  * launch of each kernel of the step, over `reps` back-to-back launches timed with
  * CUDA events on the context's stream, every member in corrector mode:
@@ -224,6 +234,13 @@ int nsp_set_strict(nsp_ctx* ctx, int strict);
  * [2] theta-forward transforms, [3] linear predictor/corrector pass, [4] convergence
  * bookkeeping.  The state is preserved; the corrector iterate buffers are overwritten. */
 int nsp_profile_stages(nsp_ctx* ctx, int reps, double* ms_out);
+
+/* Measurement hook (no reference counterpart): average device time in ms of one launch
+ * of the linear pass with every member in its predictor pass (ms_out[0]) and in a
+ * corrector pass (ms_out[1]; the mixed form's increment pass), over `reps` launches
+ * timed with CUDA events on the context's stream.  The state is preserved; the
+ * corrector iterate buffers are overwritten. */
+int nsp_profile_linear(nsp_ctx* ctx, int reps, double* ms_out);
 
 /* Measurement hook (no reference counterpart): FP64 multiply-add throughput of the
  * context's device in TFLOP/s (8 independent chains per thread, no memory traffic,

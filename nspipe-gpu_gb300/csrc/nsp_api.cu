@@ -21,6 +21,7 @@
 #include <tuple>
 #include <vector>
 
+#include "nsp_bounds.cuh"
 #include "nsp_fft.cuh"
 #include "nsp_internal.h"
 
@@ -604,6 +605,11 @@ int nsp_create(const nsp_params* members, int n_members, int precision, int devi
   CK(cudaMemset(h.err, 0, sizeof(double) * n_members));
   if ((rc = dalloc(c, &c->dctl, sizeof(Ctl)))) return rc;
   CK(cudaMemcpy(c->dctl, &h, sizeof(Ctl), cudaMemcpyHostToDevice));
+  // Bounds record of the bounds-checked build (nsp_bounds.cuh), shared by every group.
+  unsigned long long* bc = nullptr;
+  if ((rc = dalloc(c, &bc, 4 * sizeof(unsigned long long)))) return rc;
+  CK(cudaMemset(bc, 0, 4 * sizeof(unsigned long long)));
+  for (auto& g : c->groups) g.tb.bc = bc;
   CK(cudaMallocHost(&c->pin, sizeof(int) * ((size_t)(h.hist_cap + 2) * n_members + 1)));
   return NSP_OK;
 }
@@ -1495,6 +1501,17 @@ int nsp_set_stream(nsp_ctx* c, void* stream) {
   return NSP_OK;
 }
 
+int nsp_bounds_report(nsp_ctx* c, long long* out) {
+  if (!c || !out) return NSP_ERR_ARG;
+  if (c->groups.empty() || !c->groups[0].tb.bc) return fail(c, NSP_ERR_STATE, "no bounds record");
+  unsigned long long rec[4];
+  CK(cudaStreamSynchronize(c->st));
+  CK(cudaMemcpy(rec, c->groups[0].tb.bc, sizeof rec, cudaMemcpyDeviceToHost));
+  for (int k = 0; k < 4; k++) out[k] = (long long)rec[k];
+  out[4] = kBoundsCheck ? 1 : 0;
+  return NSP_OK;
+}
+
 int nsp_set_strict(nsp_ctx* c, int strict) {
   if (!c) return NSP_ERR_ARG;
   c->strict = strict != 0;
@@ -1537,6 +1554,34 @@ int nsp_profile_stages(nsp_ctx* c, int reps, double* ms_out) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   // Restore the step-boundary control state.
+  return reset_control(c);
+}
+
+int nsp_profile_linear(nsp_ctx* c, int reps, double* ms_out) {
+  if (!c || !ms_out || reps < 1) return NSP_ERR_ARG;
+  if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_profile_linear before nsp_setup");
+  CK(cudaSetDevice(c->device));
+  const int nm = c->nmem;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  for (int pass = 0; pass < 2; pass++) {  // 0: every member in its predictor pass, 1: in a corrector pass
+    std::vector<int> ph(nm, pass);
+    CK(cudaMemcpyAsync(c->hctl.phase, ph.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, c->st));
+    const int which = pass ? LIN_CORR : LIN_PRED;
+    for (auto& g : c->groups) launch_linear(g.tb, g.bf, c->dctl, c->st, which);  // warm-up
+    CK(cudaEventRecord(e0, c->st));
+    for (int r = 0; r < reps; r++)
+      for (auto& g : c->groups) launch_linear(g.tb, g.bf, c->dctl, c->st, which);
+    CK(cudaEventRecord(e1, c->st));
+    CK(cudaGetLastError());
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    ms_out[pass] = ms / reps;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
   return reset_control(c);
 }
 

@@ -66,6 +66,7 @@ struct Tables {
   const float* dft_fwd; //   ([hi | lo] x N x K core matrices, nsp_theta_tc.cu)
   int tc_theta;        // 1: the mixed form's theta transforms run as tcgen05 GEMMs
   int nsm;             // SM count (persistent grids)
+  unsigned long long* bc;  // bounds record of the bounds-checked build (nsp_bounds.cuh); unused otherwise
 };
 
 #ifdef __CUDACC__

@@ -19,6 +19,7 @@
 // array, no shared-memory staging), so a block holds 4 radial lines per mode.
 #include <cstdio>
 
+#include "nsp_bounds.cuh"
 #include "nsp_cvt.cuh"
 #include "nsp_fft.cuh"
 #include "nsp_internal.h"
@@ -135,6 +136,7 @@ template <int LM, int NTH, bool INC>
 __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 : (1024 / NTH)))
     linear_k(Tables tb, Bufs bf, Ctl* ctl) {
   const int mloc = blockIdx.y, gm = tb.mem0 + mloc;
+  if (!NSP_IN_BOUNDS(tb, mloc, tb.nmem, BC_LIN_MEMBER) || !NSP_IN_BOUNDS(tb, gm, ctl->nmem, BC_LIN_MEMBER)) return;
   const int ph = ctl->phase[gm];
   if (ph < 0) return;
   if (INC ? ph == 0 : (ph > 0 && bf.U32[0] != nullptr)) return;  // the other kernel's pass
@@ -226,6 +228,10 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       const int lo = (1 - par_m) * STEN * NR + STEN * i + i0;  // u_r, u_theta rows (odd flag)
       const int le = par_m * STEN * NR + STEN * i + i0;        // u_z rows
       const size_t h = (size_t)i * NTNZ + k;
+      if (!NSP_IN_BOUNDS(tb, h, S, BC_LIN_POINT) || !NSP_IN_BOUNDS(tb, lo + len - 1, 2 * STEN * NR, BC_LIN_TAP) ||
+          !NSP_IN_BOUNDS(tb, le + len - 1, 2 * STEN * NR, BC_LIN_TAP) ||
+          !NSP_IN_BOUNDS(tb, (size_t)(left + len - 1) * NTNZ + k, S, BC_LIN_TAP))
+        continue;
       if (Un32 && k != 0) {
         // mixed form: everything but u^n/dt in FP32 on the FP32 mirror of u^n -- the
         // stencil sums and the diagonal terms ((1-d_im)/Re times the Laplacian) and N/2
@@ -305,7 +311,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
 #pragma unroll
       for (int u = 0; u < UB; u++) {
         const int p = pb + u * nth, i = p / LM, k = k0 + p - i * LM;
-        const bool ok = p < LN && k < NTNZ;
+        const bool ok = p < LN && k < NTNZ && NSP_IN_BOUNDS(tb, (size_t)i * NTNZ + k, S, BC_LIN_POINT);
         const size_t h = ok ? (size_t)i * NTNZ + k : 0;
 #pragma unroll
         for (int c = 0; c < 3; c++) {
@@ -317,7 +323,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       for (int u = 0; u < UB; u++) {
         const int p = pb + u * nth, i = p / LM, k = k0 + p - i * LM;
         if (p >= LN) continue;
-        const bool ok = k < NTNZ;
+        const bool ok = k < NTNZ && (!kBoundsCheck || (size_t)i * NTNZ + k < (size_t)S);
         const size_t h = (size_t)i * NTNZ + k;
 #pragma unroll
         for (int c = 0; c < 3; c++) {
@@ -343,7 +349,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
 #pragma unroll
       for (int u = 0; u < U; u++) {
         const int p = pb + u * nth, i = p / LM, k = k0 + p - i * LM;
-        const bool ok = p < LN && k < NTNZ;
+        const bool ok = p < LN && k < NTNZ && NSP_IN_BOUNDS(tb, (size_t)i * NTNZ + k, S, BC_LIN_POINT);
         const size_t h = ok ? (size_t)i * NTNZ + k : 0;
 #pragma unroll
         for (int c = 0; c < 3; c++) {
@@ -409,9 +415,14 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
 
   // D. pressure Poisson solve, one thread per mode.
   // (two threads per mode line: real and imaginary parts; every lane of the warp busy)
+  // The last factor a solve reads of kind c, mode k: row NR-1, entry 6.
+  auto fac_ok = [&](int c, int k) {
+    return NSP_IN_BOUNDS(tb, ((size_t)c * NR + NR - 1) * NFAC * NTNZ + 6 * (size_t)NTNZ + k,
+                         (size_t)4 * NR * NFAC * NTNZ, BC_LIN_FACTOR);
+  };
   if (tid < 2 * LM) {
     const int mm = tid >> 1, part = tid & 1;
-    if (k0 + mm < NTNZ)
+    if (k0 + mm < NTNZ && fac_ok(3, k0 + mm))
       solve_line(reinterpret_cast<double*>(P + mm) + part, 2 * LM, fac + 3 * (size_t)NR * NFAC * NTNZ + k0 + mm,
                  NTNZ, NR);
   }
@@ -473,10 +484,15 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   }
   __syncthreads();
 
-  // F. Helmholtz solves for u+, u-, u_z.
-  if (tid < 6 * LM) {
-    const int c = tid / (2 * LM), rem = tid - c * 2 * LM, mm = rem >> 1, part = rem & 1;
-    if (k0 + mm < NTNZ)
+  // F. Helmholtz solves for u+, u-, u_z, on the warps after the pressure solve's: a
+  // block's four solves then run on four different warps, and so on four different SM
+  // sub-partitions (warp w of a block on sub-partition (base + w) mod 4), each taking its
+  // share of the FP64 pipe.
+  constexpr int F0 = ((2 * LM + 31) / 32) * 32 + 6 * LM <= NTH ? ((2 * LM + 31) / 32) * 32 : 0;
+  if (tid >= F0 && tid < F0 + 6 * LM) {
+    const int tf = tid - F0;
+    const int c = tf / (2 * LM), rem = tf - c * 2 * LM, mm = rem >> 1, part = rem & 1;
+    if (k0 + mm < NTNZ && fac_ok(c, k0 + mm))
       solve_line(reinterpret_cast<double*>(R + c * LN + mm) + part, 2 * LM,
                  fac + (size_t)c * NR * NFAC * NTNZ + k0 + mm, NTNZ, NR);
   }
@@ -518,6 +534,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     double2 up = R[p], um = R[LN + p], uz = R[2 * LN + p];
     double2 dv = dvs[mm];
     size_t hv = (size_t)i * NTNZ + k;
+    if (!NSP_IN_BOUNDS(tb, hv, S, BC_LIN_POINT)) continue;
     double2 v0 = Vp[hv], v1 = Vp[S + hv], v2 = Vp[2 * S + hv];
     up.x += dv.x * v0.x - dv.y * v0.y; up.y += dv.x * v0.y + dv.y * v0.x;
     um.x += dv.x * v1.x - dv.y * v1.y; um.y += dv.x * v1.y + dv.y * v1.x;
@@ -554,7 +571,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
 #pragma unroll
       for (int u = 0; u < UI; u++) {
         const int p = pb + u * nth, i = p / LM, k = k0 + p - i * LM;
-        const bool ok = p < LN && k < NTNZ;
+        const bool ok = p < LN && k < NTNZ && NSP_IN_BOUNDS(tb, (size_t)i * NTNZ + k, S, BC_LIN_POINT);
         const size_t h = ok ? (size_t)i * NTNZ + k : 0;
 #pragma unroll
         for (int c = 0; c < 3; c++) o[u][c] = ok ? Ui[c * S + h] : c2(0, 0);
@@ -565,6 +582,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       const int p = pb + u * nth, i = p / LM, k = k0 + p - i * LM;
       if (p >= LN || k >= NTNZ) continue;
       const size_t h = (size_t)i * NTNZ + k;
+      if (kBoundsCheck && h >= (size_t)S) continue;  // (recorded by the load loop above)
 #pragma unroll
       for (int c = 0; c < 3; c++) {
         double2 v = R[c * LN + p];
@@ -613,6 +631,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       if (k >= NTNZ) continue;
       const int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
       const size_t h = (size_t)i * NTNZ + k;
+      if (!NSP_IN_BOUNDS(tb, h, S, BC_LIN_POINT)) continue;
 #pragma unroll
       for (int c = 0; c < 3; c++) {
         const int tab = abs(spar[mm] - (c < 2 ? 1 : 0));

@@ -86,4 +86,66 @@ __device__ __forceinline__ float2 dr32_line(const float* Dr, int left, int len, 
   return make_float2(vx, vy);
 }
 
+// ---- the mean flow of the mixed form's nonlinear term
+// The mixed form evaluates -(u.grad)u with the mean flow -- W(r) = Re u_theta(m=0,k_z=0)
+// and U(r) = Re u_z(0,0) -- taken out of the transform input, and adds the terms that
+// contain it afterwards, mode by mode.  With u' = u minus that mean flow (the mean u_r,
+// zero after every pass, stays in the transforms), the terms of -(u.grad)u with a factor
+// W, U, W' or U' are, for mode (m, k_z) with a = m W / r + k_z U:
+//   N_r:     -i a u'_r + 2 W u'_theta / r        (+ W^2 / r at mode (0,0))
+//   N_theta: -i a u'_theta - (W' + W / r) u'_r
+//   N_z:     -i a u'_z - U' u'_r
+// (at mode (0,0) u'_theta = u'_z = 0 and u'_r is the mean u_r).  No product of the mean
+// with a retained mode leaves the retained modes, so these are exactly the terms the
+// dealiased transforms would give.  Taking the mean flow out matters because the
+// transforms then carry the perturbation only: a base flow of order 1 over a
+// perturbation of order 1e-3 otherwise sets the transforms' rounding (and the tensor
+// cores' accumulation) at 1e-3 of the perturbation's scale, and the mean mode of N --
+// a sum over theta that cancels to the perturbation's square -- inherits it.
+//
+// True for the transform input fields whose mean mode is taken out: u_theta, u_z and
+// their radial derivatives (fields 1, 2, 4, 5 of the inverse transforms' 9).
+__device__ __forceinline__ bool mean_field(int f) { return f == 1 || f == 2 || f == 4 || f == 5; }
+
+struct Mean32 {
+  float W, U, Wp, Up, rinv;
+};
+// The mean flow at level i of a member's FP32 transform input (U32: its 3 components; DR32:
+// their radial derivatives, or null: the 7-point parity stencil, u_theta odd and u_z even
+// at m = 0).
+__device__ __forceinline__ Mean32 mean_flow32(const Tables& tb, const float2* U32, const float2* DR32, int i) {
+  const long long S = tb.S;
+  const size_t h = (size_t)i * tb.NTNZ;
+  Mean32 o;
+  o.W = U32[S + h].x;
+  o.U = U32[2 * S + h].x;
+  o.rinv = tb.rinv32[i];
+  if (DR32) {
+    o.Wp = DR32[S + h].x;
+    o.Up = DR32[2 * S + h].x;
+  } else {
+    const int NR = tb.NR, left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
+    const size_t NTNZ = tb.NTNZ;
+    o.Wp = dr32_line(tb.D32 + STEN * NR + STEN * i + i0, left, len,
+                     [&](int row) { return U32[S + (size_t)row * NTNZ]; }).x;
+    o.Up = dr32_line(tb.D32 + STEN * i + i0, left, len, [&](int row) { return U32[2 * S + (size_t)row * NTNZ]; }).x;
+  }
+  return o;
+}
+// The mean-flow terms of component c of N at mode (m, l): kt = k_theta m, kz = k_z of l;
+// ur, ut, uz the transform input's values at the mode (ut = uz = 0 at mode (0,0)).
+__device__ __forceinline__ float2 mean_terms32(const Mean32& mf, int c, bool zero_mode, float kt, float kz,
+                                               float2 ur, float2 ut, float2 uz) {
+  const float a = fmaf(kt * mf.W, mf.rinv, kz * mf.U);
+  if (c == 0) {
+    const float w2 = 2.f * mf.W * mf.rinv;
+    float2 v = make_float2(fmaf(a, ur.y, w2 * ut.x), fmaf(-a, ur.x, w2 * ut.y));
+    if (zero_mode) v.x += mf.W * mf.W * mf.rinv;
+    return v;
+  }
+  const float b = c == 1 ? fmaf(mf.W, mf.rinv, mf.Wp) : mf.Up;
+  const float2 q = c == 1 ? ut : uz;
+  return make_float2(fmaf(a, q.y, -b * ur.x), fmaf(-a, q.x, -b * ur.y));
+}
+
 }  // namespace nsp

@@ -38,6 +38,7 @@
 #include <cstring>
 #include <vector>
 
+#include "nsp_bounds.cuh"
 #include "nsp_cvt.cuh"
 #include "nsp_fft.cuh"
 #include "nsp_internal.h"
@@ -140,6 +141,9 @@ template <int NT, int NTP> struct InvJob {
       const int i = g / (9 * NZ), rem = g - i * 9 * NZ, f = rem / NZ, l = rem - f * NZ;
       const int comp = f < 3 ? f : (f < 6 ? f - 3 : f - 6);
       const size_t base = (size_t)comp * S + l;
+      // the largest index this line reads: level min(i + IW, NR - 1), mode NT - 1
+      if (!NSP_IN_BOUNDS(tb, (size_t)min(i + IW, NR - 1) * NTNZ + base + (size_t)(NT - 1) * NZ, 3 * S, BC_THETA_IN))
+        return;
       if (f >= 3 && f < 6 && DR) {  // d_r u from the mirror the linear pass wrote
 #pragma unroll
         for (int j = 0; j < J; j++) {
@@ -182,6 +186,10 @@ template <int NT, int NTP> struct InvJob {
           vy[j] = kt * a.x * ri;
         }
       }
+      if (l == 0 && mq == 0 && mean_field(f)) {  // mode (0,0) = mode_of(0, 0): the mean flow stays out
+        vx[0] = 0.f;
+        vy[0] = 0.f;
+      }
     }
   }
 
@@ -200,7 +208,7 @@ template <int NT, int NTP> struct InvJob {
 
   // A draining warp reads TMEM lanes 32 q.. (its lines) and columns [c0, c0 + nc).
   __device__ static void epilogue(const Tables& tb, const Bufs& bf, const Ctl*, int mloc, int t, const double2*,
-                                  double2*, uint32_t tacc) {
+                                  const float2*, double2*, uint32_t tacc) {
     int q, c0, nc;
     if (!drain_share<N>(threadIdx.x >> 5, &q, &c0, &nc)) return;
     constexpr int CM = drain_max<N>();
@@ -215,6 +223,9 @@ template <int NT, int NTP> struct InvJob {
     const int i = g / (9 * NZ), rem = g - i * 9 * NZ, f = rem / NZ, l = rem - f * NZ;
     cpx<float>* G = reinterpret_cast<cpx<float>*>(bf.G) + (size_t)mloc * 9 * NR * NTP * NZ;
     cpx<float>* Gl = G + (((size_t)f * NR + i) * NTP + (size_t)(c0 / 2)) * NZ + l;
+    if (!NSP_IN_BOUNDS(tb, (((size_t)f * NR + i) * NTP + (size_t)((c0 + nc) / 2 - 1)) * NZ + l,
+                       (size_t)9 * NR * NTP * NZ, BC_THETA_OUT))
+      return;
 #pragma unroll
     for (int j = 0; j < CM / 2; j++)
       if (2 * j < nc) Gl[(size_t)j * NZ] = mk<float>(v[2 * j], v[2 * j + 1]);
@@ -244,7 +255,8 @@ template <int NT, int NTP> struct FwdJob {
     for (int j = 0; j < J; j++) h[j] = mk<float>(0.f, 0.f);
     if (g < columns(tb)) {
       const int c = g / (NR * NZ), rem = g - c * NR * NZ, i = rem / NZ, l = rem - i * NZ;
-      if (l < NZ - 1) {  // H holds the half spectrum l < NZ-1 (padBackward_k drops l = NZ-1)
+      if (l < NZ - 1 && NSP_IN_BOUNDS(tb, (((size_t)c * NR + i) * NTP + NTP - 1) * NZ + l, (size_t)3 * NR * NTP * NZ,
+                                      BC_THETA_IN)) {  // H holds the half spectrum l < NZ-1 (padBackward_k drops l = NZ-1)
         const cpx<float>* H = reinterpret_cast<const cpx<float>*>(bf.H) + (size_t)mloc * 3 * NR * NTP * NZ +
                               ((size_t)c * NR + i) * NTP * NZ + l;
 #pragma unroll
@@ -268,7 +280,7 @@ template <int NT, int NTP> struct FwdJob {
   }
 
   __device__ static void epilogue(const Tables& tb, const Bufs& bf, const Ctl* ctl, int mloc, int t,
-                                  const double2* src, double2* dst, uint32_t tacc) {
+                                  const double2* src, const float2* src32, double2* dst, uint32_t tacc) {
     int q, c0, nc;
     if (!drain_share<N>(threadIdx.x >> 5, &q, &c0, &nc)) return;
     constexpr int CM = drain_max<N>();
@@ -291,11 +303,29 @@ template <int NT, int NTP> struct FwdJob {
       for (int j = 0; j <= IW; j++) dwall += Dw[j] * U[2 * S + (size_t)(NR - 1 - IW + j) * NTNZ].x;
     }
     double2* Nout = (dst ? dst : bf.N + (size_t)mloc * 3 * S) + c * S + (size_t)i * NTNZ + l;
+    if (!NSP_IN_BOUNDS(tb, c * S + (size_t)i * NTNZ + l + (size_t)((c0 + nc) / 2 - 1) * NZ, 3 * S, BC_THETA_OUT))
+      return;
+    // the mean-flow terms (nsp_state.cuh), from the FP32 transform input
+    const float2* U32 = member_input<float>(tb, bf, ctl, mloc, src, src32).p;
+    const Mean32 mf = mean_flow32(tb, U32, member_dr32(tb, bf, ctl, mloc, src), i);
+    const float2* Uq = U32 + (c == 2 ? 2 : 1) * S + (size_t)i * NTNZ + l;  // u_theta (N_r, N_theta) or u_z (N_z)
+    const float2* Ur = U32 + (size_t)i * NTNZ + l;
+    const float kzl = tb.kzs32 * (float)l;
 #pragma unroll
     for (int j = 0; j < CM / 2; j++) {
       if (2 * j >= nc) break;
       const int it = c0 / 2 + j;
-      double2 o = make_double2(f32_to_f64(v[2 * j]), f32_to_f64(v[2 * j + 1]));  // exact, integer pipe
+      float2 w = make_float2(v[2 * j], v[2 * j + 1]);
+      if (it != NT / 2 && l != NZ - 1) {
+        const bool zm = it == 0 && l == 0;
+        const float2 ur = Ur[(size_t)it * NZ], uq = zm ? make_float2(0.f, 0.f) : Uq[(size_t)it * NZ];
+        const float kt = (float)(it < NT / 2 ? it : it - NT) * tb.kts32;
+        const float2 ml = mean_terms32(mf, c, zm, kt, kzl, ur, c < 2 ? uq : make_float2(0.f, 0.f),
+                                       c == 2 ? uq : make_float2(0.f, 0.f));
+        w.x += ml.x;
+        w.y += ml.y;
+      }
+      double2 o = make_double2(f32_to_f64(w.x), f32_to_f64(w.y));  // exact, integer pipe
       if (it == NT / 2 || l == NZ - 1) o = make_double2(0.0, 0.0);  // padBackward_k's dropped modes
       if (c == 2 && it == 0 && l == 0) o.x -= tb.sscal[4 * member_set(tb, mloc) + 1] * dwall;  // 2/Re
       Nout[(size_t)it * NZ] = o;
@@ -390,7 +420,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         drained = j;
       }
       tc::fence_after_sync();
-      if (ok) JOB::epilogue(tb, bf, ctl, prev_m, prev_t, src, dst, tmem + (uint32_t)(((j - 1) & 1) * ACC));
+      if (ok) JOB::epilogue(tb, bf, ctl, prev_m, prev_t, src, src32, dst, tmem + (uint32_t)(((j - 1) & 1) * ACC));
     }
     tc::fence_before_sync();
     __syncthreads();
@@ -406,7 +436,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (wait_batch(issued - 1)) {
       drained = issued;
       tc::fence_after_sync();
-      JOB::epilogue(tb, bf, ctl, prev_m, prev_t, src, dst, tmem + (uint32_t)(((issued - 1) & 1) * ACC));
+      JOB::epilogue(tb, bf, ctl, prev_m, prev_t, src, src32, dst, tmem + (uint32_t)(((issued - 1) & 1) * ACC));
     } else {
       fault = true;
     }

@@ -29,6 +29,7 @@
 #include <cstdio>
 #include <cstdlib>
 
+#include "nsp_bounds.cuh"
 #include "nsp_cvt.cuh"
 #include "nsp_fft.cuh"
 #include "nsp_internal.h"
@@ -90,7 +91,8 @@ __global__ void __launch_bounds__(TTH) nl_theta_inv(Tables tb, Bufs bf, const Ct
     int f = colf[lc];
     int it = (p < NT / 2) ? p : (p >= NT ? p - NT / 2 : -1);
     cpx<T> v = mk<T>(0, 0);
-    if (f >= 0 && it >= 0) {
+    if (f >= 0 && it >= 0 &&
+        NSP_IN_BOUNDS(tb, (size_t)right * NTNZ + (size_t)(f % 3) * S + (size_t)it * NZ + coll[lc], 3 * S, BC_THETA_IN)) {
       int comp = f % 3;
       size_t col = (size_t)comp * S + (size_t)it * NZ + coll[lc];
       if (f < 3) {
@@ -113,6 +115,8 @@ __global__ void __launch_bounds__(TTH) nl_theta_inv(Tables tb, Bufs bf, const Ct
         cpx<T> a = U.ld((size_t)i * NTNZ + col);
         v = mk<T>(-kt * a.y * rinv, kt * a.x * rinv);
       }
+      // mixed form: the mean flow stays out of the transforms (its terms: nl_theta_fwd)
+      if (sizeof(T) == 4 && it == 0 && coll[lc] == 0 && mean_field(f)) v = mk<T>(0, 0);
     }
     buf[idx] = v;
   }
@@ -122,7 +126,9 @@ __global__ void __launch_bounds__(TTH) nl_theta_inv(Tables tb, Bufs bf, const Ct
   for (int idx = threadIdx.x; idx < NTP * LC; idx += TTH) {
     int p = idx / LC, lc = idx % LC;
     int f = colf[lc];
-    if (f >= 0) G[(((size_t)f * NR + i) * NTP + p) * NZ + coll[lc]] = buf[idx];
+    if (f >= 0 && NSP_IN_BOUNDS(tb, (((size_t)f * NR + i) * NTP + p) * NZ + coll[lc], (size_t)9 * NR * NTP * NZ,
+                                BC_THETA_OUT))
+      G[(((size_t)f * NR + i) * NTP + p) * NZ + coll[lc]] = buf[idx];
   }
 }
 
@@ -155,7 +161,8 @@ __global__ void __launch_bounds__(ZTH) nl_z(Tables tb, Bufs bf, const Ctl* ctl, 
       for (int h = 0; h < 2; h++) {
         int fld = 2 * t + h;
         int src = fld < 9 ? fld : fld - 9;  // dz u_c comes from the u_c columns
-        cpx<T> g = G[(((size_t)src * NR + i) * NTP + j) * NZ + qq];
+        const size_t gi = (((size_t)src * NR + i) * NTP + j) * NZ + qq;
+        cpx<T> g = NSP_IN_BOUNDS(tb, gi, (size_t)9 * NR * NTP * NZ, BC_Z_IN) ? G[gi] : mk<T>(0, 0);
         if (fld >= 9) {
           T kz = kzs * (T)qq;
           g = mk<T>(-kz * g.y, kz * g.x);
@@ -214,7 +221,8 @@ __global__ void __launch_bounds__(ZTH) nl_z(Tables tb, Bufs bf, const Ctl* ctl, 
     cpx<T> xq = X[q], xm = X[(NZR - q) % NZR];
     cpx<T> v = takeB ? mk<T>((T)0.5 * (xq.y + xm.y), (T)-0.5 * (xq.x - xm.x))
                      : mk<T>((T)0.5 * (xq.x + xm.x), (T)0.5 * (xq.y - xm.y));
-    H[(((size_t)c * NR + i) * NTP + j) * NZ + q] = v;
+    if (NSP_IN_BOUNDS(tb, (((size_t)c * NR + i) * NTP + j) * NZ + q, (size_t)3 * NR * NTP * NZ, BC_Z_OUT))
+      H[(((size_t)c * NR + i) * NTP + j) * NZ + q] = v;
   }
 }
 
@@ -330,6 +338,7 @@ __global__ void __launch_bounds__(Z2TH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl
     const int fa = 2 * t, fb = 2 * t + 1;  // d_z u_c (fields 9-11) comes from the u_c columns
     const cpx<T>* Ga = Gi + (size_t)(fa < 9 ? fa : fa - 9) * fstride;
     const cpx<T>* Gb = Gi + (size_t)(fb < 9 ? fb : fb - 9) * fstride;
+    if (!NSP_IN_BOUNDS(tb, ((size_t)i * NTP + j0 + r) * NZ + NZ - 1, fstride, BC_Z_IN)) continue;
     cpx<T> x[N2];
 #pragma unroll
     for (int n2 = 0; n2 < N2; n2++) {
@@ -431,14 +440,15 @@ __global__ void __launch_bounds__(Z2TH) nl_z2(Tables tb, Bufs bf, const Ctl* ctl
     const cpx<T> xq = X[q], xm = X[(NZRC - q) % NZRC];
     const cpx<T> v = takeB ? mk<T>((T)0.5 * (xq.y + xm.y), (T)-0.5 * (xq.x - xm.x))
                            : mk<T>((T)0.5 * (xq.x + xm.x), (T)0.5 * (xq.y - xm.y));
-    H[(((size_t)c * NR + i) * NTP + j) * NZ + q] = v;
+    if (NSP_IN_BOUNDS(tb, (((size_t)c * NR + i) * NTP + j) * NZ + q, 3 * fstride, BC_Z_OUT))
+      H[(((size_t)c * NR + i) * NTP + j) * NZ + q] = v;
   }
 }
 
 // ---------------------------------------------------------------- theta forward
 template <typename T, int NTPC>
 __global__ void __launch_bounds__(TTH) nl_theta_fwd(Tables tb, Bufs bf, const Ctl* ctl, const double2* src_override,
-                                                    double2* dst_override) {
+                                                    const float2* src32_override, double2* dst_override) {
   const int mloc = blockIdx.z, i = blockIdx.y, c0 = blockIdx.x * LC;
   bool skip;
   const double2* U = member_source(tb, bf, ctl, mloc, src_override, skip);
@@ -460,7 +470,9 @@ __global__ void __launch_bounds__(TTH) nl_theta_fwd(Tables tb, Bufs bf, const Ct
   for (int idx = threadIdx.x; idx < NTP * LC; idx += TTH) {
     int p = idx / LC, lc = idx % LC;
     int c = colc[lc], l = coll[lc];
-    buf[idx] = (c >= 0 && l < NZ - 1) ? H[(((size_t)c * NR + i) * NTP + p) * NZ + l] : mk<T>(0, 0);
+    const size_t hi = (((size_t)c * NR + i) * NTP + p) * NZ + l;
+    buf[idx] = (c >= 0 && l < NZ - 1 && NSP_IN_BOUNDS(tb, hi, (size_t)3 * NR * NTP * NZ, BC_THETA_IN)) ? H[hi]
+                                                                                                : mk<T>(0, 0);
   }
   __syncthreads();
   theta_fft<T, NTPC>(buf, tb, -1);
@@ -471,6 +483,13 @@ __global__ void __launch_bounds__(TTH) nl_theta_fwd(Tables tb, Bufs bf, const Ct
     for (int j = 0; j <= IW; j++) dwall += Dw[j] * U[2 * S + (size_t)(NR - 1 - IW + j) * NTNZ].x;
   }
   const T scale = tb_inv_norm<T>(tb);
+  // mixed form: the mean-flow terms (nsp_state.cuh), from the FP32 transform input
+  const float2* U32 = nullptr;
+  Mean32 mf{};
+  if constexpr (sizeof(T) == 4) {
+    U32 = member_input<float>(tb, bf, ctl, mloc, src_override, src32_override).p;
+    mf = mean_flow32(tb, U32, member_dr32(tb, bf, ctl, mloc, src_override), i);
+  }
   for (int idx = threadIdx.x; idx < NT * LC; idx += TTH) {
     int it = idx / LC, lc = idx % LC;
     int c = colc[lc], l = coll[lc];
@@ -478,11 +497,26 @@ __global__ void __launch_bounds__(TTH) nl_theta_fwd(Tables tb, Bufs bf, const Ct
     int p = it < NT / 2 ? it : NTP + it - NT;
     cpx<T> b = buf[p * LC + lc];
     double2 v;
-    if (sizeof(T) == 8) v = make_double2((double)b.x * tb.inv_norm, (double)b.y * tb.inv_norm);
-    else v = make_double2(f32_to_f64(b.x * scale), f32_to_f64(b.y * scale));  // exact, integer pipe
+    if constexpr (sizeof(T) == 8) {
+      v = make_double2((double)b.x * tb.inv_norm, (double)b.y * tb.inv_norm);
+    } else {
+      float2 w = make_float2(b.x * scale, b.y * scale);
+      if (it != NT / 2 && l != NZ - 1) {
+        const bool zm = it == 0 && l == 0;
+        const size_t hq = (size_t)i * NTNZ + (size_t)it * NZ + l;
+        const float2 ur = U32[hq], uq = zm ? make_float2(0.f, 0.f) : U32[(c == 2 ? 2 : 1) * S + hq];
+        const float kt = (float)(it < NT / 2 ? it : it - NT) * tb.kts32;
+        const float2 ml = mean_terms32(mf, c, zm, kt, tb.kzs32 * (float)l, ur, c < 2 ? uq : make_float2(0.f, 0.f),
+                                       c == 2 ? uq : make_float2(0.f, 0.f));
+        w.x += ml.x;
+        w.y += ml.y;
+      }
+      v = make_double2(f32_to_f64(w.x), f32_to_f64(w.y));  // exact, integer pipe
+    }
     if (it == NT / 2 || l == NZ - 1) v = make_double2(0.0, 0.0);
     if (c == 2 && it == 0 && l == 0) v.x -= tb.sscal[4 * member_set(tb, mloc) + 1] * dwall;  // 2/Re
-    Nout[c * S + (size_t)i * NTNZ + (size_t)it * NZ + l] = v;
+    if (NSP_IN_BOUNDS(tb, c * S + (size_t)i * NTNZ + (size_t)it * NZ + l, 3 * S, BC_THETA_OUT))
+      Nout[c * S + (size_t)i * NTNZ + (size_t)it * NZ + l] = v;
   }
 }
 
@@ -497,7 +531,7 @@ static void launch_theta(const Tables& tb, const Bufs& bf, Ctl* dctl, const doub
   }
   if (mask & 4) {
     dim3 g((3 * tb.NZ + LC - 1) / LC, tb.NR, nm);
-    nl_theta_fwd<T, NTPC><<<g, TTH, sm, st>>>(tb, bf, dctl, src, dst);
+    nl_theta_fwd<T, NTPC><<<g, TTH, sm, st>>>(tb, bf, dctl, src, src32, dst);
   }
 }
 
@@ -668,6 +702,7 @@ __global__ void __launch_bounds__(MIR_T) mirror_k(Tables tb, const double2* __re
     __syncthreads();  // the previous line's tile has been read
     if (k < NTNZ)
       for (int r = lo + ry; r < hi; r += RY) {
+        if (!NSP_IN_BOUNDS(tb, base + (size_t)r * NTNZ + k, (size_t)3 * tb.nmem * tb.S, BC_MIRROR)) break;
         const double2 a = U[base + (size_t)r * NTNZ + k];
         tile[(r - lo) * MIR_K + kx] = make_float2(f64_to_f32(a.x), f64_to_f32(a.y));
       }
@@ -676,6 +711,7 @@ __global__ void __launch_bounds__(MIR_T) mirror_k(Tables tb, const double2* __re
     const int tab = abs(par_m - (line % 3 < 2 ? 1 : 0));
     for (int i = r0 + ry; i < r1; i += RY) {
       const size_t h = base + (size_t)i * NTNZ + k;
+      if (!NSP_IN_BOUNDS(tb, h, (size_t)3 * tb.nmem * tb.S, BC_MIRROR)) break;
       U32[h] = tile[(i - lo) * MIR_K + kx];
       const int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
       const float* Dr = tb.D32 + tab * STEN * NR + STEN * i + i0;

@@ -15,7 +15,9 @@ import numpy as np
 from .initfield import PI2, radial_grid, read_state, seeded_field, write_state  # noqa: F401
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(os.path.dirname(_HERE), "libnspipe_gb300.so")
+# $NSP_LIBRARY selects another build of the library, e.g. the bounds-checked
+# libnspipe_gb300_bc.so (nspipe-gpu_gb300/build.py --bounds-check).
+LIB_PATH = os.environ.get("NSP_LIBRARY") or os.path.join(os.path.dirname(_HERE), "libnspipe_gb300.so")
 
 (NSP_OK, NSP_ERR_ARG, NSP_ERR_CUDA, NSP_ERR_IO, NSP_ERR_NONFINITE, NSP_ERR_STATE, NSP_ERR_NOMEM, NSP_ERR_DEVICE,
  NSP_ERR_MAXIT) = range(9)
@@ -31,7 +33,7 @@ EXPORTS = [
     "nsp_run_checkpoint", "nsp_run_time", "nsp_run_close", "nsp_checkpoint_info", "nsp_output_schedule",
     "nsp_remesh_create", "nsp_remesh_matrix", "nsp_remesh_device", "nsp_remesh_members", "nsp_remesh_files",
     "nsp_remesh_destroy", "nsp_step_host", "nsp_diag_all", "nsp_mean_profile_all", "nsp_cross_sections_all",
-    "nsp_debug_inject", "nsp_set_strict",
+    "nsp_debug_inject", "nsp_set_strict", "nsp_profile_linear", "nsp_bounds_report",
 ]
 
 
@@ -77,7 +79,7 @@ def lib():
     global _LIB
     if _LIB is None:
         if not os.path.exists(LIB_PATH):
-            raise ImportError("libnspipe_gb300.so not found at %s: run nspipe-gpu_gb300/build.py" % LIB_PATH)
+            raise ImportError("%s not found: run nspipe-gpu_gb300/build.py" % LIB_PATH)
         L = ctypes.CDLL(LIB_PATH)
         vp, ip, dp = ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)
         L.nsp_default_params.argtypes = [ctypes.POINTER(NspParams)]
@@ -127,6 +129,8 @@ def lib():
         L.nsp_remesh_destroy.argtypes = [vp]
         L.nsp_debug_inject.argtypes = [vp, ip]
         L.nsp_set_strict.argtypes = [vp, ip]
+        L.nsp_profile_linear.argtypes = [vp, ip, dp]
+        L.nsp_bounds_report.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
         L.nsp_last_error.argtypes = [vp]
         L.nsp_last_error.restype = ctypes.c_char_p
         L.nsp_destroy.argtypes = [vp]
@@ -368,11 +372,23 @@ class Stepper:
         self._check(lib().nsp_profile_stages(self._h, reps, _dp(ms)))
         return ms
 
+    def profile_linear(self, reps=5):
+        """Average ms per launch of the linear pass: [predictor pass, corrector pass]."""
+        ms = np.zeros(2)
+        self._check(lib().nsp_profile_linear(self._h, reps, _dp(ms)))
+        return ms
+
     def fp64_peak_tflops(self):
         """Measured FP64 multiply-add throughput of the device (TFLOP/s)."""
         t = ctypes.c_double()
         self._check(lib().nsp_measure_fp64_peak(self._h, ctypes.byref(t)))
         return t.value
+
+    def bounds_report(self):
+        """(violations, first site, its index, its extent, bounds-checked build?) of nsp_bounds_report."""
+        out = (ctypes.c_longlong * 5)()
+        self._check(lib().nsp_bounds_report(self._h, out))
+        return tuple(out)
 
     def set_strict(self, strict=True):
         """Strict convergence: steps that stop at maxit with err > tol raise NSP_ERR_MAXIT."""
