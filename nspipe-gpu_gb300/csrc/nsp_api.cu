@@ -206,6 +206,7 @@ void range_view(const Group& g, bool mixed, int a, int b, Tables* t, Bufs* bf) {
   const size_t plane = (size_t)g.tb.NR * g.tb.NTP * g.tb.NZ * esz;
   bf->G = static_cast<char*>(g.bf.G) + (size_t)a * 9 * plane;
   bf->H = static_cast<char*>(g.bf.H) + (size_t)a * 3 * plane;
+  if (g.bf.MEAN) bf->MEAN = g.bf.MEAN + (size_t)a * g.tb.NR * MEAN_N;
 }
 
 int check_params(nsp_ctx* c, const nsp_params& p, int idx) {
@@ -569,7 +570,10 @@ int nsp_create(const nsp_params* members, int n_members, int precision, int devi
     CK(cudaMemset(g.bf.RHSW, 0, S3 * sizeof(double2)));
     g.bf.U32[0] = g.bf.U32[1] = nullptr;
     g.bf.DR32[0] = g.bf.DR32[1] = nullptr;
+    g.bf.MEAN = nullptr;
     if (precision == NSP_MIXED) {
+      if ((rc = dalloc(c, &g.bf.MEAN, sizeof(float) * MEAN_N * tb.nmem * (size_t)tb.NR))) return rc;
+      CK(cudaMemset(g.bf.MEAN, 0, sizeof(float) * MEAN_N * tb.nmem * (size_t)tb.NR));
       for (int k = 0; k < 2; k++) {
         if ((rc = dalloc(c, &g.bf.U32[k], S3 * sizeof(float2)))) return rc;
         if ((rc = dalloc(c, &g.bf.DR32[k], S3 * sizeof(float2)))) return rc;

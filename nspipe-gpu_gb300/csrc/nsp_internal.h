@@ -89,7 +89,11 @@ struct Bufs {
   double2* N;          // [nmem][3][S]: nonlinear term output
   void* G;             // [nmem][9][NR][NTP][NZ] complex T: theta-inverse of u, dr u, i m u / r
   void* H;             // [nmem][3][NR][NTP][NZ] complex T: z-forward of the nonlinear product
+  float* MEAN;         // mixed form only: [nmem][NR][MEAN_N] mean flow of the transform input
+                       // (V = Re u_r, W = Re u_theta, U = Re u_z at mode (0,0), W', U'),
+                       // written by the theta-inverse, read by the linear pass
 };
+enum { MEAN_V = 0, MEAN_W, MEAN_U, MEAN_WP, MEAN_UP, MEAN_N };
 
 // Device control block of one context.  phase[m]: 0 = predictor pending,
 // p > 0 = corrector iteration p pending, -1 = converged for this step.

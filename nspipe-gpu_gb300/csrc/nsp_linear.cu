@@ -154,6 +154,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   __shared__ double skt[LM], skz[LM];  // k_theta, k_z of the block's modes
   __shared__ double snkz2[LM], snkt2[LM], shdk[LM];  // -k_z^2, -k_theta^2, -c_ex k_theta (predictor)
   __shared__ int spar[LM];             // |m| mod 2 (selects the parity tables)
+  __shared__ bool sdrop[LM];           // theta Nyquist slot or l = NZ-1: modes the transforms drop
   __shared__ float skt32[LM], skz32[LM];  // k_theta, k_z in FP32 (increment passes)
   __shared__ float snkz2_32[LM], snkt2_32[LM], shdk32[LM];  // FP32 copies (mixed predictor)
   __shared__ int bad;
@@ -183,6 +184,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     skt[tid] = kt;
     skz[tid] = kz;
     spar[tid] = abs(m) % 2;
+    sdrop[tid] = it == NT / 2 || l == NZ - 1;
     snkz2[tid] = -kz * kz;
     snkt2[tid] = -kt * kt;
     shdk[tid] = -(0.5 * c_ex) * (2.0 * kt);
@@ -250,6 +252,14 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
         const float ri = tb.rinv32[i], ir2f = ri * ri, hcf = f64_to_f32(hc);
         const float basef = fmaf(snkt2_32[mm], ir2f, snkz2_32[mm]);  // -k_z^2 - k_theta^2 / r^2
         const float hzf = hcf * basef, hsf = hcf * (basef - ir2f), hdf = shdk32[mm] * ir2f;
+        // N(u^n) in FP32 (the transforms' values are exact in FP32) plus the mean-flow terms
+        // (nsp_state.cuh), from the same FP32 values of u^n the explicit stencil uses
+        float2 nf[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          const double2 n = Nn[c * S + h];
+          nf[c] = make_float2(f64_to_f32(n.x), f64_to_f32(n.y));
+        }
         {
           const float2 fur = __ldg(Un32 + h), fut = __ldg(Un32 + S + h), fuz = __ldg(Un32 + 2 * S + h);
           fr.x += fmaf(hsf, fur.x, -hdf * fut.y);
@@ -258,14 +268,23 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
           ft.y += fmaf(hsf, fut.y, -hdf * fur.x);
           fz.x += hzf * fuz.x;
           fz.y += hzf * fuz.y;
+          if (!sdrop[mm]) {
+            const Mean32 mf = mean_flow32_rec(tb, bf.MEAN + (size_t)mloc * NR * MEAN_N, i);
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+              const float2 ml = mean_terms32(mf, c, false, skt32[mm], skz32[mm], fur, fut, fuz);
+              nf[c].x += ml.x;
+              nf[c].y += ml.y;
+            }
+          }
         }
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-          const double2 n = Nn[c * S + h], u = Un[c * S + h];
-          Rw[c * S + h] = n;  // N(u^n) for the first increment pass
+          Rw[c * S + h] = c2(f32_to_f64(nf[c].x), f32_to_f64(nf[c].y));  // full N(u^n) for the first increment pass
           const float2 f = c == 0 ? fr : (c == 1 ? ft : fz);
-          const float gx = fmaf(0.5f, f64_to_f32(n.x), f.x), gy = fmaf(0.5f, f64_to_f32(n.y), f.y);
+          const float gx = fmaf(0.5f, nf[c].x, f.x), gy = fmaf(0.5f, nf[c].y, f.y);
           // widening on the integer pipe (the hardware conversion issues on the FP64 pipe)
+          const double2 u = Un[c * S + h];
           R[c * LN + p] = c2(fma(hidt, u.x, f32_to_f64(gx)), fma(hidt, u.y, f32_to_f64(gy)));
         }
         continue;
@@ -289,7 +308,15 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       double2 er = c2(lr.x + hs * ur.x - hd * ut.y, lr.y + hs * ur.y + hd * ut.x);
       double2 et = c2(lt.x + hs * ut.x + hd * ur.y, lt.y + hs * ut.y - hd * ur.x);
       double2 ez = c2(lz.x + hz * uz.x, lz.y + hz * uz.y);
-      const double2 nr = Nn[h], nt = Nn[S + h], nz = Nn[2 * S + h];
+      double2 nr = Nn[h], nt = Nn[S + h], nz = Nn[2 * S + h];
+      if (Un32) {  // mixed form, mode (0,0): the mean flow's own terms (nsp_state.cuh)
+        const float* mean = bf.MEAN + (size_t)mloc * NR * MEAN_N;
+        const Mean32 mf = mean_flow32_rec(tb, mean, i);
+        const float2 vr = make_float2(mean[(size_t)i * MEAN_N + MEAN_V], 0.f), zero = make_float2(0.f, 0.f);
+        nr.x = f32_to_f64(f64_to_f32(nr.x) + mean_terms32(mf, 0, true, 0.f, 0.f, vr, zero, zero).x);
+        nt.x = f32_to_f64(f64_to_f32(nt.x) + mean_terms32(mf, 1, true, 0.f, 0.f, vr, zero, zero).x);
+        nz.x += (double)mean_terms32(mf, 2, true, 0.f, 0.f, vr, zero, zero).x;  // (nz: FP64 wall forcing)
+      }
       R[p] = c2(0.5 * nr.x + er.x, 0.5 * nr.y + er.y);
       R[LN + p] = c2(0.5 * nt.x + et.x, 0.5 * nt.y + et.y);
       R[2 * LN + p] = c2(0.5 * nz.x + ez.x, 0.5 * nz.y + ez.y);
@@ -304,8 +331,12 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   } else if constexpr (INC) {
     // B'. N_i - N_{i-1} in FP32 (the FP32 transforms' values are exact in FP32; the
     // u_z line of mode (0,0) carries the FP64 wall forcing, so its difference is taken
-    // in FP64), into the FP32 halves of the line slots; RHSW takes N_i.
-    constexpr int UB = 2;  // points per thread whose loads are issued together (RHSW is also stored)
+    // in FP64), into the FP32 halves of the line slots; RHSW takes N_i.  N_i is the
+    // transforms' output plus the mean-flow terms (nsp_state.cuh), from u_i's FP32 mirror
+    // -- the transforms' input, at this block's own points -- and the mean flow the
+    // theta-inverse recorded.
+    constexpr int UB = 1;  // points per thread whose loads are issued together (2 spills registers here)
+    const float* mean = bf.MEAN + (size_t)mloc * NR * MEAN_N;
     for (int pb = tid; pb < LN; pb += UB * nth) {
       double2 n[UB][3], q[UB][3];
 #pragma unroll
@@ -321,19 +352,30 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       }
 #pragma unroll
       for (int u = 0; u < UB; u++) {
-        const int p = pb + u * nth, i = p / LM, k = k0 + p - i * LM;
+        const int p = pb + u * nth, i = p / LM, mm = p - i * LM, k = k0 + mm;
         if (p >= LN) continue;
         const bool ok = k < NTNZ && (!kBoundsCheck || (size_t)i * NTNZ + k < (size_t)S);
         const size_t h = (size_t)i * NTNZ + k;
+        float2 ml[3] = {};
+        if (ok && !sdrop[mm]) {
+          const Mean32 mf = mean_flow32_rec(tb, mean, i);
+          const float2 zero = make_float2(0.f, 0.f);
+          const float2 wr = k == 0 ? make_float2(mean[(size_t)i * MEAN_N + MEAN_V], 0.f) : Ui32[h];
+          const float2 wt = k == 0 ? zero : Ui32[S + h], wz = k == 0 ? zero : Ui32[2 * S + h];
+#pragma unroll
+          for (int c = 0; c < 3; c++) ml[c] = mean_terms32(mf, c, k == 0, skt32[mm], skz32[mm], wr, wt, wz);
+        }
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-          if (ok) Rw[c * S + h] = n[u][c];
           float2 d;
           if (c == 2 && k == 0) {
-            d = make_float2(f64_to_f32(n[u][c].x - q[u][c].x), f64_to_f32(n[u][c].y - q[u][c].y));
+            const double2 nf = c2(n[u][c].x + (double)ml[c].x, n[u][c].y);
+            if (ok) Rw[c * S + h] = nf;
+            d = make_float2(f64_to_f32(nf.x - q[u][c].x), f64_to_f32(nf.y - q[u][c].y));
           } else {
-            d = make_float2(f64_to_f32(n[u][c].x) - f64_to_f32(q[u][c].x),
-                            f64_to_f32(n[u][c].y) - f64_to_f32(q[u][c].y));
+            const float nx = f64_to_f32(n[u][c].x) + ml[c].x, ny = f64_to_f32(n[u][c].y) + ml[c].y;
+            if (ok) Rw[c * S + h] = c2(f32_to_f64(nx), f32_to_f64(ny));
+            d = make_float2(nx - f64_to_f32(q[u][c].x), ny - f64_to_f32(q[u][c].y));
           }
           f32slot(R, c * LN + p) = d;  // zero where k >= NTNZ
         }

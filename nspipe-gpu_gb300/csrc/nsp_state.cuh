@@ -113,6 +113,17 @@ struct Mean32 {
 // The mean flow at level i of a member's FP32 transform input (U32: its 3 components; DR32:
 // their radial derivatives, or null: the 7-point parity stencil, u_theta odd and u_z even
 // at m = 0).
+// The mean flow at level i as the theta-inverse recorded it (Bufs::MEAN of a member: NR rows).
+__device__ __forceinline__ Mean32 mean_flow32_rec(const Tables& tb, const float* mean, int i) {
+  const float* m = mean + (size_t)i * MEAN_N;
+  Mean32 o;
+  o.W = m[MEAN_W];
+  o.U = m[MEAN_U];
+  o.Wp = m[MEAN_WP];
+  o.Up = m[MEAN_UP];
+  o.rinv = tb.rinv32[i];
+  return o;
+}
 __device__ __forceinline__ Mean32 mean_flow32(const Tables& tb, const float2* U32, const float2* DR32, int i) {
   const long long S = tb.S;
   const size_t h = (size_t)i * tb.NTNZ;
@@ -133,9 +144,11 @@ __device__ __forceinline__ Mean32 mean_flow32(const Tables& tb, const float2* U3
   return o;
 }
 // The mean-flow terms of component c of N at mode (m, l): kt = k_theta m, kz = k_z of l;
-// ur, ut, uz the transform input's values at the mode (ut = uz = 0 at mode (0,0)).
+// ur, ut, uz the transform input's values at the mode (ut = uz = 0 at mode (0,0), where
+// only the real part of u_r -- the mean radial velocity the transforms see -- counts).
 __device__ __forceinline__ float2 mean_terms32(const Mean32& mf, int c, bool zero_mode, float kt, float kz,
                                                float2 ur, float2 ut, float2 uz) {
+  if (zero_mode) ur.y = 0.f;
   const float a = fmaf(kt * mf.W, mf.rinv, kz * mf.U);
   if (c == 0) {
     const float w2 = 2.f * mf.W * mf.rinv;

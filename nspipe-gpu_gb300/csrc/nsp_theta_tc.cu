@@ -186,9 +186,15 @@ template <int NT, int NTP> struct InvJob {
           vy[j] = kt * a.x * ri;
         }
       }
-      if (l == 0 && mq == 0 && mean_field(f)) {  // mode (0,0) = mode_of(0, 0): the mean flow stays out
-        vx[0] = 0.f;
-        vy[0] = 0.f;
+      if (l == 0 && mq == 0) {  // mode (0,0) = mode_of(0, 0): the mean flow
+        // recorded for the linear pass, which adds its terms (member steps; an explicit
+        // field's terms are added by the forward transform) ...
+        const int slot = f == 0 ? MEAN_V : f == 1 ? MEAN_W : f == 2 ? MEAN_U : f == 4 ? MEAN_WP : f == 5 ? MEAN_UP : -1;
+        if (!src && slot >= 0) bf.MEAN[((size_t)mloc * NR + i) * MEAN_N + slot] = vx[0];
+        if (mean_field(f)) {  // ... and kept out of the transforms
+          vx[0] = 0.f;
+          vy[0] = 0.f;
+        }
       }
     }
   }
@@ -305,9 +311,11 @@ template <int NT, int NTP> struct FwdJob {
     double2* Nout = (dst ? dst : bf.N + (size_t)mloc * 3 * S) + c * S + (size_t)i * NTNZ + l;
     if (!NSP_IN_BOUNDS(tb, c * S + (size_t)i * NTNZ + l + (size_t)((c0 + nc) / 2 - 1) * NZ, 3 * S, BC_THETA_OUT))
       return;
-    // the mean-flow terms (nsp_state.cuh), from the FP32 transform input
-    const float2* U32 = member_input<float>(tb, bf, ctl, mloc, src, src32).p;
-    const Mean32 mf = mean_flow32(tb, U32, member_dr32(tb, bf, ctl, mloc, src), i);
+    // An explicit field's mean-flow terms (nsp_state.cuh), from its FP32 copy; a member
+    // state's are added by the linear pass.
+    const float2* U32 = src ? src32 : nullptr;
+    Mean32 mf{};
+    if (U32) mf = mean_flow32(tb, U32, nullptr, i);
     const float2* Uq = U32 + (c == 2 ? 2 : 1) * S + (size_t)i * NTNZ + l;  // u_theta (N_r, N_theta) or u_z (N_z)
     const float2* Ur = U32 + (size_t)i * NTNZ + l;
     const float kzl = tb.kzs32 * (float)l;
@@ -316,7 +324,7 @@ template <int NT, int NTP> struct FwdJob {
       if (2 * j >= nc) break;
       const int it = c0 / 2 + j;
       float2 w = make_float2(v[2 * j], v[2 * j + 1]);
-      if (it != NT / 2 && l != NZ - 1) {
+      if (U32 && it != NT / 2 && l != NZ - 1) {
         const bool zm = it == 0 && l == 0;
         const float2 ur = Ur[(size_t)it * NZ], uq = zm ? make_float2(0.f, 0.f) : Uq[(size_t)it * NZ];
         const float kt = (float)(it < NT / 2 ? it : it - NT) * tb.kts32;

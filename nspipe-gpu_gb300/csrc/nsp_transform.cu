@@ -115,8 +115,14 @@ __global__ void __launch_bounds__(TTH) nl_theta_inv(Tables tb, Bufs bf, const Ct
         cpx<T> a = U.ld((size_t)i * NTNZ + col);
         v = mk<T>(-kt * a.y * rinv, kt * a.x * rinv);
       }
-      // mixed form: the mean flow stays out of the transforms (its terms: nl_theta_fwd)
-      if (sizeof(T) == 4 && it == 0 && coll[lc] == 0 && mean_field(f)) v = mk<T>(0, 0);
+      // mixed form: the mean flow is recorded for the linear pass (member steps) and kept
+      // out of the transforms; its terms are added by the linear pass, or for an explicit
+      // field by nl_theta_fwd
+      if (sizeof(T) == 4 && it == 0 && coll[lc] == 0) {
+        const int slot = f == 0 ? MEAN_V : f == 1 ? MEAN_W : f == 2 ? MEAN_U : f == 4 ? MEAN_WP : f == 5 ? MEAN_UP : -1;
+        if (!src_override && slot >= 0) bf.MEAN[((size_t)mloc * NR + i) * MEAN_N + slot] = (float)v.x;
+        if (mean_field(f)) v = mk<T>(0, 0);
+      }
     }
     buf[idx] = v;
   }
@@ -483,12 +489,14 @@ __global__ void __launch_bounds__(TTH) nl_theta_fwd(Tables tb, Bufs bf, const Ct
     for (int j = 0; j <= IW; j++) dwall += Dw[j] * U[2 * S + (size_t)(NR - 1 - IW + j) * NTNZ].x;
   }
   const T scale = tb_inv_norm<T>(tb);
-  // mixed form: the mean-flow terms (nsp_state.cuh), from the FP32 transform input
+  // mixed form, explicit field: the mean-flow terms (nsp_state.cuh), from its FP32 copy
   const float2* U32 = nullptr;
   Mean32 mf{};
   if constexpr (sizeof(T) == 4) {
-    U32 = member_input<float>(tb, bf, ctl, mloc, src_override, src32_override).p;
-    mf = mean_flow32(tb, U32, member_dr32(tb, bf, ctl, mloc, src_override), i);
+    if (src_override) {  // a member state's terms are added by the linear pass
+      U32 = src32_override;
+      mf = mean_flow32(tb, U32, nullptr, i);
+    }
   }
   for (int idx = threadIdx.x; idx < NT * LC; idx += TTH) {
     int it = idx / LC, lc = idx % LC;
@@ -501,7 +509,7 @@ __global__ void __launch_bounds__(TTH) nl_theta_fwd(Tables tb, Bufs bf, const Ct
       v = make_double2((double)b.x * tb.inv_norm, (double)b.y * tb.inv_norm);
     } else {
       float2 w = make_float2(b.x * scale, b.y * scale);
-      if (it != NT / 2 && l != NZ - 1) {
+      if (U32 && it != NT / 2 && l != NZ - 1) {
         const bool zm = it == 0 && l == 0;
         const size_t hq = (size_t)i * NTNZ + (size_t)it * NZ + l;
         const float2 ur = U32[hq], uq = zm ? make_float2(0.f, 0.f) : U32[(c == 2 ? 2 : 1) * S + hq];
