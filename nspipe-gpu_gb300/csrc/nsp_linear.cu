@@ -335,10 +335,13 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     // transforms' output plus the mean-flow terms (nsp_state.cuh), from u_i's FP32 mirror
     // -- the transforms' input, at this block's own points -- and the mean flow the
     // theta-inverse recorded.
-    constexpr int UB = 1;  // points per thread whose loads are issued together (2 spills registers here)
+    // N_i and N_{i-1} are held in FP32 (exact: the transforms' values and the FP32 sums
+    // stored by the previous pass), except on the u_z line of mode (0,0), which carries
+    // the FP64 wall forcing and is read again in FP64 (one block's NR points).
+    constexpr int UB = 2;  // points per thread whose loads are issued together (RHSW is also stored)
     const float* mean = bf.MEAN + (size_t)mloc * NR * MEAN_N;
     for (int pb = tid; pb < LN; pb += UB * nth) {
-      double2 n[UB][3], q[UB][3];
+      float2 n[UB][3], q[UB][3], w[UB][3];
 #pragma unroll
       for (int u = 0; u < UB; u++) {
         const int p = pb + u * nth, i = p / LM, k = k0 + p - i * LM;
@@ -346,8 +349,10 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
         const size_t h = ok ? (size_t)i * NTNZ + k : 0;
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-          n[u][c] = ok ? Nn[c * S + h] : c2(0, 0);
-          q[u][c] = ok ? Rw[c * S + h] : c2(0, 0);
+          const double2 a = ok ? Nn[c * S + h] : c2(0, 0), b = ok ? Rw[c * S + h] : c2(0, 0);
+          n[u][c] = make_float2(f64_to_f32(a.x), f64_to_f32(a.y));
+          q[u][c] = make_float2(f64_to_f32(b.x), f64_to_f32(b.y));
+          w[u][c] = ok ? Ui32[c * S + h] : make_float2(0.f, 0.f);
         }
       }
 #pragma unroll
@@ -359,23 +364,25 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
         float2 ml[3] = {};
         if (ok && !sdrop[mm]) {
           const Mean32 mf = mean_flow32_rec(tb, mean, i);
-          const float2 zero = make_float2(0.f, 0.f);
-          const float2 wr = k == 0 ? make_float2(mean[(size_t)i * MEAN_N + MEAN_V], 0.f) : Ui32[h];
-          const float2 wt = k == 0 ? zero : Ui32[S + h], wz = k == 0 ? zero : Ui32[2 * S + h];
+          if (k == 0) {  // mode (0,0): u'_theta = u'_z = 0, and only the mean u_r counts
+            w[u][0] = make_float2(mean[(size_t)i * MEAN_N + MEAN_V], 0.f);
+            w[u][1] = w[u][2] = make_float2(0.f, 0.f);
+          }
 #pragma unroll
-          for (int c = 0; c < 3; c++) ml[c] = mean_terms32(mf, c, k == 0, skt32[mm], skz32[mm], wr, wt, wz);
+          for (int c = 0; c < 3; c++) ml[c] = mean_terms32(mf, c, k == 0, skt32[mm], skz32[mm], w[u][0], w[u][1], w[u][2]);
         }
 #pragma unroll
         for (int c = 0; c < 3; c++) {
           float2 d;
           if (c == 2 && k == 0) {
-            const double2 nf = c2(n[u][c].x + (double)ml[c].x, n[u][c].y);
-            if (ok) Rw[c * S + h] = nf;
-            d = make_float2(f64_to_f32(nf.x - q[u][c].x), f64_to_f32(nf.y - q[u][c].y));
+            const double2 a = Nn[2 * S + h], b = Rw[2 * S + h];
+            const double2 nf = c2(a.x + (double)ml[c].x, a.y);
+            Rw[2 * S + h] = nf;
+            d = make_float2(f64_to_f32(nf.x - b.x), f64_to_f32(nf.y - b.y));
           } else {
-            const float nx = f64_to_f32(n[u][c].x) + ml[c].x, ny = f64_to_f32(n[u][c].y) + ml[c].y;
+            const float nx = n[u][c].x + ml[c].x, ny = n[u][c].y + ml[c].y;
             if (ok) Rw[c * S + h] = c2(f32_to_f64(nx), f32_to_f64(ny));
-            d = make_float2(nx - f64_to_f32(q[u][c].x), ny - f64_to_f32(q[u][c].y));
+            d = make_float2(nx - q[u][c].x, ny - q[u][c].y);
           }
           f32slot(R, c * LN + p) = d;  // zero where k >= NTNZ
         }
