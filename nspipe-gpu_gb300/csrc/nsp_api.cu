@@ -301,8 +301,60 @@ int reset_control(nsp_ctx* c) {
   return NSP_OK;
 }
 
+// The z-stage kernel of each group (radix-stage or one of the two-pass splits compiled
+// for its length and precision), timed like the linear pass: z stage alone on the
+// group's buffers, best of 3 after a warm-up.  Cached per shape and precision,
+// "z1:NRxNTxNZ:pP", not per member count: the kernels differ in rounding, and members
+// of one shape give the same bits whatever ensemble they are stepped in.
+int autotune_z(nsp_ctx* c, std::map<std::string, int>& cache, bool* dirty) {
+  const bool mixed = c->precision == NSP_MIXED;
+  const int nm = c->nmem;
+  std::vector<int> zeros(nm, 0);
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  for (auto& g : c->groups) {
+    const int nv = z_variants(g.tb.NZR, g.tb.NTP, mixed);
+    if (nv == 0) continue;
+    char key[128];
+    snprintf(key, sizeof key, "z1:%dx%dx%d:p%d", g.tb.NR, g.tb.NT, g.tb.NZ, c->precision);
+    auto it = cache.find(key);
+    if (it != cache.end() && it->second >= 0 && it->second <= nv) {
+      g.tb.z_variant = it->second;
+      continue;
+    }
+    CK(cudaMemcpyAsync(c->hctl.phase, zeros.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, c->st));
+    float best = 1e30f;
+    for (int v = 0; v <= nv; v++) {
+      Tables tv = g.tb;
+      tv.z_variant = v;
+      launch_nonlinear(tv, g.bf, c->dctl, mixed, nullptr, nullptr, c->st, 2);
+      float t = 1e30f;
+      for (int r = 0; r < 3; r++) {
+        CK(cudaEventRecord(e0, c->st));
+        launch_nonlinear(tv, g.bf, c->dctl, mixed, nullptr, nullptr, c->st, 2);
+        CK(cudaEventRecord(e1, c->st));
+        CK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, e0, e1));
+        t = std::min(t, ms);
+      }
+      CK(cudaGetLastError());
+      if (t < best) { best = t; g.tb.z_variant = v; }
+    }
+    cache[key] = g.tb.z_variant;
+    *dirty = true;
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return NSP_OK;
+}
+
 int autotune(nsp_ctx* c) {
-  for (auto& g : c->groups) g.tb.lin_variant = g.tb.lin_variant_inc = linear_default_variant(g.tb.NR);
+  for (auto& g : c->groups) {
+    g.tb.lin_variant = g.tb.lin_variant_inc = linear_default_variant(g.tb.NR);
+    g.tb.z_variant = z_default_variant(g.tb.NZR, g.tb.NTP, c->precision == NSP_MIXED);
+  }
   const char* ev = getenv("NSP_AUTOTUNE");
   if (ev && ev[0] == '0') return NSP_OK;
   std::map<std::string, int> cache = tune_load();
@@ -364,6 +416,9 @@ int autotune(nsp_ctx* c) {
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  const char* ez = getenv("NSP_Z2");
+  if (!(ez && ez[0] == '0'))
+    if (int rc = autotune_z(c, cache, &dirty)) return rc;
   if (dirty) tune_store(cache);
   return reset_control(c);
 }
@@ -1483,12 +1538,13 @@ int nsp_describe(nsp_ctx* c, char* buf, int cap) {
     linear_shape(vi, &LMi, &NTHi);
     char inc[64] = "";
     if (c->precision == NSP_MIXED) snprintf(inc, sizeof inc, ", \"linear_block_corrector\": [%d, %d]", LMi, NTHi);
-    char g[448];
+    char g[512];
     snprintf(g, sizeof(g),
              "%s{\"shape\": [%d, %d, %d], \"members\": %d, \"parameter_sets\": %d, \"linear_block\": [%d, %d]%s, "
-             "\"theta\": \"%s\", \"setup\": \"%s\"}",
+             "\"theta\": \"%s\", \"z_stage\": \"%s\", \"setup\": \"%s\"}",
              k ? ", " : "", tb.NR, tb.NT, tb.NZ, tb.nmem, tb.nsets, LM, NTH, inc,
              c->precision != NSP_MIXED ? "fft-fp64" : (tb.tc_theta ? "tcgen05-3xtf32" : "fft-fp32"),
+             z_variant_name(tb.NZR, tb.NTP, c->precision == NSP_MIXED, tb.z_variant).c_str(),
              c->groups[k].device_setup ? "device" : "host");
     s += g;
   }

@@ -59,6 +59,8 @@ struct Tables {
   FftPlan pt, pz;
   int lin_variant;     // block shape of the linear pass (autotuned at setup)
   int lin_variant_inc; // mixed form: block shape of the increment (corrector) pass
+  int z_variant;       // z-stage kernel (autotuned at setup): 0 radix-stage, k >= 1 the k-th
+                       // two-pass N1 x N2 split compiled for the length and precision
   int nsets;           // operator parameter sets (distinct Re) of the group
   const int* mset;     // [nmem] parameter set of each member
   const double* sscal; // [nsets][4]: (1-d_im)/Re, 2/Re, Qc, Re
@@ -154,6 +156,11 @@ void launch_to_f32(const double2* src, float2* dst, long long n, cudaStream_t st
 // The FP32 mirror and its radial derivative (DR32) of a group's state U (mixed form).
 void launch_mirror(const Tables& tb, const double2* U, float2* U32, float2* DR32, cudaStream_t st);
 int kernels_per_nonlinear();
+// z-stage kernels of a length (nsp_transform.cu): the number of two-pass splits compiled
+// for NZR (rows per block dividing NTP) in the precision, and a description of variant v.
+int z_variants(int NZR, int NTP, bool fp32);
+int z_default_variant(int NZR, int NTP, bool fp32);
+std::string z_variant_name(int NZR, int NTP, bool fp32, int v);
 // Tensor-core theta transforms (nsp_theta_tc.cu).
 bool theta_tc_supported(int NT, int NTP);
 std::vector<float> theta_dft_image(int NT, int NTP, bool inverse, double scale);

@@ -550,8 +550,6 @@ static void launch_z(const Tables& tb, const Bufs& bf, Ctl* dctl, bool standalon
   nl_z<T, NZRC, RPB><<<g, ZTH, sm, st>>>(tb, bf, dctl, standalone ? 1 : 0);
 }
 
-static bool z2_enabled();
-
 template <typename T, int NZRC, int N1, int N2, int R>
 static constexpr size_t z2_smem() {
   return sizeof(cpx<T>) * ((size_t)R * 6 * N2 * (N1 + 1) + (size_t)R * 6 * z2_pitch(NZRC));
@@ -565,9 +563,40 @@ static void launch_z2(const Tables& tb, const Bufs& bf, Ctl* dctl, bool standalo
 
 #define NSP_NTP_LIST(X) X(12) X(24) X(48) X(72) X(96) X(144) X(192)
 #define NSP_NZR_LIST(X) X(24, 2) X(48, 2) X(96, 2) X(192, 2) X(384, 2) X(576, 1) X(768, 1)
-// Two-pass z stage: (NZR, N1, N2, rows per block) for FP32 and FP64.
-#define NSP_Z2_LIST_F(X) X(24, 4, 6, 2) X(48, 8, 6, 2) X(96, 8, 12, 2) X(192, 16, 12, 2) X(384, 16, 24, 2) \
-  X(576, 24, 24, 2) X(768, 32, 24, 2)
+// Two-pass z stage: (NZR, N1, N2, rows per block), the splits compiled for FP32 and for
+// FP64 (whose shared memory, twice FP32's, limits it to NZR <= 384); the setup-time
+// autotuner picks among them and the radix-stage kernel per shape.
+#define NSP_Z2_LIST_F(X) X(24, 4, 6, 2) X(48, 8, 6, 2) X(96, 8, 12, 2) X(96, 12, 8, 2) X(192, 16, 12, 2) \
+  X(192, 12, 16, 2) X(384, 16, 24, 2) X(384, 24, 16, 2) X(576, 24, 24, 2) X(768, 32, 24, 2) X(768, 24, 32, 2)
+#define NSP_Z2_LIST_D(X) X(24, 4, 6, 2) X(48, 8, 6, 2) X(96, 8, 12, 2) X(192, 16, 12, 2) X(192, 12, 16, 2) \
+  X(384, 16, 24, 2)
+
+int z_variants(int NZR, int NTP, bool fp32) {
+  int n = 0;
+#define NSP_Z2_COUNT(len, a, b, r) n += (NZR == len && NTP % r == 0);
+  if (fp32) { NSP_Z2_LIST_F(NSP_Z2_COUNT) } else { NSP_Z2_LIST_D(NSP_Z2_COUNT) }
+#undef NSP_Z2_COUNT
+  return n;
+}
+
+// The two-pass kernel where one is compiled for the length (the FP32 default, measured
+// faster than the radix-stage kernel on the bench shape), else the radix-stage kernel.
+int z_default_variant(int NZR, int NTP, bool fp32) {
+  const char* e = getenv("NSP_Z2");
+  if (e && e[0] == '0') return 0;
+  return fp32 && z_variants(NZR, NTP, true) > 0 ? 1 : 0;
+}
+
+std::string z_variant_name(int NZR, int NTP, bool fp32, int v) {
+  if (v <= 0) return "radix";
+  int k = 0;
+  std::string s = "radix";
+#define NSP_Z2_NAME(len, a, b, r) \
+  if (NZR == len && NTP % r == 0 && ++k == v) s = "two-pass " #a "x" #b;
+  if (fp32) { NSP_Z2_LIST_F(NSP_Z2_NAME) } else { NSP_Z2_LIST_D(NSP_Z2_NAME) }
+#undef NSP_Z2_NAME
+  return s;
+}
 
 template <typename T>
 static void launch_nl_t(const Tables& tb, const Bufs& bf, Ctl* dctl, const double2* src, const float2* src32,
@@ -587,14 +616,15 @@ static void launch_nl_t(const Tables& tb, const Bufs& bf, Ctl* dctl, const doubl
   }
   if (mask & 2) {
     bool done = false;
-    // FP32 (mixed form) only: in FP64 the radix-stage kernel issues fewer FP64 instructions.
-    if (sizeof(T) == 4 && z2_enabled()) {
-#define NSP_CASE_Z2(n, a, b, r)                                             \
-  if (!done && tb.NZR == n && tb.NTP % r == 0) {                           \
-    launch_z2<T, n, a, b, r>(tb, bf, dctl, src != nullptr, st, nm);         \
-    done = true;                                                            \
+    // the group's z-stage variant: the k-th two-pass split of the length, or (0) radix
+    if (tb.z_variant > 0) {
+      int k = 0;
+#define NSP_CASE_Z2(n, a, b, r)                                                      \
+  if (!done && tb.NZR == n && tb.NTP % r == 0 && ++k == tb.z_variant) {             \
+    launch_z2<T, n, a, b, r>(tb, bf, dctl, src != nullptr, st, nm);                  \
+    done = true;                                                                     \
   }
-      NSP_Z2_LIST_F(NSP_CASE_Z2)
+      if constexpr (sizeof(T) == 4) { NSP_Z2_LIST_F(NSP_CASE_Z2) } else { NSP_Z2_LIST_D(NSP_CASE_Z2) }
 #undef NSP_CASE_Z2
     }
     if (!done) {
@@ -637,10 +667,6 @@ static void configure_t() {
 #undef NSP_CFG_Z
 }
 
-// NSP_Z2=0 keeps the radix-stage z kernels (for comparisons).
-static bool g_z2 = true;
-static bool z2_enabled() { return g_z2; }
-
 void configure_transform_kernels() {
   configure_t<double>();
   configure_t<float>();
@@ -649,6 +675,11 @@ void configure_transform_kernels() {
                        (int)z2_smem<float, n, a, b, r>());
   NSP_Z2_LIST_F(NSP_CFG_Z2F)
 #undef NSP_CFG_Z2F
+#define NSP_CFG_Z2D(n, a, b, r)                                                           \
+  cudaFuncSetAttribute(nl_z2<double, n, a, b, r>, cudaFuncAttributeMaxDynamicSharedMemorySize, \
+                       (int)z2_smem<double, n, a, b, r>());
+  NSP_Z2_LIST_D(NSP_CFG_Z2D)
+#undef NSP_CFG_Z2D
   // Twiddles of the register sub-transforms, exp(-2 pi i e / 96), from long double.
   float2 wf[96];
   double2 wd[96];
@@ -659,8 +690,6 @@ void configure_transform_kernels() {
   }
   cudaMemcpyToSymbol(c_w96f, wf, sizeof(wf));
   cudaMemcpyToSymbol(c_w96d, wd, sizeof(wd));
-  const char* e = getenv("NSP_Z2");
-  g_z2 = !(e && e[0] == '0');
 }
 
 bool transform_supported(int NTP, int NZR) {
