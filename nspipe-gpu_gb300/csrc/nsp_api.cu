@@ -178,6 +178,7 @@ Tables member_view(const Group& g, int slot) {
   const int ps = g.mset[slot];
   t.fac += (size_t)ps * 4 * t.NR * NFAC * t.NTNZ;
   t.V += (size_t)ps * 3 * t.S;
+  if (t.V32) t.V32 += (size_t)ps * 3 * t.S;
   t.Luc += (size_t)ps * 2 * STEN * t.NR;
   t.Luc32 += (size_t)ps * 2 * STEN * t.NR;
   t.uc += (size_t)ps * t.NR;
@@ -753,6 +754,14 @@ int nsp_setup(nsp_ctx* c) {
       if ((rc = upload(c, &tb.fac, fac_all)) || (rc = upload(c, &tb.V, V_all))) return rc;
     }
     tb.nsets = nsets;
+    tb.V32 = nullptr;
+    if (c->precision == NSP_MIXED) {  // FP32 copy of the correction profiles for the increment passes
+      float2* v32 = nullptr;
+      if ((rc = dalloc(c, &v32, sizeof(float2) * V_n))) return rc;
+      launch_to_f32(tb.V, v32, (long long)V_n, c->st);
+      CK(cudaGetLastError());
+      tb.V32 = v32;
+    }
     std::vector<double2> wt = twiddles(tb.NTP), wz = twiddles(tb.NZR);
     if ((rc = upload(c, &tb.tw_t, wt)) || (rc = upload(c, &tb.tw_z, wz)) || (rc = upload(c, &tb.tw_t32, to_f32(wt))) ||
         (rc = upload(c, &tb.tw_z32, to_f32(wz))))

@@ -52,6 +52,7 @@ struct Tables {
   const float* Luc32;  // the same in FP32 (mixed form: the explicit stencil runs on the FP32 mirror)
   const double* fac;   // [4][NR][7][NTNZ]: banded LU factors of u+, u-, u_z, p
   const double2* V;    // [3][NR][NTNZ]: influence-matrix correction profiles (+, -, z)
+  const float2* V32;   // mixed form: the same in FP32 (the corrector increments' correction)
   const double2* tw_t; // [NTP] exp(-2 pi i e/NTP), FP64
   const double2* tw_z; // [NZR]
   const float2* tw_t32;

@@ -150,6 +150,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   double2* R = sm;           // [3][NR][LM] right-hand side, then the new velocity
   double2* P = sm + 3 * LN;  // [NR][LM] divergence, then the pressure
   __shared__ double2 dvs[LM];
+  __shared__ float2 dvs32[LM];  // increment passes: the same in FP32
   __shared__ unsigned long long wnum[NTH / 32], wden[NTH / 32];
   __shared__ double skt[LM], skz[LM];  // k_theta, k_z of the block's modes
   __shared__ double snkz2[LM], snkt2[LM], shdk[LM];  // -k_z^2, -k_theta^2, -c_ex k_theta (predictor)
@@ -573,11 +574,35 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       dv = c2(-sx, -sy);
     }
     dvs[mm] = dv;
+    dvs32[mm] = make_float2(f64_to_f32(dv.x), f64_to_f32(dv.y));
   }
   __syncthreads();
 
   // G2. u += (-div_wall) V (both at half scale), back to full-scale r/theta, mode (0,0) constraints.
-  for (int p = tid; p < LN; p += nth) {
+  // Increment passes: in FP32 on the increment (the solves' FP64 results rounded), into the
+  // FP32 halves of the slots -- the increment needs FP32's relative precision, the update of
+  // u in stage I stays FP64.
+  if constexpr (INC) {
+    const float2* Vp32 = tb.V32 + (size_t)ps * 3 * S;
+    for (int p = tid; p < LN; p += nth) {
+      const int i = p / LM, mm = p - i * LM, k = k0 + mm;
+      if (k >= NTNZ) continue;
+      const size_t hv = (size_t)i * NTNZ + k;
+      if (!NSP_IN_BOUNDS(tb, hv, S, BC_LIN_POINT)) continue;
+      const double2 a = R[p], b = R[LN + p], z = R[2 * LN + p];
+      float2 up = make_float2(f64_to_f32(a.x), f64_to_f32(a.y)), um = make_float2(f64_to_f32(b.x), f64_to_f32(b.y));
+      float2 uz = make_float2(f64_to_f32(z.x), f64_to_f32(z.y));
+      const float2 dv = dvs32[mm], v0 = Vp32[hv], v1 = Vp32[S + hv], v2 = Vp32[2 * S + hv];
+      up.x += dv.x * v0.x - dv.y * v0.y; up.y += dv.x * v0.y + dv.y * v0.x;
+      um.x += dv.x * v1.x - dv.y * v1.y; um.y += dv.x * v1.y + dv.y * v1.x;
+      uz.x += dv.x * v2.x - dv.y * v2.y; uz.y += dv.x * v2.y + dv.y * v2.x;
+      float2 ur = make_float2(up.x + um.x, up.y + um.y);
+      float2 ut = make_float2(up.y - um.y, -(up.x - um.x));
+      uz = make_float2(uz.x + uz.x, uz.y + uz.y);
+      if (k == 0) { ur = make_float2(0.f, 0.f); ut.y = 0.f; uz.y = 0.f; }
+      f32slot(R, p) = ur; f32slot(R, LN + p) = ut; f32slot(R, 2 * LN + p) = uz;
+    }
+  } else for (int p = tid; p < LN; p += nth) {
     int i = p / LM, mm = p - i * LM, k = k0 + mm;
     if (k >= NTNZ) continue;
     double2 up = R[p], um = R[LN + p], uz = R[2 * LN + p];
@@ -596,12 +621,19 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   }
   __syncthreads();
 
-  // H. constant mass flux on mode (0,0).
+  // H. constant mass flux on mode (0,0) (increment passes: on the FP32 increment, the
+  // flux summed in FP64, no Qdes term).
   if (k0 == 0 && tid == 0) {
     double Q = 0.0;
-    for (int i = 0; i < NR; i++) Q += tb.rdr[i] * R[2 * LN + i * LM].x;
-    double corr = ((INC ? 0.0 : tb.Qdes) - Q) / Qc;
-    for (int i = 0; i < NR; i++) R[2 * LN + i * LM].x += corr * ucp[i];
+    if constexpr (INC) {
+      for (int i = 0; i < NR; i++) Q += tb.rdr[i] * f32_to_f64(f32slot(R, 2 * LN + i * LM).x);
+      const double corr = -Q / Qc;
+      for (int i = 0; i < NR; i++) f32slot(R, 2 * LN + i * LM).x += f64_to_f32(corr * ucp[i]);
+    } else {
+      for (int i = 0; i < NR; i++) Q += tb.rdr[i] * R[2 * LN + i * LM].x;
+      double corr = (tb.Qdes - Q) / Qc;
+      for (int i = 0; i < NR; i++) R[2 * LN + i * LM].x += corr * ucp[i];
+    }
   }
   __syncthreads();
 
@@ -634,18 +666,21 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       if (kBoundsCheck && h >= (size_t)S) continue;  // (recorded by the load loop above)
 #pragma unroll
       for (int c = 0; c < 3; c++) {
-        double2 v = R[c * LN + p];
+        double2 v;
         if constexpr (INC) {
           // |increment|^2 and |u_i|^2 in FP32 (the measure only decides err > tol)
-          const float fx = f64_to_f32(v.x), fy = f64_to_f32(v.y);
+          const float2 f = f32slot(R, c * LN + p);
           const float ox = f64_to_f32(o[u][c].x), oy = f64_to_f32(o[u][c].y);
-          lnum32 = max(lnum32, __float_as_uint(fmaf(fx, fx, fy * fy)));
+          lnum32 = max(lnum32, __float_as_uint(fmaf(f.x, f.x, f.y * f.y)));
           lden32 = max(lden32, __float_as_uint(fmaf(ox, ox, oy * oy)));
-          v = c2(fma(hdi, v.x, o[u][c].x), fma(hdi, v.y, o[u][c].y));
-        } else if (!pred) {
-          const double ex = o[u][c].x - v.x, ey = o[u][c].y - v.y;
-          lnum = max(lnum, (unsigned long long)__double_as_longlong(ex * ex + ey * ey));
-          lden = max(lden, (unsigned long long)__double_as_longlong(o[u][c].x * o[u][c].x + o[u][c].y * o[u][c].y));
+          v = c2(fma(hdi, f32_to_f64(f.x), o[u][c].x), fma(hdi, f32_to_f64(f.y), o[u][c].y));
+        } else {
+          v = R[c * LN + p];
+          if (!pred) {
+            const double ex = o[u][c].x - v.x, ey = o[u][c].y - v.y;
+            lnum = max(lnum, (unsigned long long)__double_as_longlong(ex * ex + ey * ey));
+            lden = max(lden, (unsigned long long)__double_as_longlong(o[u][c].x * o[u][c].x + o[u][c].y * o[u][c].y));
+          }
         }
         const unsigned EX = 0x7FF00000u;
         nonfin |= ((unsigned)__double2hiint(v.x) & EX) == EX || ((unsigned)__double2hiint(v.y) & EX) == EX;
