@@ -368,42 +368,16 @@ def main():
     names = ["nl_theta_inv", "nl_z", "nl_theta_fwd", "linear_k", "converge_k"]
     csz = 8 if prec == nsp.NSP_MIXED else 16
     NTP, NZR = 3 * NT // 2, 3 * (NZ - 1)
-    # The linear pass in each of its kinds: the full predictor (the first step after the
-    # state is set), the corrector and, in the mixed form, the increment predictor that
-    # every later step runs.  Algorithmic models per grid point (16-byte FP64 values,
-    # 8-byte FP32 values, 3 components):
-    #   full predictor:  bytes read u^n, N, V, write u^*, RHSW (15 x 16), mixed: read u^n's
-    #     mirror, write the new mirror and its d_r (9 x 8) and NP (3 x 16); FP64 flops 347
-    #     (explicit Laplacian 84, coefficients 7, right-hand sides 32, step-invariant part 12,
-    #     divergence 37, pressure solve 26, gradient and +/- 41, Helmholtz solves 78,
-    #     correction and r/theta 30), mixed 224 (its explicit right-hand side but u^n/dt FP32);
-    #   corrector:  FP64 form: bytes read N, RHSW, V, u_i, write u_{i+1} (15 x 16); flops 242
-    #     (right-hand side 12, divergence 37, pressure solve 26, gradient and +/- 41, Helmholtz
-    #     solves 78, correction 30, convergence measure 18).  Mixed (the increment pass):
-    #     read N, RHSW, u_i (9 x 16), V's and u_i's FP32 copies (6 x 8), write u_{i+1}, RHSW
-    #     (6 x 16), the mirror and its d_r (6 x 8); flops: banded solves 104, update 12;
-    #   increment predictor (mixed): read N, RHSW, NP, u^n, u^{n-1} (15 x 16), V's FP32 copy
-    #     and both mirrors (9 x 8), write u^*, RHSW, NP (9 x 16), the mirror and its d_r
-    #     (6 x 8); flops: banded solves 104, the difference u^n - u^{n-1} 6, update 6.
-    mixed = prec == nsp.NSP_MIXED
-    lin = st.profile_linear(5)  # [full predictor, corrector, increment predictor]
-    models = {
-        "full_predictor": (M * S * (15 * 16 + (9 * 8 + 3 * 16 if mixed else 0)), (224.0 if mixed else 347.0) * S * M),
-        "corrector": (M * S * ((15 * 16 + 12 * 8 + 6 * 16) if mixed else 15 * 16), (116.0 if mixed else 242.0) * S * M),
-        "increment_predictor": (M * S * (24 * 16 + 15 * 8), 116.0 * S * M),
-    }
-    lin_ms = {"full_predictor": float(lin[0]), "corrector": float(lin[1]), "increment_predictor": float(lin[2])}
-    # the kernels of a steady step: its predictor (the increment predictor in the mixed form)
-    pred_kind = "increment_predictor" if mixed else "full_predictor"
     alg_bytes = [  # algorithmic bytes per launch (all members)
         M * (3 * S * 16 + 9 * NR * NTP * NZ * csz),           # read u (stencil counted once), write G
         M * (9 * NR * NTP * NZ * csz + 3 * NR * NTP * (NZ - 1) * csz),  # read G, write H
         M * (3 * NR * NTP * (NZ - 1) * csz + 3 * S * 16),     # read H, write N
-        models[pred_kind][0],
+        # predictor pass (the one timed): read u^n, N, V, write u_1 and RHSW (16 bytes per
+        # value, 3 components); the mixed form also reads u^n's FP32 mirror for the explicit
+        # stencil and writes the new FP32 mirror and its d_r (8 bytes per value)
+        M * S * (15 * 16 + (9 * 8 if prec == nsp.NSP_MIXED else 0)),
         M * 64,
     ]
-    stage_ms = list(stage_ms)
-    stage_ms[3] = lin_ms[pred_kind]
     dom = int(np.argmax(stage_ms[:4]))
     peak, peak_kind = measured_peaks()
     achieved = alg_bytes[dom] / (stage_ms[dom] * 1e-3) / 1e9
@@ -411,28 +385,38 @@ def main():
     tpath = os.path.join(ROOT, "profiles", "traffic.json")
     if os.path.exists(tpath):
         try:
-            key = "%s_%s" % (names[dom], args.precision) + ("_increment_predictor" if dom == 3 and mixed else "")
-            traffic = json.load(open(tpath)).get(key)
+            traffic = json.load(open(tpath)).get("%s_%s" % (names[dom], args.precision))
         except ValueError:
             traffic = None
-    roofline = {"bound": "hbm", "kernel": names[dom] + (" (%s)" % pred_kind.replace("_", " ") if dom == 3 else ""),
-                "achieved": achieved, "peak": peak, "unit": "GB/s",
+    roofline = {"bound": "hbm", "kernel": names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                 "algorithmic_bytes_per_launch": alg_bytes[dom], "launch_ms": stage_ms[dom],
                 "stage_ms": dict(zip(names, [float(x) for x in stage_ms]))}
-    # The linear pass is FP64-bound on GB300 (FP64 ~1/60 of FP32): its FP64 roofline, per kind.
-    fp64_peak = st.fp64_peak_tflops()
-    if dom == 3:
-        fl = models[pred_kind][1]
+    # The linear pass is FP64-bound on GB300 (FP64 ~1/60 of FP32): its FP64 roofline.
+    # FP64 flops per grid point of the timed predictor pass: explicit Laplacian 84,
+    # coefficients 7, right-hand sides 20 + 12, step-invariant part 12, divergence 37,
+    # pressure solve 26, gradient and +/- 41, three Helmholtz solves 78, influence
+    # correction and r/theta 30: 347.  The mixed form sums the explicit right-hand side
+    # in FP32 but for u^n/dt (12) and stores no step-invariant part: 224.
+    if names[dom] == "linear_k":
+        fp64_peak = st.fp64_peak_tflops()
+        fl = (224.0 if prec == nsp.NSP_MIXED else 347.0) * S * M
         ach = fl / (stage_ms[dom] * 1e-3) / 1e12
         roofline["compute_bound"] = "fp64"
         roofline["fp64"] = {"achieved_tflops": ach, "peak_tflops": fp64_peak, "frac": ach / fp64_peak,
                             "algorithmic_flops_per_launch": fl, "peak_source": "measured live (nsp_measure_fp64_peak)"}
-    roofline["linear_passes"] = {
-        kind: {"launch_ms": lin_ms[kind], "fp64_frac": models[kind][1] / (lin_ms[kind] * 1e-3) / 1e12 / fp64_peak,
-               "hbm_frac": models[kind][0] / (lin_ms[kind] * 1e-3) / 1e9 / peak,
-               "algorithmic_flops_per_launch": models[kind][1], "algorithmic_bytes_per_launch": models[kind][0]}
-        for kind in models if lin_ms[kind] > 0}
+        # The corrector pass.  Mixed form (the increment pass): about 150 FP64 flops per
+        # point (banded solves 104, influence correction 30, update 12; its stencils are
+        # FP32).  FP64 form: 242 (right-hand side 12, divergence 37, pressure solve 26,
+        # gradient and +/- 41, Helmholtz solves 78, correction 30, convergence measure 18).
+        # Bytes: read N, RHSW, V, u_i, write u_{i+1} (15 x 16 per point); mixed, also the
+        # RHSW update (3 x 16) and the FP32 mirror and its d_r (6 x 8).
+        lin = st.profile_linear(5)
+        fl_c = (150.0 if prec == nsp.NSP_MIXED else 242.0) * S * M
+        by_c = M * S * ((18 * 16 + 6 * 8) if prec == nsp.NSP_MIXED else 15 * 16)
+        roofline["corrector"] = {"launch_ms": float(lin[1]), "fp64_frac": fl_c / (lin[1] * 1e-3) / 1e12 / fp64_peak,
+                                 "hbm_frac": by_c / (lin[1] * 1e-3) / 1e9 / peak,
+                                 "algorithmic_flops_per_launch": fl_c, "algorithmic_bytes_per_launch": by_c}
 
     # End to end through the C ABI with host buffers: every step is one nsp_step_host
     # call -- H2D of all members' state from pinned memory, one step, D2H of all

@@ -236,12 +236,10 @@ int nsp_bounds_report(nsp_ctx* ctx, long long* out);
 int nsp_profile_stages(nsp_ctx* ctx, int reps, double* ms_out);
 
 /* Measurement hook (no reference counterpart): average device time in ms of one launch
- * of the linear pass with every member in its predictor pass (ms_out[0], the full pass),
- * in a corrector pass (ms_out[1]; the mixed form's increment pass) and, in the mixed
- * form, in the increment predictor that steps after the first use (ms_out[2]; 0 in the
- * FP64 form), over `reps` launches timed with CUDA events on the context's stream.  The
- * state is preserved; the corrector iterate buffers are overwritten, so the next step
- * takes the full predictor. */
+ * of the linear pass with every member in its predictor pass (ms_out[0]) and in a
+ * corrector pass (ms_out[1]; the mixed form's increment pass), over `reps` launches
+ * timed with CUDA events on the context's stream.  The state is preserved; the
+ * corrector iterate buffers are overwritten. */
 int nsp_profile_linear(nsp_ctx* ctx, int reps, double* ms_out);
 
 /* Measurement hook (no reference counterpart): FP64 multiply-add throughput of the

@@ -61,12 +61,7 @@ struct nsp_ctx {
   Ctl* dctl = nullptr;
   int parity = 0;  // host mirror of ctl.parity
   bool setup_done = false;
-  cudaGraphExec_t gexec = nullptr;     // the step graph with the full predictor pass
-  cudaGraphExec_t gexec_ip = nullptr;  // mixed form: the same with the increment predictor
-  // The last step ran in this context and nothing wrote the state or the step's buffers
-  // since: the mixed form's next predictor can be the increment predictor (it reads
-  // u^{n-1}, N(u^{n-1}) and the last corrector's N, which such a step leaves behind).
-  bool hist_ok = false;
+  cudaGraphExec_t gexec = nullptr;
   bool use_graph = false;
   long long launches_last = 0;
   double2* scratch = nullptr;  // 2 x 3 x Smax, for nsp_nonlinear
@@ -81,8 +76,7 @@ struct nsp_ctx {
   // nsp_step_host: copy streams and per-chunk events (created on first use)
   cudaStream_t cp_in = nullptr, cp_out = nullptr;
   std::vector<cudaEvent_t> ev_in, ev_done;
-  std::vector<cudaGraphExec_t> chunk_exec;     // step graphs of the member chunks
-  std::vector<cudaGraphExec_t> chunk_exec_ip;  // mixed form: the same with the increment predictor
+  std::vector<cudaGraphExec_t> chunk_exec;  // step graphs of the member chunks
   std::vector<int> chunk_lo;                // their internal member bounds (K+1 values)
   long long Smax = 0;
   // Mixed form: U32/DR32[parity] hold the FP32 mirror of U[parity] (kept current by the
@@ -209,7 +203,6 @@ void range_view(const Group& g, bool mixed, int a, int b, Tables* t, Bufs* bf) {
   }
   bf->RHSW += s3;
   bf->N += s3;
-  if (bf->NP) bf->NP += s3;
   const size_t esz = mixed ? sizeof(float2) : sizeof(double2);
   const size_t plane = (size_t)g.tb.NR * g.tb.NTP * g.tb.NZ * esz;
   bf->G = static_cast<char*>(g.bf.G) + (size_t)a * 9 * plane;
@@ -433,7 +426,7 @@ int autotune(nsp_ctx* c) {
 
 // The step graph of the members with internal index in [lo, hi) (all members: the
 // context's step graph; a sub-range: a chunk graph of nsp_step_host) into *out.
-int build_graph_range(nsp_ctx* c, int lo, int hi, cudaGraphExec_t* out, bool ipred = false) {
+int build_graph_range(nsp_ctx* c, int lo, int hi, cudaGraphExec_t* out) {
   if (*out) { cudaGraphExecDestroy(*out); *out = nullptr; }
   cudaGraph_t g = nullptr;
   CK(cudaGraphCreate(&g, 0));
@@ -504,7 +497,7 @@ int build_graph_range(nsp_ctx* c, int lo, int hi, cudaGraphExec_t* out, bool ipr
   // value 1 makes at least one corrector pass, as in the reference.
   cudaGraph_t gp = nullptr;
   CK(cudaGraphCreate(&gp, 0));
-  if (int rc = capture_pass(gp, ipred ? LIN_PINC : LIN_PRED, false)) { cudaGraphDestroy(gp); return rc; }
+  if (int rc = capture_pass(gp, LIN_PRED, false)) { cudaGraphDestroy(gp); return rc; }
   cudaGraphNode_t pnode;
   cudaError_t ec = cudaGraphAddChildGraphNode(&pnode, g, nullptr, 0, gp);  // (clones gp)
   cudaGraphDestroy(gp);
@@ -522,19 +515,11 @@ int build_graph_range(nsp_ctx* c, int lo, int hi, cudaGraphExec_t* out, bool ipr
   return NSP_OK;
 }
 
-int build_graph(nsp_ctx* c) {
-  if (int rc = build_graph_range(c, 0, c->nmem, &c->gexec)) return rc;
-  if (c->precision == NSP_MIXED && c->use_graph) return build_graph_range(c, 0, c->nmem, &c->gexec_ip, true);
-  return NSP_OK;
-}
+int build_graph(nsp_ctx* c) { return build_graph_range(c, 0, c->nmem, &c->gexec); }
 
 }  // namespace
 
 namespace nsp {
-void ctx_restart_predictor(nsp_ctx* c) {
-  if (c) c->hist_ok = false;
-}
-
 int ctx_fail(nsp_ctx* c, int code, const std::string& msg) {
   if (c) c->err = msg;
   else set_host_error(msg);
@@ -630,11 +615,6 @@ int nsp_create(const nsp_params* members, int n_members, int precision, int devi
     if ((rc = dalloc(c, &g.bf.U[0], S3 * sizeof(double2)))) return rc;
     if ((rc = dalloc(c, &g.bf.U[1], S3 * sizeof(double2)))) return rc;
     if ((rc = dalloc(c, &g.bf.RHSW, S3 * sizeof(double2)))) return rc;
-    g.bf.NP = nullptr;
-    if (precision == NSP_MIXED) {
-      if ((rc = dalloc(c, &g.bf.NP, S3 * sizeof(double2)))) return rc;
-      CK(cudaMemset(g.bf.NP, 0, S3 * sizeof(double2)));
-    }
     if ((rc = dalloc(c, &g.bf.N, S3 * sizeof(double2)))) return rc;
     if ((rc = dalloc(c, &g.bf.G, gsz))) return rc;
     if ((rc = dalloc(c, &g.bf.H, hsz))) return rc;
@@ -830,7 +810,6 @@ int nsp_setup(nsp_ctx* c) {
     if (rc) return rc;
   }
   c->setup_done = true;
-  c->hist_ok = false;  // (the autotuner's passes overwrote the step's buffers)
   return NSP_OK;
 }
 
@@ -891,7 +870,6 @@ static int copy_states(nsp_ctx* c, int m, double* const* host, bool to_device) {
   const int m0 = m < 0 ? 0 : m, mend = m < 0 ? c->nmem : m + 1;
   if (to_device) {
     c->mirror_ok = false;
-    c->hist_ok = false;
     if (int rc = clear_status(c, m)) return rc;
   }
   size_t off = 0;  // doubles into each host component array
@@ -940,7 +918,6 @@ int nsp_set_state_device(nsp_ctx* c, int m, const void* ur, const void* ut, cons
   size_t bytes = sizeof(double2) * (size_t)c->groups[c->grp[m]].tb.S;
   const void* src[3] = {ur, ut, uz};
   c->mirror_ok = false;
-  c->hist_ok = false;
   if (int rc = clear_status(c, m)) return rc;
   for (int k = 0; k < 3; k++) CK(cudaMemcpyAsync(state_ptr(c, m, k), src[k], bytes, cudaMemcpyDeviceToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
@@ -959,17 +936,9 @@ int nsp_get_state_device(nsp_ctx* c, int m, void* ur, void* ut, void* uz) {
 
 // One step of every member whose phase is 0 at its start (members at -1 sit it out):
 // the step graph, or the same kernels driven from the host (NSP_GRAPH=0).
-// The mixed form's predictor pass is the increment predictor when the previous step ran
-// here (hist_ok), for a whole-context step and for the member chunks of a chunked step
-// alike (hist_ok changes only once a step is complete: here, or after a chunked step's
-// last chunk).
 static int run_step(nsp_ctx* c, int chunk = -1) {
-  const bool ipred = c->hist_ok && c->precision == NSP_MIXED;
   if (c->use_graph) {
-    cudaGraphExec_t x = chunk >= 0 ? (ipred && c->chunk_exec_ip[chunk] ? c->chunk_exec_ip[chunk] : c->chunk_exec[chunk])
-                                   : (ipred && c->gexec_ip ? c->gexec_ip : c->gexec);
-    CK(cudaGraphLaunch(x, c->st));
-    if (chunk < 0) c->hist_ok = true;
+    CK(cudaGraphLaunch(chunk < 0 ? c->gexec : c->chunk_exec[chunk], c->st));
     return NSP_OK;
   }
   const int lo = chunk < 0 ? 0 : c->chunk_lo[chunk], hi = chunk < 0 ? c->nmem : c->chunk_lo[chunk + 1];
@@ -981,7 +950,7 @@ static int run_step(nsp_ctx* c, int chunk = -1) {
       Bufs bf;
       range_view(g, c->precision == NSP_MIXED, a, b, &t, &bf);
       launch_nonlinear(t, bf, c->dctl, c->precision == NSP_MIXED, nullptr, nullptr, c->st);
-      launch_linear(t, bf, c->dctl, c->st, it == 0 ? (ipred ? LIN_PINC : LIN_PRED) : LIN_CORR);
+      launch_linear(t, bf, c->dctl, c->st);
     }
     launch_converge(c->dctl, c->nmem, 0ull, 0, c->st);
     CK(cudaGetLastError());
@@ -990,7 +959,6 @@ static int run_step(nsp_ctx* c, int chunk = -1) {
     CK(cudaStreamSynchronize(c->st));
     if (!any) break;
   }
-  if (chunk < 0) c->hist_ok = true;
   return NSP_OK;
 }
 
@@ -1034,8 +1002,12 @@ static void mirror_range(nsp_ctx* c, int lo, int hi, int par, cudaStream_t st) {
 }
 
 // Kernels launched per predictor or corrector pass: per group the three transform
-// kernels and the pass's own linear kernel, then converge_k.
-static long long kernels_per_pass(const nsp_ctx* c) { return 4LL * (long long)c->groups.size() + 1; }
+// kernels and the linear pass, then converge_k.  The step graph launches the pass's
+// own linear kernel; the host-driven loop launches both of the mixed form's (the
+// full pass for the predictor, the increment pass for the correctors).
+static long long kernels_per_pass(const nsp_ctx* c) {
+  return (c->precision == NSP_MIXED && !c->use_graph ? 5LL : 4LL) * (long long)c->groups.size() + 1;
+}
 
 // The step history of the last `batch` steps into the pinned buffer; with `final` also
 // the members' status words, the fault flag and the unconverged-step counts.  One
@@ -1112,7 +1084,6 @@ int nsp_step(nsp_ctx* c, int nsteps, int* iters_out) {
   c->launches_last = launches;
   const int rc = control_verdict(c);
   c->mirror_ok = rc == NSP_OK && nsteps > 0;
-  if (rc == NSP_ERR_DEVICE) c->hist_ok = false;
   return rc;
 }
 
@@ -1125,7 +1096,6 @@ int nsp_step_host(nsp_ctx* c, int nsteps, const double* in, double* out, int* it
   const int nm = c->nmem;
   double* hin = const_cast<double*>(in);
   c->mirror_ok = false;
-  c->hist_ok = false;  // the states come from `in`
   if (nsteps == 0) {
     if (int rc = copy_chunk(c, 0, nm, c->parity, hin, true, c->st)) return rc;
     if (int rc = copy_chunk(c, 0, nm, c->parity, out, false, c->st)) return rc;
@@ -1165,18 +1135,13 @@ int nsp_step_host(nsp_ctx* c, int nsteps, const double* in, double* out, int* it
   }
   const int K = (int)lo.size() - 1;
   if (c->chunk_lo != lo) {
-    for (auto* v : {&c->chunk_exec, &c->chunk_exec_ip}) {
-      for (cudaGraphExec_t x : *v)
-        if (x) cudaGraphExecDestroy(x);
-      v->assign(K, nullptr);
-    }
+    for (cudaGraphExec_t x : c->chunk_exec)
+      if (x) cudaGraphExecDestroy(x);
+    c->chunk_exec.assign(K, nullptr);
     c->chunk_lo = lo;
     if (c->use_graph)
-      for (int k = 0; k < K; k++) {
+      for (int k = 0; k < K; k++)
         if (int rc = build_graph_range(c, c->chunk_lo[k], c->chunk_lo[k + 1], &c->chunk_exec[k])) return rc;
-        if (c->precision == NSP_MIXED)
-          if (int rc = build_graph_range(c, c->chunk_lo[k], c->chunk_lo[k + 1], &c->chunk_exec_ip[k], true)) return rc;
-      }
   }
   if (!c->cp_in) {
     CK(cudaStreamCreateWithFlags(&c->cp_in, cudaStreamNonBlocking));
@@ -1241,7 +1206,6 @@ int nsp_step_host(nsp_ctx* c, int nsteps, const double* in, double* out, int* it
         CK(cudaMemsetAsync(&c->dctl->hold, 0, sizeof(int), c->st));
         launch_finish_step(c->dctl, c->st);
         restore.armed = false;
-        c->hist_ok = true;
       } else {
         if (int rc = run_step(c)) return rc;
       }
@@ -1267,7 +1231,6 @@ int nsp_step_host(nsp_ctx* c, int nsteps, const double* in, double* out, int* it
   c->launches_last = launches;
   const int rc = control_verdict(c);
   c->mirror_ok = rc == NSP_OK;
-  if (rc == NSP_ERR_DEVICE) c->hist_ok = false;
   return rc;
 }
 
@@ -1587,11 +1550,10 @@ int nsp_describe(nsp_ctx* c, char* buf, int cap) {
     char g[512];
     snprintf(g, sizeof(g),
              "%s{\"shape\": [%d, %d, %d], \"members\": %d, \"parameter_sets\": %d, \"linear_block\": [%d, %d]%s, "
-             "\"theta\": \"%s\", \"z_stage\": \"%s\", \"predictor\": \"%s\", \"setup\": \"%s\"}",
+             "\"theta\": \"%s\", \"z_stage\": \"%s\", \"setup\": \"%s\"}",
              k ? ", " : "", tb.NR, tb.NT, tb.NZ, tb.nmem, tb.nsets, LM, NTH, inc,
              c->precision != NSP_MIXED ? "fft-fp64" : (tb.tc_theta ? "tcgen05-3xtf32" : "fft-fp32"),
              z_variant_name(tb.NZR, tb.NTP, c->precision == NSP_MIXED, tb.z_variant).c_str(),
-             c->precision == NSP_MIXED ? "increment after a step of the context" : "full",
              c->groups[k].device_setup ? "device" : "host");
     s += g;
   }
@@ -1628,7 +1590,6 @@ int nsp_set_strict(nsp_ctx* c, int strict) {
 int nsp_profile_stages(nsp_ctx* c, int reps, double* ms_out) {
   if (!c || !ms_out || reps < 1) return NSP_ERR_ARG;
   if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_profile_stages before nsp_setup");
-  c->hist_ok = false;  // its passes overwrite the step's buffers
   CK(cudaSetDevice(c->device));
   const int nm = c->nmem;
   std::vector<int> zeros(nm, 0), ones(nm, 1);
@@ -1668,19 +1629,15 @@ int nsp_profile_stages(nsp_ctx* c, int reps, double* ms_out) {
 int nsp_profile_linear(nsp_ctx* c, int reps, double* ms_out) {
   if (!c || !ms_out || reps < 1) return NSP_ERR_ARG;
   if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_profile_linear before nsp_setup");
-  c->hist_ok = false;  // its passes overwrite the step's buffers
   CK(cudaSetDevice(c->device));
   const int nm = c->nmem;
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
-  // 0: every member in its predictor pass (full pass), 1: in a corrector pass, 2: the
-  // mixed form's increment predictor (0 in the FP64 form, which has none)
-  ms_out[2] = 0.0;
-  for (int pass = 0; pass < (c->precision == NSP_MIXED ? 3 : 2); pass++) {
-    std::vector<int> ph(nm, pass == 1 ? 1 : 0);
+  for (int pass = 0; pass < 2; pass++) {  // 0: every member in its predictor pass, 1: in a corrector pass
+    std::vector<int> ph(nm, pass);
     CK(cudaMemcpyAsync(c->hctl.phase, ph.data(), sizeof(int) * nm, cudaMemcpyHostToDevice, c->st));
-    const int which = pass == 2 ? LIN_PINC : (pass ? LIN_CORR : LIN_PRED);
+    const int which = pass ? LIN_CORR : LIN_PRED;
     for (auto& g : c->groups) launch_linear(g.tb, g.bf, c->dctl, c->st, which);  // warm-up
     CK(cudaEventRecord(e0, c->st));
     for (int r = 0; r < reps; r++)
@@ -1787,7 +1744,6 @@ int nsp_remesh_members(nsp_remesh* rm, nsp_ctx* src, const int* src_members, nsp
       if (sp[k] == dp[q]) return fail(dst, NSP_ERR_ARG, "a member is both a source and a destination");
   nsp_ctx* c = dst;  // CUDA failures are reported on the destination context
   c->mirror_ok = false;
-  c->hist_ok = false;
   CK(cudaSetDevice(dst->device));
   CK(cudaStreamSynchronize(src->st));
   int rc = remesh_launch(rm, count, sp.data(), dp.data(), dst->st);
@@ -1800,7 +1756,6 @@ int nsp_destroy(nsp_ctx* c) {
   cudaSetDevice(c->device);
   if (c->st) cudaStreamSynchronize(c->st);
   if (c->gexec) cudaGraphExecDestroy(c->gexec);
-  if (c->gexec_ip) cudaGraphExecDestroy(c->gexec_ip);
   for (void* p : c->allocs) cudaFree(p);
   for (cudaStream_t s2 : c->side) cudaStreamDestroy(s2);
   for (cudaEvent_t e2 : c->ev_join) cudaEventDestroy(e2);
@@ -1810,8 +1765,6 @@ int nsp_destroy(nsp_ctx* c) {
   for (cudaEvent_t e2 : c->ev_in) cudaEventDestroy(e2);
   for (cudaEvent_t e2 : c->ev_done) cudaEventDestroy(e2);
   for (cudaGraphExec_t x : c->chunk_exec)
-    if (x) cudaGraphExecDestroy(x);
-  for (cudaGraphExec_t x : c->chunk_exec_ip)
     if (x) cudaGraphExecDestroy(x);
   if (c->own_st) cudaStreamDestroy(c->own_st);
   if (c->pin) cudaFreeHost(c->pin);

@@ -92,8 +92,6 @@ struct Bufs {
   double2* N;          // [nmem][3][S]: nonlinear term output
   void* G;             // [nmem][9][NR][NTP][NZ] complex T: theta-inverse of u, dr u, i m u / r
   void* H;             // [nmem][3][NR][NTP][NZ] complex T: z-forward of the nonlinear product
-  double2* NP;         // mixed form only: [nmem][3][S] N(u^n) of the last predictor pass (the
-                       // increment predictor's N(u^{n-1}) at the next step)
   float* MEAN;         // mixed form only: [nmem][NR][MEAN_N] mean flow of the transform input
                        // (V = Re u_r, W = Re u_theta, U = Re u_z at mode (0,0), W', U'),
                        // written by the theta-inverse, read by the linear pass
@@ -136,9 +134,7 @@ void launch_nonlinear(const Tables& tb, const Bufs& bf, Ctl* dctl, bool mixed, c
 // correctors' (the mixed form's increment pass; the full pass again in the FP64 form)
 // or both (each returns at once in the other's passes; the FP64 form launches its one
 // kernel once).
-// LIN_PINC: the mixed form's increment predictor (a predictor pass that follows a step of
-// this context: u^* = u^n + L(the change of the right-hand side since the last corrector)).
-enum { LIN_PRED = 1, LIN_CORR = 2, LIN_BOTH = 3, LIN_PINC = 4 };
+enum { LIN_PRED = 1, LIN_CORR = 2, LIN_BOTH = 3 };
 void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st, int which = LIN_BOTH);
 void launch_converge(Ctl* dctl, int nmem, unsigned long long cond_handle, int use_cond, cudaStream_t st);
 // Completes a step taken in member chunks: parity flip and step count (converge_k's
@@ -174,10 +170,6 @@ void configure_theta_tc_kernels();
 void launch_theta_tc(const Tables& tb, const Bufs& bf, Ctl* dctl, int dir, const double2* src, const float2* src32,
                      double2* dst, cudaStream_t st);
 
-// The context's next step takes the full predictor pass, as after its state was set
-// (the run driver calls it at every checkpoint, so that a run resumed from the
-// checkpoint and the run that wrote it step on identically).
-void ctx_restart_predictor(nsp_ctx* c);
 // Records msg as the context's last error (nsp_last_error) and returns code.
 int ctx_fail(nsp_ctx* c, int code, const std::string& msg);
 // Records the failure of a context-free call (nsp_last_error(NULL)), per thread.

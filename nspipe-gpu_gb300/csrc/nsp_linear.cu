@@ -132,28 +132,15 @@ __device__ __forceinline__ float2& f32slot(double2* a, int e) { return reinterpr
 // update of u stay in FP64.  N_{i-1} is kept in RHSW (the predictor stores N(u^n)
 // there in the mixed form).  Without INC the kernel is the full pass, and in the
 // mixed form it takes only the predictor.
-//
-// INC and IP (mixed form, a predictor pass that follows a step of this context): the
-// same affinity across steps.  The last corrector pass of the previous step solved for
-// u^n with the right-hand side (half scale) R_last = (d_im/2) N_last + ((1-d_im)/2)
-// N(u^{n-1}) + e(u^{n-1}), e(u) = u/(2 dt) + ((1-d_im)/(2 Re)) L+- u the explicit part,
-// so the predictor's u^* = u^n + L(Delta) with
-//   Delta = N(u^n)/2 - (d_im/2) N_last - ((1-d_im)/2) N(u^{n-1}) + e(u^n - u^{n-1}),
-// a difference of order dt next to the right-hand side's u^n/dt: the divergence and
-// gradient stencils then run in FP32 as in the correctors' increments, while the
-// predictor's full pass needs them in FP64.  N_last is in RHSW, N(u^{n-1}) in NP (each
-// predictor stores its N there), u^{n-1} and its FP32 mirror are still in the iterate
-// buffers (this pass overwrites them only in stage I); u^n - u^{n-1} is taken in FP64,
-// the mean mode's whole Delta in FP64.
-template <int LM, int NTH, bool INC, bool IP = false>
+template <int LM, int NTH, bool INC>
 __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 : (1024 / NTH)))
     linear_k(Tables tb, Bufs bf, Ctl* ctl) {
   const int mloc = blockIdx.y, gm = tb.mem0 + mloc;
   if (!NSP_IN_BOUNDS(tb, mloc, tb.nmem, BC_LIN_MEMBER) || !NSP_IN_BOUNDS(tb, gm, ctl->nmem, BC_LIN_MEMBER)) return;
   const int ph = ctl->phase[gm];
   if (ph < 0) return;
-  if (INC ? (IP ? ph != 0 : ph == 0) : (ph > 0 && bf.U32[0] != nullptr)) return;  // the other kernels' passes
-  const bool pred = (!INC || IP) && ph == 0;
+  if (INC ? ph == 0 : (ph > 0 && bf.U32[0] != nullptr)) return;  // the other kernel's pass
+  const bool pred = !INC && ph == 0;
   const int par = ctl->parity;
   const int NR = tb.NR, NT = tb.NT, NZ = tb.NZ, NTNZ = tb.NTNZ;
   const long long S = tb.S;
@@ -221,126 +208,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   // right-hand side is then d_im N(u_i) + rhsw' (addRHS_k + addLaplacian), with no
   // stencil, no +/- conversion and no read of u^n.  (The mixed form's increment
   // passes need no rhsw': its predictor stores N(u^n) there instead.)
-  if constexpr (INC && IP) {
-    // B''. The increment predictor's right-hand side Delta (see above), into the FP32
-    // halves of the line slots; RHSW and NP take N(u^n).
-    const double hidt = 0.5 * tb.inv_dt, hdim = 0.5 * tb.d_im, hw = 0.5 * tb.one_m_dim, hc = 0.5 * c_ex;
-    const float hidt32 = f64_to_f32(hidt), hdim32 = f64_to_f32(hdim), hw32 = f64_to_f32(hw), hcf = f64_to_f32(hc);
-    const float2* Un32 = (par ? bf.U32[1] : bf.U32[0]) + (size_t)mloc * 3 * S;  // u^n's mirror: the transforms' input
-    const double2* Uo = Ui;     // u^{n-1}, until stage I writes u^*
-    const float2* Uo32 = Ui32;  // its FP32 mirror
-    double2* Np = bf.NP + (size_t)mloc * 3 * S;
-    const float* Luc32 = tb.Luc32 + (size_t)ps * 2 * STEN * NR;
-    const float* mean = bf.MEAN + (size_t)mloc * NR * MEAN_N;
-    for (int p = tid; p < LN; p += nth) {
-      const int i = p / LM, mm = p - i * LM, k = k0 + mm;
-      if (k >= NTNZ) {
-        for (int c = 0; c < 3; c++) f32slot(R, c * LN + p) = make_float2(0.f, 0.f);
-        continue;
-      }
-      const int par_m = spar[mm];
-      const int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
-      const int lo = (1 - par_m) * STEN * NR + STEN * i + i0;  // u_r, u_theta rows (odd flag)
-      const int le = par_m * STEN * NR + STEN * i + i0;        // u_z rows
-      const size_t h = (size_t)i * NTNZ + k;
-      if (!NSP_IN_BOUNDS(tb, h, S, BC_LIN_POINT) || !NSP_IN_BOUNDS(tb, lo + len - 1, 2 * STEN * NR, BC_LIN_TAP) ||
-          !NSP_IN_BOUNDS(tb, le + len - 1, 2 * STEN * NR, BC_LIN_TAP) ||
-          !NSP_IN_BOUNDS(tb, (size_t)(left + len - 1) * NTNZ + k, S, BC_LIN_TAP))
-        continue;
-      if (k != 0) {
-        float2 nf[3], d[3];
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-          const double2 n = Nn[c * S + h], a = Un[c * S + h], b = Uo[c * S + h];
-          nf[c] = make_float2(f64_to_f32(n.x), f64_to_f32(n.y));
-          d[c] = make_float2(f64_to_f32(a.x - b.x), f64_to_f32(a.y - b.y));  // u^n - u^{n-1}, FP64 difference
-        }
-        if (!sdrop[mm]) {  // the mean-flow terms of N(u^n) (nsp_state.cuh)
-          const float2 fur = __ldg(Un32 + h), fut = __ldg(Un32 + S + h), fuz = __ldg(Un32 + 2 * S + h);
-          const Mean32 mf = mean_flow32_rec(tb, mean, i);
-#pragma unroll
-          for (int c = 0; c < 3; c++) {
-            const float2 ml = mean_terms32(mf, c, false, skt32[mm], skz32[mm], fur, fut, fuz);
-            nf[c].x += ml.x;
-            nf[c].y += ml.y;
-          }
-        }
-        // (1-d_im)/(2 Re) L+- (u^n - u^{n-1}) in FP32: the stencil on the mirrors' difference,
-        // the diagonal terms on the FP64 difference
-        float2 fr = make_float2(0.f, 0.f), ft = fr, fz = fr;
-        for (int j = 0; j < len; j++) {
-          const float a = __ldg(Luc32 + lo + j), b = __ldg(Luc32 + le + j);
-          const size_t hj = (size_t)(left + j) * NTNZ + k;
-          const float2 ar = __ldg(Un32 + hj), br = __ldg(Uo32 + hj), at = __ldg(Un32 + S + hj), bt = __ldg(Uo32 + S + hj);
-          const float2 az = __ldg(Un32 + 2 * S + hj), bz = __ldg(Uo32 + 2 * S + hj);
-          fr.x = fmaf(a, ar.x - br.x, fr.x); fr.y = fmaf(a, ar.y - br.y, fr.y);
-          ft.x = fmaf(a, at.x - bt.x, ft.x); ft.y = fmaf(a, at.y - bt.y, ft.y);
-          fz.x = fmaf(b, az.x - bz.x, fz.x); fz.y = fmaf(b, az.y - bz.y, fz.y);
-        }
-        const float ri = tb.rinv32[i], ir2f = ri * ri;
-        const float basef = fmaf(snkt2_32[mm], ir2f, snkz2_32[mm]);  // -k_z^2 - k_theta^2 / r^2
-        const float hzf = hcf * basef, hsf = hcf * (basef - ir2f), hdf = shdk32[mm] * ir2f;
-        fr.x += fmaf(hsf, d[0].x, -hdf * d[1].y);
-        fr.y += fmaf(hsf, d[0].y, hdf * d[1].x);
-        ft.x += fmaf(hsf, d[1].x, hdf * d[0].y);
-        ft.y += fmaf(hsf, d[1].y, -hdf * d[0].x);
-        fz.x += hzf * d[2].x;
-        fz.y += hzf * d[2].y;
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-          const double2 nl = Rw[c * S + h], np = Np[c * S + h];
-          const float2 f = c == 0 ? fr : (c == 1 ? ft : fz);
-          float2 dl;
-          dl.x = fmaf(0.5f, nf[c].x, fmaf(-hdim32, f64_to_f32(nl.x), fmaf(-hw32, f64_to_f32(np.x), fmaf(hidt32, d[c].x, f.x))));
-          dl.y = fmaf(0.5f, nf[c].y, fmaf(-hdim32, f64_to_f32(nl.y), fmaf(-hw32, f64_to_f32(np.y), fmaf(hidt32, d[c].y, f.y))));
-          f32slot(R, c * LN + p) = dl;
-          const double2 w = c2(f32_to_f64(nf[c].x), f32_to_f64(nf[c].y));
-          Rw[c * S + h] = w;  // N(u^n): the first increment corrector's N_{i-1}
-          Np[c * S + h] = w;  // and the next increment predictor's N(u^{n-1})
-        }
-      } else {  // the mean mode in FP64 (its Laplacian is steady: FP32 rounding there would add up)
-        const double ir2 = tb.rinv2[i];
-        const double base = fma(snkt2[mm], ir2, snkz2[mm]);
-        const double hz = fma(hc, base, hidt), hs = fma(-hc, ir2, hz), hd = shdk[mm] * ir2;
-        double2 lr = c2(0, 0), lt = c2(0, 0), lz = c2(0, 0);
-        for (int j = 0; j < len; j++) {
-          const double a = __ldg(Luc + lo + j), b = __ldg(Luc + le + j);
-          const size_t hj = (size_t)(left + j) * NTNZ + k;
-          const double2 vr = Un[hj], wr = Uo[hj], vt = Un[S + hj], wt = Uo[S + hj], vz = Un[2 * S + hj], wz = Uo[2 * S + hj];
-          lr.x += a * (vr.x - wr.x); lr.y += a * (vr.y - wr.y);
-          lt.x += a * (vt.x - wt.x); lt.y += a * (vt.y - wt.y);
-          lz.x += b * (vz.x - wz.x); lz.y += b * (vz.y - wz.y);
-        }
-        double2 du[3];
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-          const double2 a = Un[c * S + h], b = Uo[c * S + h];
-          du[c] = c2(a.x - b.x, a.y - b.y);
-        }
-        const double2 er = c2(lr.x + hs * du[0].x - hd * du[1].y, lr.y + hs * du[0].y + hd * du[1].x);
-        const double2 et = c2(lt.x + hs * du[1].x + hd * du[0].y, lt.y + hs * du[1].y - hd * du[0].x);
-        const double2 ez = c2(lz.x + hz * du[2].x, lz.y + hz * du[2].y);
-        double2 nr = Nn[h], nt = Nn[S + h], nz = Nn[2 * S + h];
-        {  // the mean flow's own terms (nsp_state.cuh)
-          const Mean32 mf = mean_flow32_rec(tb, mean, i);
-          const float2 vr = make_float2(mean[(size_t)i * MEAN_N + MEAN_V], 0.f), zero = make_float2(0.f, 0.f);
-          nr.x = f32_to_f64(f64_to_f32(nr.x) + mean_terms32(mf, 0, true, 0.f, 0.f, vr, zero, zero).x);
-          nt.x = f32_to_f64(f64_to_f32(nt.x) + mean_terms32(mf, 1, true, 0.f, 0.f, vr, zero, zero).x);
-          nz.x += (double)mean_terms32(mf, 2, true, 0.f, 0.f, vr, zero, zero).x;
-        }
-        const double2 nfv[3] = {nr, nt, nz}, ev[3] = {er, et, ez};
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-          const double2 nl = Rw[c * S + h], np = Np[c * S + h];
-          const double dx = 0.5 * nfv[c].x - hdim * nl.x - hw * np.x + ev[c].x;
-          const double dy = 0.5 * nfv[c].y - hdim * nl.y - hw * np.y + ev[c].y;
-          f32slot(R, c * LN + p) = make_float2(f64_to_f32(dx), f64_to_f32(dy));
-          Rw[c * S + h] = nfv[c];
-          Np[c * S + h] = nfv[c];
-        }
-      }
-    }
-  } else if (pred) {
+  if (pred) {
     // e = u^n/dt + (1-d_im)/Re (L_r - k_z^2 - m^2/r^2 [-1/r^2 -+ 2m/r^2]) u^n on the +/- lines
     // (addLaplacian), evaluated in r/theta form: with dd+- the two diagonals,
     // s = (dd+ + dd-)/2 and d = (dd+ - dd-)/2,
@@ -414,7 +282,6 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
 #pragma unroll
         for (int c = 0; c < 3; c++) {
           Rw[c * S + h] = c2(f32_to_f64(nf[c].x), f32_to_f64(nf[c].y));  // full N(u^n) for the first increment pass
-          bf.NP[(size_t)mloc * 3 * S + c * S + h] = Rw[c * S + h];       // and for the next increment predictor
           const float2 f = c == 0 ? fr : (c == 1 ? ft : fz);
           const float gx = fmaf(0.5f, nf[c].x, f.x), gy = fmaf(0.5f, nf[c].y, f.y);
           // widening on the integer pipe (the hardware conversion issues on the FP64 pipe)
@@ -454,10 +321,8 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       R[p] = c2(0.5 * nr.x + er.x, 0.5 * nr.y + er.y);
       R[LN + p] = c2(0.5 * nt.x + et.x, 0.5 * nt.y + et.y);
       R[2 * LN + p] = c2(0.5 * nz.x + ez.x, 0.5 * nz.y + ez.y);
-      if (Un32) {  // mixed form: N(u^n) for the first increment pass and the next increment predictor
+      if (Un32) {  // mixed form: N(u^n) for the first increment pass
         Rw[h] = nr; Rw[S + h] = nt; Rw[2 * S + h] = nz;
-        double2* Np = bf.NP + (size_t)mloc * 3 * S;
-        Np[h] = nr; Np[S + h] = nt; Np[2 * S + h] = nz;
       } else {
         Rw[h] = c2(hw * nr.x + er.x, hw * nr.y + er.y);
         Rw[S + h] = c2(hw * nt.x + et.x, hw * nt.y + et.y);
@@ -782,16 +647,15 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   bool nonfin = false;
   constexpr int UI = 2;  // points per thread whose previous-iterate loads are issued together
   for (int pb = tid; pb < LN; pb += UI * nth) {
-    double2 o[UI][3];  // the base of the update: u_i (correctors), u^n (increment predictor)
-    if (!pred || IP) {
-      const double2* base = IP ? Un : Ui;
+    double2 o[UI][3];
+    if (!pred) {
 #pragma unroll
       for (int u = 0; u < UI; u++) {
         const int p = pb + u * nth, i = p / LM, k = k0 + p - i * LM;
         const bool ok = p < LN && k < NTNZ && NSP_IN_BOUNDS(tb, (size_t)i * NTNZ + k, S, BC_LIN_POINT);
         const size_t h = ok ? (size_t)i * NTNZ + k : 0;
 #pragma unroll
-        for (int c = 0; c < 3; c++) o[u][c] = ok ? base[c * S + h] : c2(0, 0);
+        for (int c = 0; c < 3; c++) o[u][c] = ok ? Ui[c * S + h] : c2(0, 0);
       }
     }
 #pragma unroll
@@ -803,10 +667,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
 #pragma unroll
       for (int c = 0; c < 3; c++) {
         double2 v;
-        if constexpr (INC && IP) {  // u^* = u^n + the pass's result
-          const float2 f = f32slot(R, c * LN + p);
-          v = c2(o[u][c].x + f32_to_f64(f.x), o[u][c].y + f32_to_f64(f.y));
-        } else if constexpr (INC) {
+        if constexpr (INC) {
           // |increment|^2 and |u_i|^2 in FP32 (the measure only decides err > tol)
           const float2 f = f32slot(R, c * LN + p);
           const float ox = f64_to_f32(o[u][c].x), oy = f64_to_f32(o[u][c].y);
@@ -833,7 +694,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     }
   }
   if (nonfin) bad = 1;
-  if constexpr (INC && !IP) {  // float -> double is exact and monotonic; the increment is hdi x the pass's result
+  if constexpr (INC) {  // float -> double is exact and monotonic; the increment is hdi x the pass's result
     lnum = (unsigned long long)__double_as_longlong(f32_to_f64(__uint_as_float(lnum32)) * (hdi * hdi));
     lden = (unsigned long long)__double_as_longlong(f32_to_f64(__uint_as_float(lden32)));
   }
@@ -1097,20 +958,17 @@ void configure_linear_kernels() {
   const int big = 200 * 1024;
 #define NSP_LIN_CFG(v, lm, nth)                                                                        \
   cudaFuncSetAttribute(linear_k<lm, nth, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big); \
-  cudaFuncSetAttribute(linear_k<lm, nth, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);  \
-  cudaFuncSetAttribute(linear_k<lm, nth, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(linear_k<lm, nth, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   NSP_LIN_SHAPES(NSP_LIN_CFG)
 #undef NSP_LIN_CFG
 }
 
 void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st, int which) {
-  // The full pass, then in the mixed form the increment pass (correctors) and the
-  // increment predictor (the increment pass's block shape); each returns at once in the
-  // other kernels' passes.
+  // The full pass, then in the mixed form the increment pass (correctors), each with
+  // its own block shape; each returns at once in the other's passes.
   const bool mixed = bf.U32[0] != nullptr;
-  for (int pass = 0; pass < 3; pass++) {
-    static const int bit[3] = {LIN_PRED, LIN_CORR, LIN_PINC};
-    if (mixed ? !(which & bit[pass]) : (pass != 0 || which == 0)) continue;
+  for (int pass = 0; pass < 2; pass++) {
+    if (mixed ? !(which & (pass ? LIN_CORR : LIN_PRED)) : (pass == 1 || which == 0)) continue;
     const int want = pass ? tb.lin_variant_inc : tb.lin_variant;
     const int v = linear_variant_fits(want, tb.NR) ? want : linear_default_variant(tb.NR);
     const LinShape s = kLinShapes[v];
@@ -1119,8 +977,7 @@ void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st,
     switch (v) {
 #define NSP_LIN_CASE(v, lm, nth)                                                          \
   case v:                                                                                \
-    if (pass == 2) linear_k<lm, nth, true, true><<<grid, nth, smem, st>>>(tb, bf, dctl);  \
-    else if (pass) linear_k<lm, nth, true><<<grid, nth, smem, st>>>(tb, bf, dctl);       \
+    if (pass) linear_k<lm, nth, true><<<grid, nth, smem, st>>>(tb, bf, dctl);            \
     else linear_k<lm, nth, false><<<grid, nth, smem, st>>>(tb, bf, dctl);                \
     break;
       NSP_LIN_SHAPES(NSP_LIN_CASE)

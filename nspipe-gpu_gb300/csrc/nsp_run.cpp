@@ -644,8 +644,6 @@ int write_checkpoint(nsp_run* r) {
       remove_checkpoint_dir(join(r->ckpt_dir, step_dir_name(fs.first)));
     }
   }
-  // A run resumed from this checkpoint starts from the state alone; so does this one.
-  nsp::ctx_restart_predictor(r->ctx);
   return NSP_OK;
 }
 

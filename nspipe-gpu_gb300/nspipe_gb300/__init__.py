@@ -373,9 +373,8 @@ class Stepper:
         return ms
 
     def profile_linear(self, reps=5):
-        """Average ms per launch of the linear pass: [predictor (full pass), corrector pass,
-        increment predictor (mixed form; 0 in FP64)]."""
-        ms = np.zeros(3)
+        """Average ms per launch of the linear pass: [predictor pass, corrector pass]."""
+        ms = np.zeros(2)
         self._check(lib().nsp_profile_linear(self._h, reps, _dp(ms)))
         return ms
 
