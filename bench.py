@@ -405,15 +405,16 @@ def main():
         roofline["compute_bound"] = "fp64"
         roofline["fp64"] = {"achieved_tflops": ach, "peak_tflops": fp64_peak, "frac": ach / fp64_peak,
                             "algorithmic_flops_per_launch": fl, "peak_source": "measured live (nsp_measure_fp64_peak)"}
-        # The corrector pass.  Mixed form (the increment pass): about 150 FP64 flops per
-        # point (banded solves 104, influence correction 30, update 12; its stencils are
-        # FP32).  FP64 form: 242 (right-hand side 12, divergence 37, pressure solve 26,
-        # gradient and +/- 41, Helmholtz solves 78, correction 30, convergence measure 18).
-        # Bytes: read N, RHSW, V, u_i, write u_{i+1} (15 x 16 per point); mixed, also the
-        # RHSW update (3 x 16) and the FP32 mirror and its d_r (6 x 8).
+        # The corrector pass.  Mixed form (the increment pass): about 116 FP64 flops per
+        # point (banded solves 104, update 12; its stencils, influence correction and flux
+        # fix are FP32 on the increment).  FP64 form: 242 (right-hand side 12, divergence
+        # 37, pressure solve 26, gradient and +/- 41, Helmholtz solves 78, correction 30,
+        # convergence measure 18).  Bytes per point: FP64 form, read N, RHSW, V, u_i, write
+        # u_{i+1} (15 x 16); mixed, read N, RHSW, u_i (9 x 16) and the FP32 copies of V and
+        # u_i (6 x 8), write u_{i+1} and RHSW (6 x 16), the FP32 mirror and its d_r (6 x 8).
         lin = st.profile_linear(5)
-        fl_c = (150.0 if prec == nsp.NSP_MIXED else 242.0) * S * M
-        by_c = M * S * ((18 * 16 + 6 * 8) if prec == nsp.NSP_MIXED else 15 * 16)
+        fl_c = (116.0 if prec == nsp.NSP_MIXED else 242.0) * S * M
+        by_c = M * S * ((15 * 16 + 12 * 8) if prec == nsp.NSP_MIXED else 15 * 16)
         roofline["corrector"] = {"launch_ms": float(lin[1]), "fp64_frac": fl_c / (lin[1] * 1e-3) / 1e12 / fp64_peak,
                                  "hbm_frac": by_c / (lin[1] * 1e-3) / 1e9 / peak,
                                  "algorithmic_flops_per_launch": fl_c, "algorithmic_bytes_per_launch": by_c}
