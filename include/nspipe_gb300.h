@@ -165,7 +165,9 @@ int nsp_nonlinear_static(nsp_ctx* ctx, int member, const void* u3, void* n3);
 
 /* One banded solve on one member's operators (LUsolve_u flag 0/1/2 and LUsolve_p,
  * mod_linear.cu:664-679): kind 0 = u+, 1 = u-, 2 = u_z, 3 = pressure.  rhs and sol
- * are device arrays of NR*NT*NZ complex doubles (rhs is not modified). */
+ * are device arrays of NR*NT*NZ complex doubles (rhs is not modified).  Kinds 4..7:
+ * the solve of kind - 4 in double-float (FP32 pairs, about 48 bits), the form the
+ * mixed form's corrector passes use; mixed-form contexts only (NSP_ERR_ARG otherwise). */
 int nsp_lusolve(nsp_ctx* ctx, int member, int kind, const void* rhs, void* sol);
 
 /* Diagnostics of one member (synchronises the context's stream). */

@@ -36,7 +36,7 @@ CU_UNITS = ["nsp_api.cu", "nsp_linear.cu", "nsp_transform.cu", "nsp_noalloc.cu",
 CU_EXTRA = {"nsp_setup_dev.cu": ["-fmad=false"]}
 CXX_UNITS = ["nsp_setup.cpp", "nsp_run.cpp"]
 HEADERS = ["nsp_internal.h", "nsp_setup_mode.h", "nsp_fft.cuh", "nsp_cvt.cuh", "nsp_state.cuh", "nsp_tc.cuh",
-           "nsp_bounds.cuh", os.path.join("..", "..", "include", "nspipe_gb300.h")]
+           "nsp_bounds.cuh", "nsp_df.cuh", os.path.join("..", "..", "include", "nspipe_gb300.h")]
 
 
 def _stale(obj, src):

@@ -179,6 +179,7 @@ Tables member_view(const Group& g, int slot) {
   t.fac += (size_t)ps * 4 * t.NR * NFAC * t.NTNZ;
   t.V += (size_t)ps * 3 * t.S;
   if (t.V32) t.V32 += (size_t)ps * 3 * t.S;
+  if (t.facdf) t.facdf += (size_t)ps * 4 * t.NR * NFAC * t.NTNZ;
   t.Luc += (size_t)ps * 2 * STEN * t.NR;
   t.Luc32 += (size_t)ps * 2 * STEN * t.NR;
   t.uc += (size_t)ps * t.NR;
@@ -755,12 +756,15 @@ int nsp_setup(nsp_ctx* c) {
     }
     tb.nsets = nsets;
     tb.V32 = nullptr;
-    if (c->precision == NSP_MIXED) {  // FP32 copy of the correction profiles for the increment passes
-      float2* v32 = nullptr;
-      if ((rc = dalloc(c, &v32, sizeof(float2) * V_n))) return rc;
+    tb.facdf = nullptr;
+    if (c->precision == NSP_MIXED) {  // the increment passes' FP32 correction profiles and double-float factors
+      float2 *v32 = nullptr, *fdf = nullptr;
+      if ((rc = dalloc(c, &v32, sizeof(float2) * V_n)) || (rc = dalloc(c, &fdf, sizeof(float2) * fac_n))) return rc;
       launch_to_f32(tb.V, v32, (long long)V_n, c->st);
+      launch_split_df(tb.fac, fdf, (long long)fac_n, c->st);
       CK(cudaGetLastError());
       tb.V32 = v32;
+      tb.facdf = fdf;
     }
     std::vector<double2> wt = twiddles(tb.NTP), wz = twiddles(tb.NZR);
     if ((rc = upload(c, &tb.tw_t, wt)) || (rc = upload(c, &tb.tw_z, wz)) || (rc = upload(c, &tb.tw_t32, to_f32(wt))) ||
@@ -1293,8 +1297,9 @@ int nsp_nonlinear_static(nsp_ctx* c, int m, const void* u3, void* n3) {
 int nsp_lusolve(nsp_ctx* c, int m, int kind, const void* rhs, void* sol) {
   if (int rc = check_member(c, m)) return rc;
   if (!c->setup_done) return fail(c, NSP_ERR_STATE, "nsp_lusolve before nsp_setup");
-  if (kind < 0 || kind > 3) return fail(c, NSP_ERR_ARG, "kind %d not in 0..3", kind);
+  if (kind < 0 || kind > 7) return fail(c, NSP_ERR_ARG, "kind %d not in 0..7", kind);
   const Tables tv = member_view(c->groups[c->grp[m]], c->slot[m]);
+  if (kind > 3 && !tv.facdf) return fail(c, NSP_ERR_ARG, "kind %d (double-float solve): mixed-form contexts only", kind);
   launch_lusolve(tv, kind, (const double2*)rhs, (double2*)sol, c->st);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(c->st));

@@ -53,6 +53,7 @@ struct Tables {
   const double* fac;   // [4][NR][7][NTNZ]: banded LU factors of u+, u-, u_z, p
   const double2* V;    // [3][NR][NTNZ]: influence-matrix correction profiles (+, -, z)
   const float2* V32;   // mixed form: the same in FP32 (the corrector increments' correction)
+  const float2* facdf;  // mixed form: fac as double-float pairs (hi, lo) (the increment passes' solves)
   const double2* tw_t; // [NTP] exp(-2 pi i e/NTP), FP64
   const double2* tw_z; // [NZR]
   const float2* tw_t32;
@@ -154,6 +155,7 @@ size_t noalloc_scratch_bytes();
 cudaError_t noalloc_scratch(int device, void** ptr);
 // FP32 copy of nmem x 3 x S complex values (the mixed form's transform input).
 void launch_to_f32(const double2* src, float2* dst, long long n, cudaStream_t st);
+void launch_split_df(const double* src, float2* dst, long long n, cudaStream_t st);
 // The FP32 mirror and its radial derivative (DR32) of a group's state U (mixed form).
 void launch_mirror(const Tables& tb, const double2* U, float2* U32, float2* DR32, cudaStream_t st);
 int kernels_per_nonlinear();

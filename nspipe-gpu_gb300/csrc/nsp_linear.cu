@@ -21,6 +21,7 @@
 
 #include "nsp_bounds.cuh"
 #include "nsp_cvt.cuh"
+#include "nsp_df.cuh"
 #include "nsp_fft.cuh"
 #include "nsp_internal.h"
 #include "nsp_state.cuh"
@@ -57,22 +58,47 @@ __device__ __forceinline__ void bwd_row(V& x, const double* u, V& xp1, V& xp2, V
   xp3 = xp2; xp2 = xp1; xp1 = x;
 }
 
+// The same rows in double-float (nsp_df.cuh): one part of a line, factors split the same way.
+__device__ __forceinline__ void fwd_row(dfloat& x, const dfloat* l, dfloat& xm1, dfloat& xm2, dfloat& xm3) {
+  float s = x.hi, t = x.lo;
+  df_sub_prod(s, t, l[0], xm3);
+  df_sub_prod(s, t, l[1], xm2);
+  df_sub_prod(s, t, l[2], xm1);
+  x = df_norm(s, t);
+  xm3 = xm2; xm2 = xm1; xm1 = x;
+}
+__device__ __forceinline__ void bwd_row(dfloat& x, const dfloat* u, dfloat& xp1, dfloat& xp2, dfloat& xp3) {
+  float s = x.hi, t = x.lo;
+  df_sub_prod(s, t, u[0], xp3);
+  df_sub_prod(s, t, u[1], xp2);
+  df_sub_prod(s, t, u[2], xp1);
+  x = df_mul(df_norm(s, t), u[3]);
+  xp3 = xp2; xp2 = xp1; xp1 = x;
+}
+
+__device__ __forceinline__ double ldf(const double* p) { return __ldg(p); }
+__device__ __forceinline__ dfloat ldf(const dfloat* p) {
+  const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+  return dfloat{v.x, v.y};
+}
+
 // Forward + backward substitution of one mode line held in X[i*ld] (i = 0..NR-1):
 // V = double2 solves the complex line, V = double one of its parts (the factors are
 // real, so the real and imaginary parts are independent solves and two threads can
-// share a line).  Factor rows are fetched four at a time so that their L2 latencies overlap.
-template <typename V>
-__device__ __forceinline__ void solve_line(V* X, int ld, const double* __restrict__ f, int NTNZ, int NR) {
+// share a line), V = dfloat one part in double-float with the factors F = dfloat.
+// Factor rows are fetched four at a time so that their L2 latencies overlap.
+template <typename V, typename F>
+__device__ __forceinline__ void solve_line(V* X, int ld, const F* __restrict__ f, int NTNZ, int NR) {
   const size_t rs = (size_t)NFAC * NTNZ;  // row stride of the factor table
   V xm1{}, xm2{}, xm3{};
   int i = 0;
   for (; i + 4 <= NR; i += 4) {
-    double l[4][3];
+    F l[4][3];
     V b[4];
 #pragma unroll
     for (int r = 0; r < 4; r++) {
-      const double* fr = f + (i + r) * rs;
-      l[r][0] = __ldg(fr); l[r][1] = __ldg(fr + NTNZ); l[r][2] = __ldg(fr + 2 * NTNZ);
+      const F* fr = f + (i + r) * rs;
+      l[r][0] = ldf(fr); l[r][1] = ldf(fr + NTNZ); l[r][2] = ldf(fr + 2 * NTNZ);
       b[r] = X[(i + r) * ld];
     }
 #pragma unroll
@@ -82,8 +108,8 @@ __device__ __forceinline__ void solve_line(V* X, int ld, const double* __restric
     }
   }
   for (; i < NR; i++) {
-    const double* fr = f + i * rs;
-    double l[3] = {__ldg(fr), __ldg(fr + NTNZ), __ldg(fr + 2 * NTNZ)};
+    const F* fr = f + i * rs;
+    F l[3] = {ldf(fr), ldf(fr + NTNZ), ldf(fr + 2 * NTNZ)};
     V x = X[i * ld];
     fwd_row(x, l, xm1, xm2, xm3);
     X[i * ld] = x;
@@ -91,13 +117,13 @@ __device__ __forceinline__ void solve_line(V* X, int ld, const double* __restric
   V xp1{}, xp2{}, xp3{};
   i = NR - 1;
   for (; i >= 3; i -= 4) {
-    double u[4][4];
+    F u[4][4];
     V b[4];
 #pragma unroll
     for (int r = 0; r < 4; r++) {
-      const double* fr = f + (i - r) * rs;
-      u[r][0] = __ldg(fr + 6 * NTNZ); u[r][1] = __ldg(fr + 5 * NTNZ);
-      u[r][2] = __ldg(fr + 4 * NTNZ); u[r][3] = __ldg(fr + 3 * NTNZ);
+      const F* fr = f + (i - r) * rs;
+      u[r][0] = ldf(fr + 6 * NTNZ); u[r][1] = ldf(fr + 5 * NTNZ);
+      u[r][2] = ldf(fr + 4 * NTNZ); u[r][3] = ldf(fr + 3 * NTNZ);
       b[r] = X[(i - r) * ld];
     }
 #pragma unroll
@@ -107,8 +133,8 @@ __device__ __forceinline__ void solve_line(V* X, int ld, const double* __restric
     }
   }
   for (; i >= 0; i--) {
-    const double* fr = f + i * rs;
-    double u[4] = {__ldg(fr + 6 * NTNZ), __ldg(fr + 5 * NTNZ), __ldg(fr + 4 * NTNZ), __ldg(fr + 3 * NTNZ)};
+    const F* fr = f + i * rs;
+    F u[4] = {ldf(fr + 6 * NTNZ), ldf(fr + 5 * NTNZ), ldf(fr + 4 * NTNZ), ldf(fr + 3 * NTNZ)};
     V x = X[i * ld];
     bwd_row(x, u, xp1, xp2, xp3);
     X[i * ld] = x;
@@ -117,6 +143,25 @@ __device__ __forceinline__ void solve_line(V* X, int ld, const double* __restric
 
 // The low half of a line slot holds an FP32 pair in the increment passes.
 __device__ __forceinline__ float2& f32slot(double2* a, int e) { return reinterpret_cast<float2*>(a)[2 * e]; }
+// Around their banded solves the increment passes hold a line slot as two double-float
+// parts (re.hi, re.lo, im.hi, im.lo): the same 16 bytes, so the solve addresses one part
+// where the FP64 pass addresses one double.
+__device__ __forceinline__ float4& dfslot(double2* a, int e) { return reinterpret_cast<float4*>(a)[e]; }
+__device__ __forceinline__ void put_df(double2* a, int e, float x, float y) { dfslot(a, e) = make_float4(x, 0.f, y, 0.f); }
+// An FP64 value split into double-float: hi = fl32(x), lo = fl32(x - hi) (x - hi exact).
+__device__ __forceinline__ float2 split_df(double x) {
+  const float hi = f64_to_f32(x);
+  return make_float2(hi, f64_to_f32(x - f32_to_f64(hi)));
+}
+__device__ __forceinline__ void put_df(double2* a, int e, double2 v) {
+  const float2 x = split_df(v.x), y = split_df(v.y);
+  dfslot(a, e) = make_float4(x.x, x.y, y.x, y.y);
+}
+// A double-float slot's value in FP64 (the widenings on the integer pipe, one FP64 add).
+__device__ __forceinline__ double2 df_value(double2* a, int e) {
+  const float4 v = dfslot(a, e);
+  return make_double2(f32_to_f64(v.x) + f32_to_f64(v.y), f32_to_f64(v.z) + f32_to_f64(v.w));
+}
 
 // At least 1024 threads per SM resident (4 radial lines of 48 points x 16 modes
 // is 49 KB of shared memory, so four 256-thread blocks fit): 64 registers.
@@ -132,7 +177,12 @@ __device__ __forceinline__ float2& f32slot(double2* a, int e) { return reinterpr
 // update of u stay in FP64.  N_{i-1} is kept in RHSW (the predictor stores N(u^n)
 // there in the mixed form).  Without INC the kernel is the full pass, and in the
 // mixed form it takes only the predictor.
-template <int LM, int NTH, bool INC>
+//
+// DFS (mixed form, both passes): the banded solves in double-float (nsp_df.cuh) with
+// the factors split the same way, about 48 bits: the FP64 pipe's share of the pass was
+// mostly its banded solves.  In the full pass the solves' inputs are split from FP64
+// and their results summed back to FP64; the increment passes' inputs are FP32 already.
+template <int LM, int NTH, bool INC, bool DFS>
 __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 : (1024 / NTH)))
     linear_k(Tables tb, Bufs bf, Ctl* ctl) {
   const int mloc = blockIdx.y, gm = tb.mem0 + mloc;
@@ -423,11 +473,11 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   for (int p = tid; p < LN; p += nth) {
     int i = p / LM, mm = p - i * LM, k = k0 + mm;
     double2 d = c2(0, 0);
-    if constexpr (INC) {  // FP32 on the increment, widened for the FP64 solve
+    if constexpr (INC) {  // FP32 on the increment, into double-float for the solve
+      float sx = 0.f, sy = 0.f;
       if (k < NTNZ && i < NR - 1) {
         const int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
         const float* Dr = tb.Ddiv32 + (1 - spar[mm]) * STEN * NR + STEN * i + i0;
-        float sx = 0.f, sy = 0.f;
         for (int j = 0; j < len; j++) {
           const float de = __ldg(Dr + j);
           const float2 a = f32slot(R, (left + j) * LM + mm);
@@ -438,8 +488,9 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
         const float2 rt = f32slot(R, LN + p), rz = f32slot(R, 2 * LN + p);
         sx -= kti * rt.y; sy += kti * rt.x;
         sx -= kz * rz.y; sy += kz * rz.x;
-        d = c2(f32_to_f64(sx), f32_to_f64(sy));
       }
+      put_df(P, p, sx, sy);
+      continue;
     } else if (k < NTNZ && i < NR - 1) {
       double kt = skt[mm], kz = skz[mm];
       int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
@@ -459,7 +510,8 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       sx -= kz * rz.y; sy += kz * rz.x;
       d = c2(sx, sy);
     }
-    P[p] = d;
+    if constexpr (DFS) put_df(P, p, d);
+    else P[p] = d;
   }
   __syncthreads();
 
@@ -470,18 +522,29 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     return NSP_IN_BOUNDS(tb, ((size_t)c * NR + NR - 1) * NFAC * NTNZ + 6 * (size_t)NTNZ + k,
                          (size_t)4 * NR * NFAC * NTNZ, BC_LIN_FACTOR);
   };
+  // Increment passes: the solves in double-float (nsp_df.cuh) with the factors split the
+  // same way -- the FP64 pipe's share of this pass was almost all its banded solves.
+  const dfloat* facdf = reinterpret_cast<const dfloat*>(tb.facdf) + (size_t)ps * 4 * NR * NFAC * NTNZ;
   if (tid < 2 * LM) {
     const int mm = tid >> 1, part = tid & 1;
-    if (k0 + mm < NTNZ && fac_ok(3, k0 + mm))
-      solve_line(reinterpret_cast<double*>(P + mm) + part, 2 * LM, fac + 3 * (size_t)NR * NFAC * NTNZ + k0 + mm,
-                 NTNZ, NR);
+    if (k0 + mm < NTNZ && fac_ok(3, k0 + mm)) {
+      if constexpr (DFS)
+        solve_line(reinterpret_cast<dfloat*>(P + mm) + part, 2 * LM, facdf + 3 * (size_t)NR * NFAC * NTNZ + k0 + mm,
+                   NTNZ, NR);
+      else
+        solve_line(reinterpret_cast<double*>(P + mm) + part, 2 * LM, fac + 3 * (size_t)NR * NFAC * NTNZ + k0 + mm,
+                   NTNZ, NR);
+    }
   }
   __syncthreads();
-  if constexpr (INC) {  // the pressure increment to FP32, in place (each slot by its own thread)
+  if constexpr (INC) {  // the pressure increment to FP32 (hi = fl(hi + lo)), in place
     for (int p = tid; p < LN; p += nth) {
-      const double2 a = P[p];
-      f32slot(P, p) = make_float2(f64_to_f32(a.x), f64_to_f32(a.y));
+      const float4 a = dfslot(P, p);
+      f32slot(P, p) = make_float2(a.x, a.z);
     }
+    __syncthreads();
+  } else if constexpr (DFS) {  // the pressure back to FP64, in place
+    for (int p = tid; p < LN; p += nth) P[p] = df_value(P, p);
     __syncthreads();
   }
 
@@ -506,9 +569,10 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
         float2 rt = f32slot(R, LN + p), fz = f32slot(R, 2 * LN + p);
         rt.x += kti * pp.y; rt.y -= kti * pp.x;
         fz.x += kz * pp.y; fz.y -= kz * pp.x;
-        up = c2(f32_to_f64(rr.x - rt.y), f32_to_f64(rr.y + rt.x));
-        um = c2(f32_to_f64(rr.x + rt.y), f32_to_f64(rr.y - rt.x));
-        rz = c2(f32_to_f64(fz.x), f32_to_f64(fz.y));
+        put_df(R, p, rr.x - rt.y, rr.y + rt.x);
+        put_df(R, LN + p, rr.x + rt.y, rr.y - rt.x);
+        put_df(R, 2 * LN + p, fz.x, fz.y);
+        continue;
       }
     } else if (i < NR - 1) {
       double kt = skt[mm], kz = skz[mm];
@@ -530,7 +594,11 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       up = c2(rr.x - rt.y, rr.y + rt.x);
       um = c2(rr.x + rt.y, rr.y - rt.x);
     }
-    R[p] = up; R[LN + p] = um; R[2 * LN + p] = rz;
+    if constexpr (DFS) {
+      put_df(R, p, up); put_df(R, LN + p, um); put_df(R, 2 * LN + p, rz);
+    } else {
+      R[p] = up; R[LN + p] = um; R[2 * LN + p] = rz;
+    }
   }
   __syncthreads();
 
@@ -542,9 +610,14 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   if (tid >= F0 && tid < F0 + 6 * LM) {
     const int tf = tid - F0;
     const int c = tf / (2 * LM), rem = tf - c * 2 * LM, mm = rem >> 1, part = rem & 1;
-    if (k0 + mm < NTNZ && fac_ok(c, k0 + mm))
-      solve_line(reinterpret_cast<double*>(R + c * LN + mm) + part, 2 * LM,
-                 fac + (size_t)c * NR * NFAC * NTNZ + k0 + mm, NTNZ, NR);
+    if (k0 + mm < NTNZ && fac_ok(c, k0 + mm)) {
+      if constexpr (DFS)
+        solve_line(reinterpret_cast<dfloat*>(R + c * LN + mm) + part, 2 * LM,
+                   facdf + (size_t)c * NR * NFAC * NTNZ + k0 + mm, NTNZ, NR);
+      else
+        solve_line(reinterpret_cast<double*>(R + c * LN + mm) + part, 2 * LM,
+                   fac + (size_t)c * NR * NFAC * NTNZ + k0 + mm, NTNZ, NR);
+    }
   }
   __syncthreads();
 
@@ -560,14 +633,15 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       double2 urw = c2(0, 0), utw = c2(0, 0);
       for (int j = 0; j <= IW; j++) {
         int row = NR - 1 - IW + j;
-        double2 a = R[row * LM + mm], b = R[LN + row * LM + mm];
+        const double2 a = DFS ? df_value(R, row * LM + mm) : R[row * LM + mm];
+        const double2 b = DFS ? df_value(R, LN + row * LM + mm) : R[LN + row * LM + mm];
         double2 ur = c2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y));
         double de = __ldg(Dw + j);
         sx += de * ur.x;
         sy += de * ur.y;
         if (j == IW) { urw = ur; utw = c2(0.5 * (a.y - b.y), -0.5 * (a.x - b.x)); }
       }
-      double2 uzw = R[2 * LN + (NR - 1) * LM + mm];
+      const double2 uzw = DFS ? df_value(R, 2 * LN + (NR - 1) * LM + mm) : R[2 * LN + (NR - 1) * LM + mm];
       sx += urw.x; sy += urw.y;
       sx += -kt * utw.y; sy += kt * utw.x;
       sx += -kz * uzw.y; sy += kz * uzw.x;
@@ -589,9 +663,8 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       if (k >= NTNZ) continue;
       const size_t hv = (size_t)i * NTNZ + k;
       if (!NSP_IN_BOUNDS(tb, hv, S, BC_LIN_POINT)) continue;
-      const double2 a = R[p], b = R[LN + p], z = R[2 * LN + p];
-      float2 up = make_float2(f64_to_f32(a.x), f64_to_f32(a.y)), um = make_float2(f64_to_f32(b.x), f64_to_f32(b.y));
-      float2 uz = make_float2(f64_to_f32(z.x), f64_to_f32(z.y));
+      const float4 a = dfslot(R, p), b = dfslot(R, LN + p), z = dfslot(R, 2 * LN + p);  // FP32: the hi parts
+      float2 up = make_float2(a.x, a.z), um = make_float2(b.x, b.z), uz = make_float2(z.x, z.z);
       const float2 dv = dvs32[mm], v0 = Vp32[hv], v1 = Vp32[S + hv], v2 = Vp32[2 * S + hv];
       up.x += dv.x * v0.x - dv.y * v0.y; up.y += dv.x * v0.y + dv.y * v0.x;
       um.x += dv.x * v1.x - dv.y * v1.y; um.y += dv.x * v1.y + dv.y * v1.x;
@@ -605,7 +678,12 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   } else for (int p = tid; p < LN; p += nth) {
     int i = p / LM, mm = p - i * LM, k = k0 + mm;
     if (k >= NTNZ) continue;
-    double2 up = R[p], um = R[LN + p], uz = R[2 * LN + p];
+    double2 up, um, uz;
+    if constexpr (DFS) {
+      up = df_value(R, p); um = df_value(R, LN + p); uz = df_value(R, 2 * LN + p);
+    } else {
+      up = R[p]; um = R[LN + p]; uz = R[2 * LN + p];
+    }
     double2 dv = dvs[mm];
     size_t hv = (size_t)i * NTNZ + k;
     if (!NSP_IN_BOUNDS(tb, hv, S, BC_LIN_POINT)) continue;
@@ -922,11 +1000,36 @@ void launch_fp64_peak(double* out, int blocks, int threads, int iters, cudaStrea
   fp64_peak_k<<<blocks, threads, 0, st>>>(out, iters, 0.999999, 1e-7);
 }
 
+// kind 0..3: the FP64 solve; kind 4..7: the same operator's solve in double-float, as
+// the increment passes run it (the right-hand side split into hi + lo, the solution
+// returned as hi + lo in FP64).  One thread per mode line, or per part of one.
 __global__ void lusolve_k(Tables tb, int kind, const double2* rhs, double2* sol) {
   int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t fo = (size_t)(kind & 3) * tb.NR * NFAC * tb.NTNZ;
+  if (kind < 4) {
+    if (k >= tb.NTNZ) return;
+    for (int i = 0; i < tb.NR; i++) sol[(size_t)i * tb.NTNZ + k] = rhs[(size_t)i * tb.NTNZ + k];
+    solve_line(sol + k, tb.NTNZ, tb.fac + fo + k, tb.NTNZ, tb.NR);
+    return;
+  }
+  const int part = k & 1;
+  k >>= 1;
   if (k >= tb.NTNZ) return;
-  for (int i = 0; i < tb.NR; i++) sol[(size_t)i * tb.NTNZ + k] = rhs[(size_t)i * tb.NTNZ + k];
-  solve_line(sol + k, tb.NTNZ, tb.fac + (size_t)kind * tb.NR * NFAC * tb.NTNZ + k, tb.NTNZ, tb.NR);
+  const double* in = reinterpret_cast<const double*>(rhs) + part;
+  double* out = reinterpret_cast<double*>(sol) + part;
+  dfloat* X = reinterpret_cast<dfloat*>(out);  // the double slots of this part hold the double-float values
+  for (int i = 0; i < tb.NR; i++) {
+    const size_t h = 2 * ((size_t)i * tb.NTNZ + k);
+    const double x = in[h];
+    const float hi = f64_to_f32(x);
+    X[h] = dfloat{hi, f64_to_f32(x - f32_to_f64(hi))};
+  }
+  solve_line(X + 2 * (size_t)k, 2 * tb.NTNZ, reinterpret_cast<const dfloat*>(tb.facdf) + fo + k, tb.NTNZ, tb.NR);
+  for (int i = 0; i < tb.NR; i++) {
+    const size_t h = 2 * ((size_t)i * tb.NTNZ + k);
+    const dfloat v = X[h];
+    out[h] = f32_to_f64(v.hi) + f32_to_f64(v.lo);
+  }
 }
 
 // Block shapes of the linear pass (modes per block, threads): the candidates of the
@@ -957,8 +1060,9 @@ bool linear_variant_fits(int v, int NR) {
 void configure_linear_kernels() {
   const int big = 200 * 1024;
 #define NSP_LIN_CFG(v, lm, nth)                                                                        \
-  cudaFuncSetAttribute(linear_k<lm, nth, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big); \
-  cudaFuncSetAttribute(linear_k<lm, nth, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(linear_k<lm, nth, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big); \
+  cudaFuncSetAttribute(linear_k<lm, nth, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);  \
+  cudaFuncSetAttribute(linear_k<lm, nth, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
   NSP_LIN_SHAPES(NSP_LIN_CFG)
 #undef NSP_LIN_CFG
 }
@@ -977,8 +1081,9 @@ void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st,
     switch (v) {
 #define NSP_LIN_CASE(v, lm, nth)                                                          \
   case v:                                                                                \
-    if (pass) linear_k<lm, nth, true><<<grid, nth, smem, st>>>(tb, bf, dctl);            \
-    else linear_k<lm, nth, false><<<grid, nth, smem, st>>>(tb, bf, dctl);                \
+    if (pass) linear_k<lm, nth, true, true><<<grid, nth, smem, st>>>(tb, bf, dctl);      \
+    else if (mixed) linear_k<lm, nth, false, true><<<grid, nth, smem, st>>>(tb, bf, dctl); \
+    else linear_k<lm, nth, false, false><<<grid, nth, smem, st>>>(tb, bf, dctl);         \
     break;
       NSP_LIN_SHAPES(NSP_LIN_CASE)
 #undef NSP_LIN_CASE
@@ -995,7 +1100,8 @@ void launch_converge(Ctl* dctl, int nmem, unsigned long long cond_handle, int us
 void launch_finish_step(Ctl* dctl, cudaStream_t st) { finish_step_k<<<1, 1, 0, st>>>(dctl); }
 
 void launch_lusolve(const Tables& tb, int kind, const double2* rhs, double2* sol, cudaStream_t st) {
-  lusolve_k<<<(tb.NTNZ + 127) / 128, 128, 0, st>>>(tb, kind, rhs, sol);
+  const int n = kind < 4 ? tb.NTNZ : 2 * tb.NTNZ;
+  lusolve_k<<<(n + 127) / 128, 128, 0, st>>>(tb, kind, rhs, sol);
 }
 
 }  // namespace nsp

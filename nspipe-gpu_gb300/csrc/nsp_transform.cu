@@ -768,4 +768,19 @@ void launch_to_f32(const double2* src, float2* dst, long long n, cudaStream_t st
   to_f32_k<<<blocks, 256, 0, st>>>(src, dst, n);
 }
 
+// x = hi + lo with hi = fl32(x), lo = fl32(x - hi) (x - hi is exact in FP64): the
+// double-float form of set-up tables, about 48 bits of x.
+__global__ void split_df_k(const double* __restrict__ src, float2* __restrict__ dst, long long n) {
+  for (long long h = blockIdx.x * (long long)blockDim.x + threadIdx.x; h < n; h += (long long)gridDim.x * blockDim.x) {
+    const double x = src[h];
+    const float hi = f64_to_f32(x);
+    dst[h] = make_float2(hi, f64_to_f32(x - f32_to_f64(hi)));
+  }
+}
+
+void launch_split_df(const double* src, float2* dst, long long n, cudaStream_t st) {
+  int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
+  split_df_k<<<blocks, 256, 0, st>>>(src, dst, n);
+}
+
 }  // namespace nsp

@@ -74,6 +74,30 @@ def test_banded_solve_matches_oracle(nsp, orc, name, kind):
     st.close()
 
 
+@pytest.mark.parametrize("name", ["s1", "c0"])
+def test_double_float_solves_close_to_fp64(nsp, name):
+    """The mixed form's corrector solves in double-float (FP32 pairs, kinds 4..7) against
+    the FP64 solves of the same factors: relative L2 <= 1e-12 for the Helmholtz operators,
+    <= 1e-9 for the pressure operator (condition numbers up to ~1e6 on its high-m lines)."""
+    import torch
+    st = stepper(nsp, name, nsp.NSP_MIXED)
+    NR, NT, NZ = CFG[name][:3]
+    rng = np.random.default_rng(7)
+    for kind in range(4):
+        b = rng.standard_normal((NR, NT, NZ)) + 1j * rng.standard_normal((NR, NT, NZ))
+        x64 = torch.zeros(b.shape, dtype=torch.complex128, device="cuda")
+        xdf = torch.zeros_like(x64)
+        st.lusolve(0, kind, dev(b), x64)
+        st.lusolve(0, kind + 4, dev(b), xdf)
+        err = rel(xdf.cpu().numpy(), x64.cpu().numpy())
+        assert err <= (1e-9 if kind == 3 else 1e-12), (kind, err)
+    st.close()
+    st = stepper(nsp, name, nsp.NSP_FP64)
+    with pytest.raises(nsp.NspError):
+        st.lusolve(0, 4, dev(np.zeros((NR, NT, NZ), complex)), torch.zeros((NR, NT, NZ), dtype=torch.complex128, device="cuda"))
+    st.close()
+
+
 @pytest.mark.parametrize("name", ["s1", "s2", "c0"])
 @pytest.mark.parametrize("precision,tol", [(0, 1e-13), (1, 2e-6)])
 def test_nonlinear_matches_oracle(nsp, orc, name, precision, tol):
