@@ -141,6 +141,121 @@ __device__ __forceinline__ void solve_line(V* X, int ld, const F* __restrict__ f
   }
 }
 
+// 8-byte asynchronous copies global -> shared (cp.async), their groups and waits.
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// Depth of the factor ring of the double-float solves, in batches of four rows.
+constexpr int RING_B = 3;
+// Shared memory of one kind's ring: [RING_B][4 rows][4 slots][LM] double-float factors.
+constexpr size_t ring_bytes(int LM) { return (size_t)RING_B * 16 * LM * sizeof(dfloat); }
+// Dynamic shared memory of a linear-pass block beyond its 4 radial lines (mixed form): the
+// pressure solve's ring, and with the pressure line, which is dead by then, the three
+// Helmholtz solves' rings.
+inline size_t ring_extra(int NR, int LM) {
+  const size_t pl = sizeof(double2) * (size_t)NR * LM, r = ring_bytes(LM);
+  return 3 * r > pl + r ? 3 * r - pl : r;
+}
+
+// solve_line<dfloat, dfloat> with the factor rows staged through a shared-memory ring:
+// the copies of batch b + RING_B - 1 are in flight while batch b computes, so the rows
+// wait on shared memory instead of L2.  The two threads of a line (part 0 and 1, adjacent
+// lanes, both calling) share the copies -- part 0 fetches slots 0-1, part 1 slots 2-3 --
+// and meet at __syncwarp(pair) after each wait and before a slot is refilled.  Slots:
+// forward L(i-3), L(i-2), L(i-1); backward U(i+3), U(i+2), U(i+1), 1/U_ii.  Rows past the
+// last full batch read the table directly.
+template <int LM>
+__device__ __forceinline__ void solve_line_ring(dfloat* X, int ld, const dfloat* __restrict__ f, int NTNZ, int NR,
+                                                dfloat* ring, int mm, int part, unsigned pair) {
+  const size_t rs = (size_t)NFAC * NTNZ;
+  const int nb = NR / 4;
+  auto issue = [&](int b, bool fwd) {
+    dfloat* dst = ring + (b % RING_B) * 16 * LM + mm;
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      const int row = fwd ? 4 * b + r : NR - 1 - 4 * b - r;
+#pragma unroll
+      for (int q = 0; q < 2; q++) {
+        const int slot = 2 * part + q, e = fwd ? slot : 6 - slot;
+        if (!fwd || slot < 3) cp_async8(dst + (r * 4 + slot) * LM, f + row * rs + (size_t)e * NTNZ);
+      }
+    }
+  };
+  dfloat xm1{}, xm2{}, xm3{};
+#pragma unroll
+  for (int b = 0; b < RING_B - 1; b++) {
+    if (b < nb) issue(b, true);
+    cp_async_commit();
+  }
+  for (int b = 0; b < nb; b++) {
+    if (b + RING_B - 1 < nb) issue(b + RING_B - 1, true);
+    cp_async_commit();
+    cp_async_wait<RING_B - 1>();
+    __syncwarp(pair);
+    const dfloat* src = ring + (b % RING_B) * 16 * LM + mm;
+    dfloat l[4][3], x[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+#pragma unroll
+      for (int j = 0; j < 3; j++) l[r][j] = src[(r * 4 + j) * LM];
+      x[r] = X[(4 * b + r) * ld];
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      fwd_row(x[r], l[r], xm1, xm2, xm3);
+      X[(4 * b + r) * ld] = x[r];
+    }
+    __syncwarp(pair);
+  }
+  for (int i = 4 * nb; i < NR; i++) {
+    const dfloat* fr = f + i * rs;
+    dfloat l[3] = {ldf(fr), ldf(fr + NTNZ), ldf(fr + 2 * NTNZ)};
+    dfloat x = X[i * ld];
+    fwd_row(x, l, xm1, xm2, xm3);
+    X[i * ld] = x;
+  }
+  dfloat xp1{}, xp2{}, xp3{};
+#pragma unroll
+  for (int b = 0; b < RING_B - 1; b++) {
+    if (b < nb) issue(b, false);
+    cp_async_commit();
+  }
+  for (int b = 0; b < nb; b++) {
+    if (b + RING_B - 1 < nb) issue(b + RING_B - 1, false);
+    cp_async_commit();
+    cp_async_wait<RING_B - 1>();
+    __syncwarp(pair);
+    const dfloat* src = ring + (b % RING_B) * 16 * LM + mm;
+    dfloat u[4][4], x[4];
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+#pragma unroll
+      for (int j = 0; j < 4; j++) u[r][j] = src[(r * 4 + j) * LM];
+      x[r] = X[(NR - 1 - 4 * b - r) * ld];
+    }
+#pragma unroll
+    for (int r = 0; r < 4; r++) {
+      bwd_row(x[r], u[r], xp1, xp2, xp3);
+      X[(NR - 1 - 4 * b - r) * ld] = x[r];
+    }
+    __syncwarp(pair);
+  }
+  for (int i = NR - 1 - 4 * nb; i >= 0; i--) {
+    const dfloat* fr = f + i * rs;
+    dfloat u[4] = {ldf(fr + 6 * NTNZ), ldf(fr + 5 * NTNZ), ldf(fr + 4 * NTNZ), ldf(fr + 3 * NTNZ)};
+    dfloat x = X[i * ld];
+    bwd_row(x, u, xp1, xp2, xp3);
+    X[i * ld] = x;
+  }
+  cp_async_wait<0>();  // (only empty groups can be left)
+  __syncwarp(pair);
+}
+
 // The low half of a line slot holds an FP32 pair in the increment passes.
 __device__ __forceinline__ float2& f32slot(double2* a, int e) { return reinterpret_cast<float2*>(a)[2 * e]; }
 // Around their banded solves the increment passes hold a line slot as two double-float
@@ -199,6 +314,10 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   extern __shared__ double2 sm[];
   double2* R = sm;           // [3][NR][LM] right-hand side, then the new velocity
   double2* P = sm + 3 * LN;  // [NR][LM] divergence, then the pressure
+  // DFS: the solves' factor rings (solve_line_ring), the pressure's after the lines, the
+  // Helmholtz solves' from the pressure line on (dead by then)
+  dfloat* ringD = reinterpret_cast<dfloat*>(sm + 4 * LN);
+  dfloat* ringF = reinterpret_cast<dfloat*>(P);
   __shared__ double2 dvs[LM];
   __shared__ float2 dvs32[LM];  // increment passes: the same in FP32
   __shared__ unsigned long long wnum[NTH / 32], wden[NTH / 32];
@@ -529,8 +648,9 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     const int mm = tid >> 1, part = tid & 1;
     if (k0 + mm < NTNZ && fac_ok(3, k0 + mm)) {
       if constexpr (DFS)
-        solve_line(reinterpret_cast<dfloat*>(P + mm) + part, 2 * LM, facdf + 3 * (size_t)NR * NFAC * NTNZ + k0 + mm,
-                   NTNZ, NR);
+        solve_line_ring<LM>(reinterpret_cast<dfloat*>(P + mm) + part, 2 * LM,
+                            facdf + 3 * (size_t)NR * NFAC * NTNZ + k0 + mm, NTNZ, NR, ringD, mm, part,
+                            3u << ((tid & 31) & ~1));
       else
         solve_line(reinterpret_cast<double*>(P + mm) + part, 2 * LM, fac + 3 * (size_t)NR * NFAC * NTNZ + k0 + mm,
                    NTNZ, NR);
@@ -612,8 +732,9 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     const int c = tf / (2 * LM), rem = tf - c * 2 * LM, mm = rem >> 1, part = rem & 1;
     if (k0 + mm < NTNZ && fac_ok(c, k0 + mm)) {
       if constexpr (DFS)
-        solve_line(reinterpret_cast<dfloat*>(R + c * LN + mm) + part, 2 * LM,
-                   facdf + (size_t)c * NR * NFAC * NTNZ + k0 + mm, NTNZ, NR);
+        solve_line_ring<LM>(reinterpret_cast<dfloat*>(R + c * LN + mm) + part, 2 * LM,
+                            facdf + (size_t)c * NR * NFAC * NTNZ + k0 + mm, NTNZ, NR,
+                            ringF + (size_t)c * RING_B * 16 * LM, mm, part, 3u << ((tid & 31) & ~1));
       else
         solve_line(reinterpret_cast<double*>(R + c * LN + mm) + part, 2 * LM,
                    fac + (size_t)c * NR * NFAC * NTNZ + k0 + mm, NTNZ, NR);
@@ -1053,8 +1174,14 @@ void linear_shape(int v, int* LM, int* NTH) {
   *NTH = kLinShapes[v].NTH;
 }
 
+// Dynamic shared memory of a block: 4 radial lines, and the factor rings in the mixed form.
+static size_t linear_smem(int v, int NR, bool mixed) {
+  const int LM = kLinShapes[v].LM;
+  return sizeof(double2) * 4 * (size_t)NR * LM + (mixed ? ring_extra(NR, LM) : 0);
+}
+
 bool linear_variant_fits(int v, int NR) {
-  return v >= 0 && v < LIN_VARIANTS && sizeof(double2) * 4 * (size_t)NR * kLinShapes[v].LM <= 200 * 1024;
+  return v >= 0 && v < LIN_VARIANTS && linear_smem(v, NR, true) <= 200 * 1024;
 }
 
 void configure_linear_kernels() {
@@ -1062,7 +1189,9 @@ void configure_linear_kernels() {
 #define NSP_LIN_CFG(v, lm, nth)                                                                        \
   cudaFuncSetAttribute(linear_k<lm, nth, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, big); \
   cudaFuncSetAttribute(linear_k<lm, nth, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);  \
-  cudaFuncSetAttribute(linear_k<lm, nth, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+  cudaFuncSetAttribute(linear_k<lm, nth, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);      \
+  cudaFuncSetAttribute(linear_k<lm, nth, false, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);  \
+  cudaFuncSetAttribute(linear_k<lm, nth, true, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   NSP_LIN_SHAPES(NSP_LIN_CFG)
 #undef NSP_LIN_CFG
 }
@@ -1077,7 +1206,7 @@ void launch_linear(const Tables& tb, const Bufs& bf, Ctl* dctl, cudaStream_t st,
     const int v = linear_variant_fits(want, tb.NR) ? want : linear_default_variant(tb.NR);
     const LinShape s = kLinShapes[v];
     const dim3 grid((tb.NTNZ + s.LM - 1) / s.LM, tb.nmem);
-    const size_t smem = sizeof(double2) * 4 * (size_t)tb.NR * s.LM;
+    const size_t smem = linear_smem(v, tb.NR, mixed);
     switch (v) {
 #define NSP_LIN_CASE(v, lm, nth)                                                          \
   case v:                                                                                \
