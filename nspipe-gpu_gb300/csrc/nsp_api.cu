@@ -171,6 +171,16 @@ bool same_shape(const nsp_params& a, const nsp_params& b) {
          a.d_im == b.d_im && a.sten == b.sten && a.Qdes == b.Qdes && a.maxit == b.maxit && a.tol == b.tol;
 }
 
+// x = hi + lo with hi = fl32(x), lo = fl32(x - hi): the double-float form of a table.
+static std::vector<float2> split_df_host(const std::vector<double>& v) {
+  std::vector<float2> o(v.size());
+  for (size_t e = 0; e < v.size(); e++) {
+    const float hi = (float)v[e];
+    o[e] = make_float2(hi, (float)(v[e] - (double)hi));
+  }
+  return o;
+}
+
 // Tables of one member's parameter set only (for single-member calls: nsp_nonlinear,
 // nsp_lusolve), as a one-set view of its group's tables.
 Tables member_view(const Group& g, int slot) {
@@ -180,6 +190,7 @@ Tables member_view(const Group& g, int slot) {
   t.V += (size_t)ps * 3 * t.S;
   if (t.V32) t.V32 += (size_t)ps * 3 * t.S;
   if (t.facdf) t.facdf += (size_t)ps * 4 * t.NR * NFAC * t.NTNZ;
+  if (t.Vdf) t.Vdf += (size_t)ps * 2 * 3 * t.S;
   t.Luc += (size_t)ps * 2 * STEN * t.NR;
   t.Luc32 += (size_t)ps * 2 * STEN * t.NR;
   t.uc += (size_t)ps * t.NR;
@@ -756,15 +767,24 @@ int nsp_setup(nsp_ctx* c) {
     }
     tb.nsets = nsets;
     tb.V32 = nullptr;
-    tb.facdf = nullptr;
-    if (c->precision == NSP_MIXED) {  // the increment passes' FP32 correction profiles and double-float factors
-      float2 *v32 = nullptr, *fdf = nullptr;
-      if ((rc = dalloc(c, &v32, sizeof(float2) * V_n)) || (rc = dalloc(c, &fdf, sizeof(float2) * fac_n))) return rc;
+    tb.facdf = tb.Vdf = tb.Ddf = tb.Ddivdf = tb.rinvdf = nullptr;
+    if (c->precision == NSP_MIXED) {
+      // the increment passes' FP32 correction profiles; the double-float factors, correction
+      // profiles and stencils of the linear passes
+      float2 *v32 = nullptr, *fdf = nullptr, *vdf = nullptr;
+      if ((rc = dalloc(c, &v32, sizeof(float2) * V_n)) || (rc = dalloc(c, &fdf, sizeof(float2) * fac_n)) ||
+          (rc = dalloc(c, &vdf, sizeof(float2) * 2 * V_n)))
+        return rc;
       launch_to_f32(tb.V, v32, (long long)V_n, c->st);
       launch_split_df(tb.fac, fdf, (long long)fac_n, c->st);
+      launch_split_df(reinterpret_cast<const double*>(tb.V), vdf, 2 * (long long)V_n, c->st);
       CK(cudaGetLastError());
       tb.V32 = v32;
       tb.facdf = fdf;
+      tb.Vdf = vdf;
+      if ((rc = upload(c, &tb.Ddf, split_df_host(o.D))) || (rc = upload(c, &tb.Ddivdf, split_df_host(Ddiv))) ||
+          (rc = upload(c, &tb.rinvdf, split_df_host(rinv))))
+        return rc;
     }
     std::vector<double2> wt = twiddles(tb.NTP), wz = twiddles(tb.NZR);
     if ((rc = upload(c, &tb.tw_t, wt)) || (rc = upload(c, &tb.tw_z, wz)) || (rc = upload(c, &tb.tw_t32, to_f32(wt))) ||

@@ -43,6 +43,20 @@ __device__ __forceinline__ void df_sub_prod(float& s, float& t, const dfloat& a,
   s = u;
 }
 
+// s + t += a b (df_sub_prod with the product's sign flipped).
+__device__ __forceinline__ void df_add_prod(float& s, float& t, const dfloat& a, const dfloat& b) {
+  df_sub_prod(s, t, dfloat{-a.hi, -a.lo}, b);
+}
+
+// a + b: two-sum of the high parts, the low parts and the error summed, renormalised.
+__device__ __forceinline__ dfloat df_add(const dfloat& a, const dfloat& b) {
+  const float s = __fadd_rn(a.hi, b.hi), v = __fsub_rn(s, a.hi);
+  const float e = __fadd_rn(__fsub_rn(a.hi, __fsub_rn(s, v)), __fsub_rn(b.hi, v));
+  return df_norm(s, __fadd_rn(e, __fadd_rn(a.lo, b.lo)));
+}
+__device__ __forceinline__ dfloat df_neg(const dfloat& a) { return dfloat{-a.hi, -a.lo}; }
+__device__ __forceinline__ dfloat df_sub(const dfloat& a, const dfloat& b) { return df_add(a, df_neg(b)); }
+
 __device__ __forceinline__ dfloat df_mul(const dfloat& a, const dfloat& b) {
   const float p = __fmul_rn(a.hi, b.hi);
   float e = __fmaf_rn(a.hi, b.hi, -p);

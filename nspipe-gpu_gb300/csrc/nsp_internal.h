@@ -53,7 +53,11 @@ struct Tables {
   const double* fac;   // [4][NR][7][NTNZ]: banded LU factors of u+, u-, u_z, p
   const double2* V;    // [3][NR][NTNZ]: influence-matrix correction profiles (+, -, z)
   const float2* V32;   // mixed form: the same in FP32 (the corrector increments' correction)
-  const float2* facdf;  // mixed form: fac as double-float pairs (hi, lo) (the increment passes' solves)
+  const float2* facdf;  // mixed form: fac as double-float pairs (hi, lo) (the linear passes' solves)
+  const float2* Vdf;    // mixed form: V as double-float pairs, real and imaginary part of each entry
+  const float2* Ddf;    // mixed form: D, Ddiv and 1/r as double-float pairs (the predictor's stencils)
+  const float2* Ddivdf;
+  const float2* rinvdf;
   const double2* tw_t; // [NTP] exp(-2 pi i e/NTP), FP64
   const double2* tw_z; // [NZR]
   const float2* tw_t32;

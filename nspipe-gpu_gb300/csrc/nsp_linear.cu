@@ -272,6 +272,15 @@ __device__ __forceinline__ void put_df(double2* a, int e, double2 v) {
   const float2 x = split_df(v.x), y = split_df(v.y);
   dfslot(a, e) = make_float4(x.x, x.y, y.x, y.y);
 }
+__device__ __forceinline__ void put_df(double2* a, int e, dfloat x, dfloat y) {
+  dfslot(a, e) = make_float4(x.hi, x.lo, y.hi, y.lo);
+}
+__device__ __forceinline__ dfloat df_re(const float4& v) { return dfloat{v.x, v.y}; }
+__device__ __forceinline__ dfloat df_im(const float4& v) { return dfloat{v.z, v.w}; }
+__device__ __forceinline__ dfloat ld_df(const float2* p) {
+  const float2 v = __ldg(p);
+  return dfloat{v.x, v.y};
+}
 // A double-float slot's value in FP64 (the widenings on the integer pipe, one FP64 add).
 __device__ __forceinline__ double2 df_value(double2* a, int e) {
   const float4 v = dfslot(a, e);
@@ -326,6 +335,8 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   __shared__ int spar[LM];             // |m| mod 2 (selects the parity tables)
   __shared__ bool sdrop[LM];           // theta Nyquist slot or l = NZ-1: modes the transforms drop
   __shared__ float skt32[LM], skz32[LM];  // k_theta, k_z in FP32 (increment passes)
+  __shared__ dfloat skt_df[LM], skz_df[LM];  // the same in double-float (mixed predictor)
+  __shared__ float4 dvs_df[LM];              // the wall divergence in double-float (mixed predictor)
   __shared__ float snkz2_32[LM], snkt2_32[LM], shdk32[LM];  // FP32 copies (mixed predictor)
   __shared__ int bad;
   // (selects instead of indexing the parameter arrays by a run-time value, which
@@ -360,6 +371,11 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     shdk[tid] = -(0.5 * c_ex) * (2.0 * kt);
     skt32[tid] = f64_to_f32(kt);
     skz32[tid] = f64_to_f32(kz);
+    if (DFS) {
+      const float2 a = split_df(kt), b = split_df(kz);
+      skt_df[tid] = dfloat{a.x, a.y};
+      skz_df[tid] = dfloat{b.x, b.y};
+    }
     snkz2_32[tid] = f64_to_f32(snkz2[tid]);
     snkt2_32[tid] = f64_to_f32(snkt2[tid]);
     shdk32[tid] = f64_to_f32(shdk[tid]);
@@ -389,6 +405,11 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     const float2* U32n = par ? bf.U32[1] : bf.U32[0];
     const float2* Un32 = U32n ? U32n + (size_t)mloc * 3 * S : nullptr;  // mixed form: FP32 mirror of u^n
     const float* Luc32 = tb.Luc32 + (size_t)ps * 2 * STEN * NR;
+    dfloat hidt_df{0.f, 0.f};
+    if constexpr (DFS) {
+      const float2 a = split_df(hidt);
+      hidt_df = dfloat{a.x, a.y};
+    }
     for (int p = tid; p < LN; p += nth) {
       int i = p / LM, mm = p - i * LM, k = k0 + mm;
       if (k >= NTNZ) {
@@ -455,7 +476,15 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
           const float gx = fmaf(0.5f, nf[c].x, f.x), gy = fmaf(0.5f, nf[c].y, f.y);
           // widening on the integer pipe (the hardware conversion issues on the FP64 pipe)
           const double2 u = Un[c * S + h];
-          R[c * LN + p] = c2(fma(hidt, u.x, f32_to_f64(gx)), fma(hidt, u.y, f32_to_f64(gy)));
+          if constexpr (DFS) {  // u^n/(2dt) + g in double-float: u^n split, the product and the sum exact
+            const float2 ux = split_df(u.x), uy = split_df(u.y);
+            float sx = 0.f, tx = 0.f, sy = 0.f, ty = 0.f;
+            df_add_prod(sx, tx, hidt_df, dfloat{ux.x, ux.y});
+            df_add_prod(sy, ty, hidt_df, dfloat{uy.x, uy.y});
+            put_df(R, c * LN + p, df_add(df_norm(sx, tx), df_make(gx)), df_add(df_norm(sy, ty), df_make(gy)));
+          } else {
+            R[c * LN + p] = c2(fma(hidt, u.x, f32_to_f64(gx)), fma(hidt, u.y, f32_to_f64(gy)));
+          }
         }
         continue;
       }
@@ -487,9 +516,13 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
         nt.x = f32_to_f64(f64_to_f32(nt.x) + mean_terms32(mf, 1, true, 0.f, 0.f, vr, zero, zero).x);
         nz.x += (double)mean_terms32(mf, 2, true, 0.f, 0.f, vr, zero, zero).x;  // (nz: FP64 wall forcing)
       }
-      R[p] = c2(0.5 * nr.x + er.x, 0.5 * nr.y + er.y);
-      R[LN + p] = c2(0.5 * nt.x + et.x, 0.5 * nt.y + et.y);
-      R[2 * LN + p] = c2(0.5 * nz.x + ez.x, 0.5 * nz.y + ez.y);
+      const double2 r0 = c2(0.5 * nr.x + er.x, 0.5 * nr.y + er.y), r1 = c2(0.5 * nt.x + et.x, 0.5 * nt.y + et.y),
+                    r2 = c2(0.5 * nz.x + ez.x, 0.5 * nz.y + ez.y);
+      if constexpr (DFS) {  // (mode (0,0) of the mixed predictor)
+        put_df(R, p, r0); put_df(R, LN + p, r1); put_df(R, 2 * LN + p, r2);
+      } else {
+        R[p] = r0; R[LN + p] = r1; R[2 * LN + p] = r2;
+      }
       if (Un32) {  // mixed form: N(u^n) for the first increment pass
         Rw[h] = nr; Rw[S + h] = nt; Rw[2 * S + h] = nz;
       } else {
@@ -610,6 +643,24 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       }
       put_df(P, p, sx, sy);
       continue;
+    } else if constexpr (DFS) {  // mixed predictor: the same stencil in double-float
+      float sx = 0.f, tx = 0.f, sy = 0.f, ty = 0.f;
+      if (k < NTNZ && i < NR - 1) {
+        const int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
+        const float2* Dr = tb.Ddivdf + (1 - spar[mm]) * STEN * NR + STEN * i + i0;
+        for (int j = 0; j < len; j++) {
+          const dfloat de = ld_df(Dr + j);
+          const float4 a = dfslot(R, (left + j) * LM + mm);
+          df_add_prod(sx, tx, de, df_re(a));
+          df_add_prod(sy, ty, de, df_im(a));
+        }
+        const dfloat kti = df_mul(skt_df[mm], ld_df(tb.rinvdf + i)), kz = skz_df[mm];
+        const float4 rt = dfslot(R, LN + p), rz = dfslot(R, 2 * LN + p);
+        df_sub_prod(sx, tx, kti, df_im(rt)); df_add_prod(sy, ty, kti, df_re(rt));
+        df_sub_prod(sx, tx, kz, df_im(rz)); df_add_prod(sy, ty, kz, df_re(rz));
+      }
+      put_df(P, p, df_norm(sx, tx), df_norm(sy, ty));
+      continue;
     } else if (k < NTNZ && i < NR - 1) {
       double kt = skt[mm], kz = skz[mm];
       int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
@@ -629,8 +680,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       sx -= kz * rz.y; sy += kz * rz.x;
       d = c2(sx, sy);
     }
-    if constexpr (DFS) put_df(P, p, d);
-    else P[p] = d;
+    P[p] = d;
   }
   __syncthreads();
 
@@ -663,9 +713,6 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       f32slot(P, p) = make_float2(a.x, a.z);
     }
     __syncthreads();
-  } else if constexpr (DFS) {  // the pressure back to FP64, in place
-    for (int p = tid; p < LN; p += nth) P[p] = df_value(P, p);
-    __syncthreads();
   }
 
   // E. rhs -= grad p, r/theta -> +/-, wall rows = 0.
@@ -694,6 +741,37 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
         put_df(R, 2 * LN + p, fz.x, fz.y);
         continue;
       }
+    } else if constexpr (DFS) {  // mixed predictor: the same in double-float
+      const dfloat z{0.f, 0.f};
+      dfloat upx = z, upy = z, umx = z, umy = z, rzx = z, rzy = z;
+      if (i < NR - 1) {
+        const int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
+        const float2* Dr = tb.Ddf + spar[mm] * STEN * NR + STEN * i + i0;
+        const float4 r0 = dfslot(R, p);
+        float sx = r0.x, tx = r0.y, sy = r0.z, ty = r0.w;  // rr - d_r p
+        for (int j = 0; j < len; j++) {
+          const dfloat de = ld_df(Dr + j);
+          const float4 a = dfslot(P, (left + j) * LM + mm);
+          df_sub_prod(sx, tx, de, df_re(a));
+          df_sub_prod(sy, ty, de, df_im(a));
+        }
+        const dfloat rrx = df_norm(sx, tx), rry = df_norm(sy, ty);
+        const dfloat kti = df_mul(skt_df[mm], ld_df(tb.rinvdf + i)), kz = skz_df[mm];
+        const float4 pp = dfslot(P, p), rt = dfslot(R, LN + p), rz = dfslot(R, 2 * LN + p);
+        float a0 = rt.x, b0 = rt.y, a1 = rt.z, b1 = rt.w;  // rt.x += kti pp.y, rt.y -= kti pp.x
+        df_add_prod(a0, b0, kti, df_im(pp));
+        df_sub_prod(a1, b1, kti, df_re(pp));
+        const dfloat rtx = df_norm(a0, b0), rty = df_norm(a1, b1);
+        a0 = rz.x; b0 = rz.y; a1 = rz.z; b1 = rz.w;  // rz.x += kz pp.y, rz.y -= kz pp.x
+        df_add_prod(a0, b0, kz, df_im(pp));
+        df_sub_prod(a1, b1, kz, df_re(pp));
+        rzx = df_norm(a0, b0);
+        rzy = df_norm(a1, b1);
+        upx = df_sub(rrx, rty); upy = df_add(rry, rtx);
+        umx = df_add(rrx, rty); umy = df_sub(rry, rtx);
+      }
+      put_df(R, p, upx, upy); put_df(R, LN + p, umx, umy); put_df(R, 2 * LN + p, rzx, rzy);
+      continue;
     } else if (i < NR - 1) {
       double kt = skt[mm], kz = skz[mm];
       int left = max(0, i - IW), right = min(i + IW, NR - 1), len = right + 1 - left, i0 = i + IW - right;
@@ -714,11 +792,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       up = c2(rr.x - rt.y, rr.y + rt.x);
       um = c2(rr.x + rt.y, rr.y - rt.x);
     }
-    if constexpr (DFS) {
-      put_df(R, p, up); put_df(R, LN + p, um); put_df(R, 2 * LN + p, rz);
-    } else {
-      R[p] = up; R[LN + p] = um; R[2 * LN + p] = rz;
-    }
+    R[p] = up; R[LN + p] = um; R[2 * LN + p] = rz;
   }
   __syncthreads();
 
@@ -770,6 +844,10 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     }
     dvs[mm] = dv;
     dvs32[mm] = make_float2(f64_to_f32(dv.x), f64_to_f32(dv.y));
+    if (DFS && !INC) {
+      const float2 x = split_df(dv.x), y = split_df(dv.y);
+      dvs_df[mm] = make_float4(x.x, x.y, y.x, y.y);
+    }
   }
   __syncthreads();
 
@@ -796,15 +874,43 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       if (k == 0) { ur = make_float2(0.f, 0.f); ut.y = 0.f; uz.y = 0.f; }
       f32slot(R, p) = ur; f32slot(R, LN + p) = ut; f32slot(R, 2 * LN + p) = uz;
     }
+  } else if constexpr (DFS) {  // mixed predictor: the same in double-float, with V split likewise
+    const float4* Vd = reinterpret_cast<const float4*>(tb.Vdf) + (size_t)ps * 3 * S;
+    for (int p = tid; p < LN; p += nth) {
+      const int i = p / LM, mm = p - i * LM, k = k0 + mm;
+      if (k >= NTNZ) continue;
+      const size_t hv = (size_t)i * NTNZ + k;
+      if (!NSP_IN_BOUNDS(tb, hv, S, BC_LIN_POINT)) continue;
+      const float4 dv = dvs_df[mm];
+      const dfloat dvx = df_re(dv), dvy = df_im(dv);
+      // u + dv v, complex: x = u.x + dv.x v.x - dv.y v.y, y = u.y + dv.x v.y + dv.y v.x
+      auto corr = [&](const float4& u, const float4& v, dfloat& ox, dfloat& oy) {
+        float s0 = u.x, t0 = u.y;
+        df_add_prod(s0, t0, dvx, df_re(v));
+        df_sub_prod(s0, t0, dvy, df_im(v));
+        ox = df_norm(s0, t0);
+        s0 = u.z; t0 = u.w;
+        df_add_prod(s0, t0, dvx, df_im(v));
+        df_add_prod(s0, t0, dvy, df_re(v));
+        oy = df_norm(s0, t0);
+      };
+      dfloat upx, upy, umx, umy, uzx, uzy;
+      corr(dfslot(R, p), __ldg(Vd + hv), upx, upy);
+      corr(dfslot(R, LN + p), __ldg(Vd + S + hv), umx, umy);
+      corr(dfslot(R, 2 * LN + p), __ldg(Vd + 2 * S + hv), uzx, uzy);
+      const dfloat zero{0.f, 0.f};
+      dfloat urx = df_add(upx, umx), ury = df_add(upy, umy);
+      const dfloat utx = df_sub(upy, umy);
+      dfloat uty = df_neg(df_sub(upx, umx));
+      uzx = dfloat{2.f * uzx.hi, 2.f * uzx.lo};
+      uzy = dfloat{2.f * uzy.hi, 2.f * uzy.lo};
+      if (k == 0) { urx = ury = zero; uty = zero; uzy = zero; }
+      put_df(R, p, urx, ury); put_df(R, LN + p, utx, uty); put_df(R, 2 * LN + p, uzx, uzy);
+    }
   } else for (int p = tid; p < LN; p += nth) {
     int i = p / LM, mm = p - i * LM, k = k0 + mm;
     if (k >= NTNZ) continue;
-    double2 up, um, uz;
-    if constexpr (DFS) {
-      up = df_value(R, p); um = df_value(R, LN + p); uz = df_value(R, 2 * LN + p);
-    } else {
-      up = R[p]; um = R[LN + p]; uz = R[2 * LN + p];
-    }
+    double2 up = R[p], um = R[LN + p], uz = R[2 * LN + p];
     double2 dv = dvs[mm];
     size_t hv = (size_t)i * NTNZ + k;
     if (!NSP_IN_BOUNDS(tb, hv, S, BC_LIN_POINT)) continue;
@@ -828,6 +934,15 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       for (int i = 0; i < NR; i++) Q += tb.rdr[i] * f32_to_f64(f32slot(R, 2 * LN + i * LM).x);
       const double corr = -Q / Qc;
       for (int i = 0; i < NR; i++) f32slot(R, 2 * LN + i * LM).x += f64_to_f32(corr * ucp[i]);
+    } else if constexpr (DFS) {  // the mixed predictor's double-float line, summed and corrected in FP64
+      for (int i = 0; i < NR; i++) Q += tb.rdr[i] * df_value(R, 2 * LN + i * LM).x;
+      const double corr = (tb.Qdes - Q) / Qc;
+      for (int i = 0; i < NR; i++) {
+        float4& v = dfslot(R, 2 * LN + i * LM);
+        const float2 x = split_df(f32_to_f64(v.x) + f32_to_f64(v.y) + corr * ucp[i]);
+        v.x = x.x;
+        v.y = x.y;
+      }
     } else {
       for (int i = 0; i < NR; i++) Q += tb.rdr[i] * R[2 * LN + i * LM].x;
       double corr = (tb.Qdes - Q) / Qc;
@@ -874,7 +989,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
           lden32 = max(lden32, __float_as_uint(fmaf(ox, ox, oy * oy)));
           v = c2(fma(hdi, f32_to_f64(f.x), o[u][c].x), fma(hdi, f32_to_f64(f.y), o[u][c].y));
         } else {
-          v = R[c * LN + p];
+          v = DFS ? df_value(R, c * LN + p) : R[c * LN + p];
           if (!pred) {
             const double ex = o[u][c].x - v.x, ey = o[u][c].y - v.y;
             lnum = max(lnum, (unsigned long long)__double_as_longlong(ex * ex + ey * ey));
