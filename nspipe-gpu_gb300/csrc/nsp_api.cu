@@ -213,8 +213,12 @@ void range_view(const Group& g, bool mixed, int a, int b, Tables* t, Bufs* bf) {
     if (bf->U32[k]) bf->U32[k] += s3;
     if (bf->DR32[k]) bf->DR32[k] += s3;
   }
-  bf->RHSW += s3;
-  bf->N += s3;
+  if (bf->RHSW) bf->RHSW += s3;
+  if (bf->N) bf->N += s3;
+  if (bf->N32) bf->N32 += s3;
+  if (bf->RHSW32) bf->RHSW32 += s3;
+  if (bf->NF) bf->NF += a;
+  if (bf->RW00) bf->RW00 += (size_t)a * g.tb.NR;
   const size_t esz = mixed ? sizeof(float2) : sizeof(double2);
   const size_t plane = (size_t)g.tb.NR * g.tb.NTP * g.tb.NZ * esz;
   bf->G = static_cast<char*>(g.bf.G) + (size_t)a * 9 * plane;
@@ -626,16 +630,30 @@ int nsp_create(const nsp_params* members, int n_members, int precision, int devi
     int rc;
     if ((rc = dalloc(c, &g.bf.U[0], S3 * sizeof(double2)))) return rc;
     if ((rc = dalloc(c, &g.bf.U[1], S3 * sizeof(double2)))) return rc;
-    if ((rc = dalloc(c, &g.bf.RHSW, S3 * sizeof(double2)))) return rc;
-    if ((rc = dalloc(c, &g.bf.N, S3 * sizeof(double2)))) return rc;
+    g.bf.N = g.bf.RHSW = nullptr;
+    g.bf.N32 = g.bf.RHSW32 = nullptr;
+    g.bf.NF = g.bf.RW00 = nullptr;
+    if (precision == NSP_MIXED) {
+      if ((rc = dalloc(c, &g.bf.N32, S3 * sizeof(float2))) || (rc = dalloc(c, &g.bf.RHSW32, S3 * sizeof(float2))) ||
+          (rc = dalloc(c, &g.bf.NF, sizeof(double) * tb.nmem)) ||
+          (rc = dalloc(c, &g.bf.RW00, sizeof(double) * tb.nmem * (size_t)tb.NR)))
+        return rc;
+      CK(cudaMemset(g.bf.N32, 0, S3 * sizeof(float2)));
+      CK(cudaMemset(g.bf.RHSW32, 0, S3 * sizeof(float2)));
+      CK(cudaMemset(g.bf.NF, 0, sizeof(double) * tb.nmem));
+      CK(cudaMemset(g.bf.RW00, 0, sizeof(double) * tb.nmem * (size_t)tb.NR));
+    } else {
+      if ((rc = dalloc(c, &g.bf.RHSW, S3 * sizeof(double2))) || (rc = dalloc(c, &g.bf.N, S3 * sizeof(double2))))
+        return rc;
+      CK(cudaMemset(g.bf.N, 0, S3 * sizeof(double2)));
+      CK(cudaMemset(g.bf.RHSW, 0, S3 * sizeof(double2)));
+    }
     if ((rc = dalloc(c, &g.bf.G, gsz))) return rc;
     if ((rc = dalloc(c, &g.bf.H, hsz))) return rc;
     CK(cudaMemset(g.bf.U[0], 0, S3 * sizeof(double2)));
     CK(cudaMemset(g.bf.U[1], 0, S3 * sizeof(double2)));
     CK(cudaMemset(g.bf.G, 0, gsz));
     CK(cudaMemset(g.bf.H, 0, hsz));
-    CK(cudaMemset(g.bf.N, 0, S3 * sizeof(double2)));
-    CK(cudaMemset(g.bf.RHSW, 0, S3 * sizeof(double2)));
     g.bf.U32[0] = g.bf.U32[1] = nullptr;
     g.bf.DR32[0] = g.bf.DR32[1] = nullptr;
     g.bf.MEAN = nullptr;

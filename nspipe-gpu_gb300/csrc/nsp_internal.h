@@ -95,6 +95,13 @@ struct Bufs {
                        // with U32 so that the theta-inverse reads it instead of re-gathering levels
   double2* RHSW;       // [nmem][3][S]: [(1-d_im) N(u^n) + u^n/dt + (1-d_im)/Re L u^n] / 2, r/theta form
   double2* N;          // [nmem][3][S]: nonlinear term output
+  // Mixed form (N and RHSW are null there): N and the increment passes' N_{i-1} hold FP32
+  // numbers -- the transforms' values plus FP32 mean-flow terms -- except on the line
+  // Re N_z(0,0), which carries the FP64 wall forcing.
+  float2* N32;         // [nmem][3][S]: N in FP32, without the forcing
+  double* NF;          // [nmem]: the forcing -(2/Re) d_r u_z(0,0)|wall, added to Re N_z(0,0) at every level
+  float2* RHSW32;      // [nmem][3][S]: N_{i-1} in FP32 (its Re N_z(0,0) line unused)
+  double* RW00;        // [nmem][NR]: Re N_z(0,0) of N_{i-1} in FP64, forcing included
   void* G;             // [nmem][9][NR][NTP][NZ] complex T: theta-inverse of u, dr u, i m u / r
   void* H;             // [nmem][3][NR][NTP][NZ] complex T: z-forward of the nonlinear product
   float* MEAN;         // mixed form only: [nmem][NR][MEAN_N] mean flow of the transform input

@@ -157,9 +157,12 @@ constexpr size_t ring_bytes(int LM) { return (size_t)RING_B * 16 * LM * sizeof(d
 // Dynamic shared memory of a linear-pass block beyond its 4 radial lines (mixed form): the
 // pressure solve's ring, and with the pressure line, which is dead by then, the three
 // Helmholtz solves' rings.
+// The same space holds, in the predictor's first stage, the block's tile of the FP32
+// mirror of u^n (3 lines of float2) that its explicit stencil reads.
 inline size_t ring_extra(int NR, int LM) {
   const size_t pl = sizeof(double2) * (size_t)NR * LM, r = ring_bytes(LM);
-  return 3 * r > pl + r ? 3 * r - pl : r;
+  const size_t rings = 3 * r > pl + r ? 3 * r - pl : r, tile = 3 * sizeof(float2) * (size_t)NR * LM;
+  return tile > pl + rings ? tile - pl : rings;
 }
 
 // solve_line<dfloat, dfloat> with the factor rows staged through a shared-memory ring:
@@ -347,8 +350,11 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   float2* Ui32 = U32i ? U32i + (size_t)mloc * 3 * S : nullptr;  // mixed form
   float2* DR32i = par ? bf.DR32[0] : bf.DR32[1];
   float2* Udr32 = DR32i ? DR32i + (size_t)mloc * 3 * S : nullptr;  // mixed form: d_r of the FP32 mirror
-  const double2* Nn = bf.N + (size_t)mloc * 3 * S;
-  double2* Rw = bf.RHSW + (size_t)mloc * 3 * S;
+  const double2* Nn = bf.N ? bf.N + (size_t)mloc * 3 * S : nullptr;  // FP64 form
+  double2* Rw = bf.RHSW ? bf.RHSW + (size_t)mloc * 3 * S : nullptr;
+  // mixed form: N and N_{i-1} in FP32, the FP64 line Re N_z(0,0) apart (bf.NF, bf.RW00)
+  const float2* N32n = bf.N32 ? bf.N32 + (size_t)mloc * 3 * S : nullptr;
+  float2* Rw32 = bf.RHSW32 ? bf.RHSW32 + (size_t)mloc * 3 * S : nullptr;
   // The member's operator parameter set (its Re): LU factors, correction profiles,
   // explicit Laplacian, flux profile and scalars.
   const int ps = member_set(tb, mloc);
@@ -406,9 +412,17 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     const float2* Un32 = U32n ? U32n + (size_t)mloc * 3 * S : nullptr;  // mixed form: FP32 mirror of u^n
     const float* Luc32 = tb.Luc32 + (size_t)ps * 2 * STEN * NR;
     dfloat hidt_df{0.f, 0.f};
+    // mixed: the block's tile of the FP32 mirror of u^n, [3][NR][LM], in the pressure line
+    // and ring space (free until stage C), loaded coalesced; the stencil reads it there.
+    float2* T32 = reinterpret_cast<float2*>(P);
     if constexpr (DFS) {
       const float2 a = split_df(hidt);
       hidt_df = dfloat{a.x, a.y};
+      for (int e = tid; e < 3 * LN; e += nth) {
+        const int c = e / LN, q = e - c * LN, ii = q / LM, k = k0 + q - ii * LM;
+        T32[e] = k < NTNZ ? __ldg(Un32 + (size_t)c * S + (size_t)ii * NTNZ + k) : make_float2(0.f, 0.f);
+      }
+      __syncthreads();
     }
     for (int p = tid; p < LN; p += nth) {
       int i = p / LM, mm = p - i * LM, k = k0 + mm;
@@ -425,7 +439,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
           !NSP_IN_BOUNDS(tb, le + len - 1, 2 * STEN * NR, BC_LIN_TAP) ||
           !NSP_IN_BOUNDS(tb, (size_t)(left + len - 1) * NTNZ + k, S, BC_LIN_TAP))
         continue;
-      if (Un32 && k != 0) {
+      if (DFS && k != 0) {  // (DFS: the mixed predictor)
         // mixed form: everything but u^n/dt in FP32 on the FP32 mirror of u^n -- the
         // stencil sums and the diagonal terms ((1-d_im)/Re times the Laplacian) and N/2
         // (exact in FP32: the FP32 transforms' values) -- then one FP64 multiply-add
@@ -434,8 +448,8 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
         float2 fr = make_float2(0.f, 0.f), ft = fr, fz = fr;
         for (int j = 0; j < len; j++) {
           const float a = __ldg(Luc32 + lo + j), b = __ldg(Luc32 + le + j);
-          const size_t hj = (size_t)(left + j) * NTNZ + k;
-          const float2 vr = __ldg(Un32 + hj), vt = __ldg(Un32 + S + hj), vz = __ldg(Un32 + 2 * S + hj);
+          const int e = (left + j) * LM + mm;
+          const float2 vr = T32[e], vt = T32[LN + e], vz = T32[2 * LN + e];
           fr.x = fmaf(a, vr.x, fr.x); fr.y = fmaf(a, vr.y, fr.y);
           ft.x = fmaf(a, vt.x, ft.x); ft.y = fmaf(a, vt.y, ft.y);
           fz.x = fmaf(b, vz.x, fz.x); fz.y = fmaf(b, vz.y, fz.y);
@@ -447,12 +461,9 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
         // (nsp_state.cuh), from the same FP32 values of u^n the explicit stencil uses
         float2 nf[3];
 #pragma unroll
-        for (int c = 0; c < 3; c++) {
-          const double2 n = Nn[c * S + h];
-          nf[c] = make_float2(f64_to_f32(n.x), f64_to_f32(n.y));
-        }
+        for (int c = 0; c < 3; c++) nf[c] = N32n[c * S + h];
         {
-          const float2 fur = __ldg(Un32 + h), fut = __ldg(Un32 + S + h), fuz = __ldg(Un32 + 2 * S + h);
+          const float2 fur = T32[p], fut = T32[LN + p], fuz = T32[2 * LN + p];
           fr.x += fmaf(hsf, fur.x, -hdf * fut.y);
           fr.y += fmaf(hsf, fur.y, hdf * fut.x);
           ft.x += fmaf(hsf, fut.x, hdf * fur.y);
@@ -471,7 +482,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
         }
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-          Rw[c * S + h] = c2(f32_to_f64(nf[c].x), f32_to_f64(nf[c].y));  // full N(u^n) for the first increment pass
+          Rw32[c * S + h] = nf[c];  // full N(u^n) for the first increment pass
           const float2 f = c == 0 ? fr : (c == 1 ? ft : fz);
           const float gx = fmaf(0.5f, nf[c].x, f.x), gy = fmaf(0.5f, nf[c].y, f.y);
           // widening on the integer pipe (the hardware conversion issues on the FP64 pipe)
@@ -507,7 +518,15 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       double2 er = c2(lr.x + hs * ur.x - hd * ut.y, lr.y + hs * ur.y + hd * ut.x);
       double2 et = c2(lt.x + hs * ut.x + hd * ur.y, lt.y + hs * ut.y - hd * ur.x);
       double2 ez = c2(lz.x + hz * uz.x, lz.y + hz * uz.y);
-      double2 nr = Nn[h], nt = Nn[S + h], nz = Nn[2 * S + h];
+      double2 nr, nt, nz;
+      if constexpr (DFS) {  // mixed form (mode (0,0)): N in FP32 plus the FP64 wall forcing on Re N_z
+        const float2 a = N32n[h], b = N32n[S + h], z = N32n[2 * S + h];
+        nr = c2(f32_to_f64(a.x), f32_to_f64(a.y));
+        nt = c2(f32_to_f64(b.x), f32_to_f64(b.y));
+        nz = c2(f32_to_f64(z.x) + bf.NF[mloc], f32_to_f64(z.y));
+      } else {
+        nr = Nn[h]; nt = Nn[S + h]; nz = Nn[2 * S + h];
+      }
       if (Un32) {  // mixed form, mode (0,0): the mean flow's own terms (nsp_state.cuh)
         const float* mean = bf.MEAN + (size_t)mloc * NR * MEAN_N;
         const Mean32 mf = mean_flow32_rec(tb, mean, i);
@@ -523,8 +542,11 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       } else {
         R[p] = r0; R[LN + p] = r1; R[2 * LN + p] = r2;
       }
-      if (Un32) {  // mixed form: N(u^n) for the first increment pass
-        Rw[h] = nr; Rw[S + h] = nt; Rw[2 * S + h] = nz;
+      if constexpr (DFS) {  // mixed form: N(u^n) for the first increment pass (all FP32 numbers but Re N_z)
+        Rw32[h] = make_float2(f64_to_f32(nr.x), f64_to_f32(nr.y));
+        Rw32[S + h] = make_float2(f64_to_f32(nt.x), f64_to_f32(nt.y));
+        Rw32[2 * S + h] = make_float2(0.f, f64_to_f32(nz.y));
+        bf.RW00[(size_t)mloc * NR + i] = nz.x;
       } else {
         Rw[h] = c2(hw * nr.x + er.x, hw * nr.y + er.y);
         Rw[S + h] = c2(hw * nt.x + et.x, hw * nt.y + et.y);
@@ -532,15 +554,12 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
       }
     }
   } else if constexpr (INC) {
-    // B'. N_i - N_{i-1} in FP32 (the FP32 transforms' values are exact in FP32; the
-    // u_z line of mode (0,0) carries the FP64 wall forcing, so its difference is taken
-    // in FP64), into the FP32 halves of the line slots; RHSW takes N_i.  N_i is the
-    // transforms' output plus the mean-flow terms (nsp_state.cuh), from u_i's FP32 mirror
-    // -- the transforms' input, at this block's own points -- and the mean flow the
-    // theta-inverse recorded.
-    // N_i and N_{i-1} are held in FP32 (exact: the transforms' values and the FP32 sums
-    // stored by the previous pass), except on the u_z line of mode (0,0), which carries
-    // the FP64 wall forcing and is read again in FP64 (one block's NR points).
+    // B'. N_i - N_{i-1} in FP32, into the FP32 halves of the line slots; RHSW32 takes N_i.
+    // N_i is the transforms' output plus the mean-flow terms (nsp_state.cuh), from u_i's
+    // FP32 mirror -- the transforms' input, at this block's own points -- and the mean
+    // flow the theta-inverse recorded.  Both are stored as FP32 numbers (the transforms'
+    // values and the FP32 sums of the previous pass), except Re N_z(0,0), which carries
+    // the FP64 wall forcing: its difference is taken in FP64 from N32 + NF and RW00.
     constexpr int UB = 2;  // points per thread whose loads are issued together (RHSW is also stored)
     const float* mean = bf.MEAN + (size_t)mloc * NR * MEAN_N;
     for (int pb = tid; pb < LN; pb += UB * nth) {
@@ -552,9 +571,8 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
         const size_t h = ok ? (size_t)i * NTNZ + k : 0;
 #pragma unroll
         for (int c = 0; c < 3; c++) {
-          const double2 a = ok ? Nn[c * S + h] : c2(0, 0), b = ok ? Rw[c * S + h] : c2(0, 0);
-          n[u][c] = make_float2(f64_to_f32(a.x), f64_to_f32(a.y));
-          q[u][c] = make_float2(f64_to_f32(b.x), f64_to_f32(b.y));
+          n[u][c] = ok ? N32n[c * S + h] : make_float2(0.f, 0.f);
+          q[u][c] = ok ? Rw32[c * S + h] : make_float2(0.f, 0.f);
           w[u][c] = ok ? Ui32[c * S + h] : make_float2(0.f, 0.f);
         }
       }
@@ -577,14 +595,15 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
 #pragma unroll
         for (int c = 0; c < 3; c++) {
           float2 d;
-          if (c == 2 && k == 0) {
-            const double2 a = Nn[2 * S + h], b = Rw[2 * S + h];
-            const double2 nf = c2(a.x + (double)ml[c].x, a.y);
-            Rw[2 * S + h] = nf;
-            d = make_float2(f64_to_f32(nf.x - b.x), f64_to_f32(nf.y - b.y));
+          if (c == 2 && k == 0) {  // Re N_z(0,0) in FP64: the FP32 value plus the wall forcing
+            const double nx = f32_to_f64(n[u][c].x) + bf.NF[mloc] + (double)ml[c].x;
+            double* rw = bf.RW00 + (size_t)mloc * NR + i;
+            d = make_float2(f64_to_f32(nx - *rw), n[u][c].y - q[u][c].y);
+            *rw = nx;
+            Rw32[2 * S + h] = make_float2(0.f, n[u][c].y);
           } else {
             const float nx = n[u][c].x + ml[c].x, ny = n[u][c].y + ml[c].y;
-            if (ok) Rw[c * S + h] = c2(f32_to_f64(nx), f32_to_f64(ny));
+            if (ok) Rw32[c * S + h] = make_float2(nx, ny);
             d = make_float2(nx - q[u][c].x, ny - q[u][c].y);
           }
           f32slot(R, c * LN + p) = d;  // zero where k >= NTNZ

@@ -308,9 +308,22 @@ template <int NT, int NTP> struct FwdJob {
       const double* Dw = tb.D + STEN * (NR - 1) + IW;
       for (int j = 0; j <= IW; j++) dwall += Dw[j] * U[2 * S + (size_t)(NR - 1 - IW + j) * NTNZ].x;
     }
-    double2* Nout = (dst ? dst : bf.N + (size_t)mloc * 3 * S) + c * S + (size_t)i * NTNZ + l;
     if (!NSP_IN_BOUNDS(tb, c * S + (size_t)i * NTNZ + l + (size_t)((c0 + nc) / 2 - 1) * NZ, 3 * S, BC_THETA_OUT))
       return;
+    if (!dst) {
+      // a member's N: FP32 (its values are FP32 numbers), the wall forcing of Re N_z(0,0)
+      // kept apart in FP64 -- the same at every level, written by level 0
+      float2* N32 = bf.N32 + (size_t)mloc * 3 * S + c * S + (size_t)i * NTNZ + l;
+      if (c == 2 && l == 0 && c0 == 0 && i == 0) bf.NF[mloc] = -(tb.sscal[4 * member_set(tb, mloc) + 1] * dwall);
+#pragma unroll
+      for (int j = 0; j < CM / 2; j++) {
+        if (2 * j >= nc) break;
+        const int it = c0 / 2 + j;
+        N32[(size_t)it * NZ] = (it == NT / 2 || l == NZ - 1) ? make_float2(0.f, 0.f) : make_float2(v[2 * j], v[2 * j + 1]);
+      }
+      return;
+    }
+    double2* Nout = dst + c * S + (size_t)i * NTNZ + l;
     // An explicit field's mean-flow terms (nsp_state.cuh), from its FP32 copy; a member
     // state's are added by the linear pass.
     const float2* U32 = src ? src32 : nullptr;

@@ -472,7 +472,7 @@ __global__ void __launch_bounds__(TTH) nl_theta_fwd(Tables tb, Bufs bf, const Ct
   }
   __syncthreads();
   const cpx<T>* H = reinterpret_cast<const cpx<T>*>(bf.H) + (size_t)mloc * 3 * NR * NTP * NZ;
-  double2* Nout = dst_override ? dst_override : bf.N + (size_t)mloc * 3 * S;
+  double2* Nout = dst_override ? dst_override : (bf.N ? bf.N + (size_t)mloc * 3 * S : nullptr);  // (null: mixed, N32)
   for (int idx = threadIdx.x; idx < NTP * LC; idx += TTH) {
     int p = idx / LC, lc = idx % LC;
     int c = colc[lc], l = coll[lc];
@@ -507,6 +507,15 @@ __global__ void __launch_bounds__(TTH) nl_theta_fwd(Tables tb, Bufs bf, const Ct
     double2 v;
     if constexpr (sizeof(T) == 8) {
       v = make_double2((double)b.x * tb.inv_norm, (double)b.y * tb.inv_norm);
+    } else if (!dst_override) {
+      // a member's N in the mixed form: FP32 (its values are FP32 numbers), the wall forcing
+      // of Re N_z(0,0) kept apart in FP64 -- the same at every level, written by level 0
+      const bool drop = it == NT / 2 || l == NZ - 1;
+      const size_t e = c * S + (size_t)i * NTNZ + (size_t)it * NZ + l;
+      if (c == 2 && it == 0 && l == 0 && i == 0) bf.NF[mloc] = -(tb.sscal[4 * member_set(tb, mloc) + 1] * dwall);
+      if (NSP_IN_BOUNDS(tb, e, 3 * S, BC_THETA_OUT))
+        bf.N32[(size_t)mloc * 3 * S + e] = drop ? make_float2(0.f, 0.f) : make_float2(b.x * scale, b.y * scale);
+      continue;
     } else {
       float2 w = make_float2(b.x * scale, b.y * scale);
       if (U32 && it != NT / 2 && l != NZ - 1) {
