@@ -371,11 +371,12 @@ def main():
     alg_bytes = [  # algorithmic bytes per launch (all members)
         M * (3 * S * 16 + 9 * NR * NTP * NZ * csz),           # read u (stencil counted once), write G
         M * (9 * NR * NTP * NZ * csz + 3 * NR * NTP * (NZ - 1) * csz),  # read G, write H
-        M * (3 * NR * NTP * (NZ - 1) * csz + 3 * S * 16),     # read H, write N
-        # predictor pass (the one timed): read u^n, N, V, write u_1 and RHSW (16 bytes per
-        # value, 3 components); the mixed form also reads u^n's FP32 mirror for the explicit
-        # stencil and writes the new FP32 mirror and its d_r (8 bytes per value)
-        M * S * (15 * 16 + (9 * 8 if prec == nsp.NSP_MIXED else 0)),
+        M * (3 * NR * NTP * (NZ - 1) * csz + 3 * S * csz),    # read H, write N (mixed: FP32)
+        # predictor pass (the one timed), bytes per point: FP64 form, read u^n, N, V, write
+        # u_1 and RHSW (5 x 3 x 16); mixed, read u^n (3 x 16), N and u^n's FP32 mirror (6 x 8),
+        # write u_1 (3 x 16), RHSW, the new FP32 mirror and its d_r (9 x 8) -- the per-set
+        # tables (factors, V, stencils) are shared by the members and L2-resident
+        M * S * (6 * 16 + 15 * 8 if prec == nsp.NSP_MIXED else 15 * 16),
         M * 64,
     ]
     dom = int(np.argmax(stage_ms[:4]))
@@ -392,29 +393,29 @@ def main():
                 "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
                 "algorithmic_bytes_per_launch": alg_bytes[dom], "launch_ms": stage_ms[dom],
                 "stage_ms": dict(zip(names, [float(x) for x in stage_ms]))}
-    # The linear pass is FP64-bound on GB300 (FP64 ~1/60 of FP32): its FP64 roofline.
-    # FP64 flops per grid point of the timed predictor pass: explicit Laplacian 84,
-    # coefficients 7, right-hand sides 20 + 12, step-invariant part 12, divergence 37,
-    # pressure solve 26, gradient and +/- 41, three Helmholtz solves 78, influence
-    # correction and r/theta 30: 347.  The mixed form sums the explicit right-hand side
-    # in FP32 but for u^n/dt (12) and stores no step-invariant part: 224.
+    # The linear pass.  FP64 form: bound by the FP64 pipe (FP64 ~1/64 of FP32 on GB300);
+    # FP64 flops per grid point of the predictor: explicit Laplacian 84, coefficients 7,
+    # right-hand sides 20 + 12, step-invariant part 12, divergence 37, pressure solve 26,
+    # gradient and +/- 41, three Helmholtz solves 78, influence correction and r/theta 30:
+    # 347; corrector 242 (right-hand side 12, divergence 37, pressure solve 26, gradient
+    # and +/- 41, Helmholtz solves 78, correction 30, convergence measure 18).  Mixed form:
+    # its stencils, solves and corrections run in FP32 and double-float, leaving 12 FP64
+    # flops per point in each pass (the split of u^n and the stored state; the increment
+    # pass's update of u) -- the pass is latency-bound, not FP64-bound.
     if names[dom] == "linear_k":
         fp64_peak = st.fp64_peak_tflops()
-        fl = (224.0 if prec == nsp.NSP_MIXED else 347.0) * S * M
+        mixed = prec == nsp.NSP_MIXED
+        fl = (12.0 if mixed else 347.0) * S * M
         ach = fl / (stage_ms[dom] * 1e-3) / 1e12
-        roofline["compute_bound"] = "fp64"
+        roofline["compute_bound"] = "latency (barrier and memory-latency stalls)" if mixed else "fp64"
         roofline["fp64"] = {"achieved_tflops": ach, "peak_tflops": fp64_peak, "frac": ach / fp64_peak,
                             "algorithmic_flops_per_launch": fl, "peak_source": "measured live (nsp_measure_fp64_peak)"}
-        # The corrector pass.  Mixed form (the increment pass): about 116 FP64 flops per
-        # point (banded solves 104, update 12; its stencils, influence correction and flux
-        # fix are FP32 on the increment).  FP64 form: 242 (right-hand side 12, divergence
-        # 37, pressure solve 26, gradient and +/- 41, Helmholtz solves 78, correction 30,
-        # convergence measure 18).  Bytes per point: FP64 form, read N, RHSW, V, u_i, write
-        # u_{i+1} (15 x 16); mixed, read N, RHSW, u_i (9 x 16) and the FP32 copies of V and
-        # u_i (6 x 8), write u_{i+1} and RHSW (6 x 16), the FP32 mirror and its d_r (6 x 8).
+        # The corrector pass, bytes per point: FP64 form, read N, RHSW, V, u_i, write u_{i+1}
+        # (15 x 16); mixed (the increment pass), read u_i (3 x 16), N, RHSW and u_i's FP32
+        # mirror (9 x 8), write u_{i+1} (3 x 16), RHSW, the FP32 mirror and its d_r (9 x 8).
         lin = st.profile_linear(5)
-        fl_c = (116.0 if prec == nsp.NSP_MIXED else 242.0) * S * M
-        by_c = M * S * ((15 * 16 + 12 * 8) if prec == nsp.NSP_MIXED else 15 * 16)
+        fl_c = (12.0 if mixed else 242.0) * S * M
+        by_c = M * S * ((6 * 16 + 18 * 8) if mixed else 15 * 16)
         roofline["corrector"] = {"launch_ms": float(lin[1]), "fp64_frac": fl_c / (lin[1] * 1e-3) / 1e12 / fp64_peak,
                                  "hbm_frac": by_c / (lin[1] * 1e-3) / 1e9 / peak,
                                  "algorithmic_flops_per_launch": fl_c, "algorithmic_bytes_per_launch": by_c}
