@@ -190,6 +190,7 @@ Tables member_view(const Group& g, int slot) {
   t.V += (size_t)ps * 3 * t.S;
   if (t.V32) t.V32 += (size_t)ps * 3 * t.S;
   if (t.facdf) t.facdf += (size_t)ps * 4 * t.NR * NFAC * t.NTNZ;
+  if (t.fac32) t.fac32 += (size_t)ps * 4 * t.NR * NFAC * t.NTNZ;
   if (t.Vdf) t.Vdf += (size_t)ps * 2 * 3 * t.S;
   t.Luc += (size_t)ps * 2 * STEN * t.NR;
   t.Luc32 += (size_t)ps * 2 * STEN * t.NR;
@@ -786,19 +787,23 @@ int nsp_setup(nsp_ctx* c) {
     tb.nsets = nsets;
     tb.V32 = nullptr;
     tb.facdf = tb.Vdf = tb.Ddf = tb.Ddivdf = tb.rinvdf = nullptr;
+    tb.fac32 = nullptr;
     if (c->precision == NSP_MIXED) {
       // the increment passes' FP32 correction profiles; the double-float factors, correction
       // profiles and stencils of the linear passes
       float2 *v32 = nullptr, *fdf = nullptr, *vdf = nullptr;
+      float* f32 = nullptr;
       if ((rc = dalloc(c, &v32, sizeof(float2) * V_n)) || (rc = dalloc(c, &fdf, sizeof(float2) * fac_n)) ||
-          (rc = dalloc(c, &vdf, sizeof(float2) * 2 * V_n)))
+          (rc = dalloc(c, &vdf, sizeof(float2) * 2 * V_n)) || (rc = dalloc(c, &f32, sizeof(float) * fac_n)))
         return rc;
       launch_to_f32(tb.V, v32, (long long)V_n, c->st);
       launch_split_df(tb.fac, fdf, (long long)fac_n, c->st);
       launch_split_df(reinterpret_cast<const double*>(tb.V), vdf, 2 * (long long)V_n, c->st);
+      launch_to_f32_real(tb.fac, f32, (long long)fac_n, c->st);
       CK(cudaGetLastError());
       tb.V32 = v32;
       tb.facdf = fdf;
+      tb.fac32 = f32;
       tb.Vdf = vdf;
       if ((rc = upload(c, &tb.Ddf, split_df_host(o.D))) || (rc = upload(c, &tb.Ddivdf, split_df_host(Ddiv))) ||
           (rc = upload(c, &tb.rinvdf, split_df_host(rinv))))

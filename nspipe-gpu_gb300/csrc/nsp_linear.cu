@@ -36,12 +36,14 @@ __device__ __forceinline__ void fms(double2& x, double l, const double2& y) { x.
 __device__ __forceinline__ void fms(double& x, double l, const double& y) { x -= l * y; }
 __device__ __forceinline__ void scale(double2& x, double u) { x.x *= u; x.y *= u; }
 __device__ __forceinline__ void scale(double& x, double u) { x *= u; }
+__device__ __forceinline__ void fms(float& x, float l, const float& y) { x = fmaf(-l, y, x); }
+__device__ __forceinline__ void scale(float& x, float u) { x *= u; }
 
 // One forward-substitution row: x -= L(i-3) x_{i-3} + L(i-2) x_{i-2} + L(i-1) x_{i-1},
 // in the reference's column order.  Factors of columns outside the band are stored
 // as 0 (and the carried x start at 0), so edge rows need no branches.
-template <typename V>
-__device__ __forceinline__ void fwd_row(V& x, const double* l, V& xm1, V& xm2, V& xm3) {
+template <typename V, typename L>
+__device__ __forceinline__ void fwd_row(V& x, const L* l, V& xm1, V& xm2, V& xm3) {
   fms(x, l[0], xm3);
   fms(x, l[1], xm2);
   fms(x, l[2], xm1);
@@ -49,8 +51,8 @@ __device__ __forceinline__ void fwd_row(V& x, const double* l, V& xm1, V& xm2, V
 }
 // One backward row, farther neighbours first so that only one multiply-add and the
 // pivot multiply wait on the row just finished: x = (x - U3 x3 - U2 x2 - U1 x1) / U_ii.
-template <typename V>
-__device__ __forceinline__ void bwd_row(V& x, const double* u, V& xp1, V& xp2, V& xp3) {
+template <typename V, typename L>
+__device__ __forceinline__ void bwd_row(V& x, const L* u, V& xp1, V& xp2, V& xp3) {
   fms(x, u[0], xp3);
   fms(x, u[1], xp2);
   fms(x, u[2], xp1);
@@ -77,6 +79,7 @@ __device__ __forceinline__ void bwd_row(dfloat& x, const dfloat* u, dfloat& xp1,
 }
 
 __device__ __forceinline__ double ldf(const double* p) { return __ldg(p); }
+__device__ __forceinline__ float ldf(const float* p) { return __ldg(p); }
 __device__ __forceinline__ dfloat ldf(const dfloat* p) {
   const float2 v = __ldg(reinterpret_cast<const float2*>(p));
   return dfloat{v.x, v.y};
@@ -146,6 +149,10 @@ __device__ __forceinline__ void cp_async8(void* dst, const void* src) {
   const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
 }
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
+}
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
@@ -165,31 +172,35 @@ inline size_t ring_extra(int NR, int LM) {
   return tile > pl + rings ? tile - pl : rings;
 }
 
-// solve_line<dfloat, dfloat> with the factor rows staged through a shared-memory ring:
+// solve_line<V, V> (V = dfloat: double-float; V = float: FP32, the increment pass's
+// Helmholtz solves) with the factor rows staged through a shared-memory ring:
 // the copies of batch b + RING_B - 1 are in flight while batch b computes, so the rows
 // wait on shared memory instead of L2.  The two threads of a line (part 0 and 1, adjacent
 // lanes, both calling) share the copies -- part 0 fetches slots 0-1, part 1 slots 2-3 --
 // and meet at __syncwarp(pair) after each wait and before a slot is refilled.  Slots:
 // forward L(i-3), L(i-2), L(i-1); backward U(i+3), U(i+2), U(i+1), 1/U_ii.  Rows past the
 // last full batch read the table directly.
-template <int LM>
-__device__ __forceinline__ void solve_line_ring(dfloat* X, int ld, const dfloat* __restrict__ f, int NTNZ, int NR,
-                                                dfloat* ring, int mm, int part, unsigned pair) {
+template <int LM, typename V>
+__device__ __forceinline__ void solve_line_ring(V* X, int ld, const V* __restrict__ f, int NTNZ, int NR,
+                                                V* ring, int mm, int part, unsigned pair) {
   const size_t rs = (size_t)NFAC * NTNZ;
   const int nb = NR / 4;
   auto issue = [&](int b, bool fwd) {
-    dfloat* dst = ring + (b % RING_B) * 16 * LM + mm;
+    V* dst = ring + (b % RING_B) * 16 * LM + mm;
 #pragma unroll
     for (int r = 0; r < 4; r++) {
       const int row = fwd ? 4 * b + r : NR - 1 - 4 * b - r;
 #pragma unroll
       for (int q = 0; q < 2; q++) {
         const int slot = 2 * part + q, e = fwd ? slot : 6 - slot;
-        if (!fwd || slot < 3) cp_async8(dst + (r * 4 + slot) * LM, f + row * rs + (size_t)e * NTNZ);
+        if (!fwd || slot < 3) {
+          if constexpr (sizeof(V) == 8) cp_async8(dst + (r * 4 + slot) * LM, f + row * rs + (size_t)e * NTNZ);
+          else cp_async4(dst + (r * 4 + slot) * LM, f + row * rs + (size_t)e * NTNZ);
+        }
       }
     }
   };
-  dfloat xm1{}, xm2{}, xm3{};
+  V xm1{}, xm2{}, xm3{};
 #pragma unroll
   for (int b = 0; b < RING_B - 1; b++) {
     if (b < nb) issue(b, true);
@@ -200,8 +211,8 @@ __device__ __forceinline__ void solve_line_ring(dfloat* X, int ld, const dfloat*
     cp_async_commit();
     cp_async_wait<RING_B - 1>();
     __syncwarp(pair);
-    const dfloat* src = ring + (b % RING_B) * 16 * LM + mm;
-    dfloat l[4][3], x[4];
+    const V* src = ring + (b % RING_B) * 16 * LM + mm;
+    V l[4][3], x[4];
 #pragma unroll
     for (int r = 0; r < 4; r++) {
 #pragma unroll
@@ -216,13 +227,13 @@ __device__ __forceinline__ void solve_line_ring(dfloat* X, int ld, const dfloat*
     __syncwarp(pair);
   }
   for (int i = 4 * nb; i < NR; i++) {
-    const dfloat* fr = f + i * rs;
-    dfloat l[3] = {ldf(fr), ldf(fr + NTNZ), ldf(fr + 2 * NTNZ)};
-    dfloat x = X[i * ld];
+    const V* fr = f + i * rs;
+    V l[3] = {ldf(fr), ldf(fr + NTNZ), ldf(fr + 2 * NTNZ)};
+    V x = X[i * ld];
     fwd_row(x, l, xm1, xm2, xm3);
     X[i * ld] = x;
   }
-  dfloat xp1{}, xp2{}, xp3{};
+  V xp1{}, xp2{}, xp3{};
 #pragma unroll
   for (int b = 0; b < RING_B - 1; b++) {
     if (b < nb) issue(b, false);
@@ -233,8 +244,8 @@ __device__ __forceinline__ void solve_line_ring(dfloat* X, int ld, const dfloat*
     cp_async_commit();
     cp_async_wait<RING_B - 1>();
     __syncwarp(pair);
-    const dfloat* src = ring + (b % RING_B) * 16 * LM + mm;
-    dfloat u[4][4], x[4];
+    const V* src = ring + (b % RING_B) * 16 * LM + mm;
+    V u[4][4], x[4];
 #pragma unroll
     for (int r = 0; r < 4; r++) {
 #pragma unroll
@@ -249,9 +260,9 @@ __device__ __forceinline__ void solve_line_ring(dfloat* X, int ld, const dfloat*
     __syncwarp(pair);
   }
   for (int i = NR - 1 - 4 * nb; i >= 0; i--) {
-    const dfloat* fr = f + i * rs;
-    dfloat u[4] = {ldf(fr + 6 * NTNZ), ldf(fr + 5 * NTNZ), ldf(fr + 4 * NTNZ), ldf(fr + 3 * NTNZ)};
-    dfloat x = X[i * ld];
+    const V* fr = f + i * rs;
+    V u[4] = {ldf(fr + 6 * NTNZ), ldf(fr + 5 * NTNZ), ldf(fr + 4 * NTNZ), ldf(fr + 3 * NTNZ)};
+    V x = X[i * ld];
     bwd_row(x, u, xp1, xp2, xp3);
     X[i * ld] = x;
   }
@@ -824,7 +835,12 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     const int tf = tid - F0;
     const int c = tf / (2 * LM), rem = tf - c * 2 * LM, mm = rem >> 1, part = rem & 1;
     if (k0 + mm < NTNZ && fac_ok(c, k0 + mm)) {
-      if constexpr (DFS)
+      if constexpr (INC)  // FP32 on the hi parts (lo stays 0): an increment of a well-conditioned operator
+        solve_line_ring<LM>(reinterpret_cast<float*>(R + c * LN + mm) + 2 * part, 4 * LM,
+                            tb.fac32 + (size_t)ps * 4 * NR * NFAC * NTNZ + (size_t)c * NR * NFAC * NTNZ + k0 + mm,
+                            NTNZ, NR, reinterpret_cast<float*>(ringF) + (size_t)c * RING_B * 16 * LM, mm, part,
+                            3u << ((tid & 31) & ~1));
+      else if constexpr (DFS)
         solve_line_ring<LM>(reinterpret_cast<dfloat*>(R + c * LN + mm) + part, 2 * LM,
                             facdf + (size_t)c * NR * NFAC * NTNZ + k0 + mm, NTNZ, NR,
                             ringF + (size_t)c * RING_B * 16 * LM, mm, part, 3u << ((tid & 31) & ~1));

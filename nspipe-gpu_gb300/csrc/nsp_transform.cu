@@ -792,4 +792,14 @@ void launch_split_df(const double* src, float2* dst, long long n, cudaStream_t s
   split_df_k<<<blocks, 256, 0, st>>>(src, dst, n);
 }
 
+__global__ void to_f32_real_k(const double* __restrict__ src, float* __restrict__ dst, long long n) {
+  for (long long h = blockIdx.x * (long long)blockDim.x + threadIdx.x; h < n; h += (long long)gridDim.x * blockDim.x)
+    dst[h] = f64_to_f32(src[h]);
+}
+
+void launch_to_f32_real(const double* src, float* dst, long long n, cudaStream_t st) {
+  int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
+  to_f32_real_k<<<blocks, 256, 0, st>>>(src, dst, n);
+}
+
 }  // namespace nsp
