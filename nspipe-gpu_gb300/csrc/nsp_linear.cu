@@ -851,37 +851,85 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   }
   __syncthreads();
 
-  // G1. wall divergence of the (half-scale) solution, in r/theta form, per mode.
+  // G1. wall divergence of the (half-scale) solution, in r/theta form, per mode: FP64;
+  // the mixed predictor in double-float, the increment passes in FP32 (their lines hold
+  // FP32 values after the solves).
   if (tid < LM) {
     int mm = tid, k = k0 + mm;
     double2 dv = c2(0, 0);
-    if (k < NTNZ) {
-      double kt = skt[mm], kz = skz[mm];
-      int tab = 1 - spar[mm];
-      const double* Dw = tb.D + tab * STEN * NR + STEN * (NR - 1) + IW;
-      double sx = 0.0, sy = 0.0;
-      double2 urw = c2(0, 0), utw = c2(0, 0);
-      for (int j = 0; j <= IW; j++) {
-        int row = NR - 1 - IW + j;
-        const double2 a = DFS ? df_value(R, row * LM + mm) : R[row * LM + mm];
-        const double2 b = DFS ? df_value(R, LN + row * LM + mm) : R[LN + row * LM + mm];
-        double2 ur = c2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y));
-        double de = __ldg(Dw + j);
-        sx += de * ur.x;
-        sy += de * ur.y;
-        if (j == IW) { urw = ur; utw = c2(0.5 * (a.y - b.y), -0.5 * (a.x - b.x)); }
+    if constexpr (INC) {
+      float sx = 0.f, sy = 0.f;
+      if (k < NTNZ) {
+        const float* Dw = tb.D32 + (1 - spar[mm]) * STEN * NR + STEN * (NR - 1) + IW;
+        float2 urw = make_float2(0.f, 0.f), utw = urw;
+        for (int j = 0; j <= IW; j++) {
+          const int row = NR - 1 - IW + j;
+          const float4 a = dfslot(R, row * LM + mm), b = dfslot(R, LN + row * LM + mm);
+          const float2 ur = make_float2(0.5f * (a.x + b.x), 0.5f * (a.z + b.z));
+          const float de = __ldg(Dw + j);
+          sx = fmaf(de, ur.x, sx);
+          sy = fmaf(de, ur.y, sy);
+          if (j == IW) { urw = ur; utw = make_float2(0.5f * (a.z - b.z), -0.5f * (a.x - b.x)); }
+        }
+        const float uzx = dfslot(R, 2 * LN + (NR - 1) * LM + mm).x, uzy = dfslot(R, 2 * LN + (NR - 1) * LM + mm).z;
+        const float kt = skt32[mm], kz = skz32[mm];
+        sx += urw.x; sy += urw.y;
+        sx += -kt * utw.y; sy += kt * utw.x;
+        sx += -kz * uzy; sy += kz * uzx;
       }
-      const double2 uzw = DFS ? df_value(R, 2 * LN + (NR - 1) * LM + mm) : R[2 * LN + (NR - 1) * LM + mm];
-      sx += urw.x; sy += urw.y;
-      sx += -kt * utw.y; sy += kt * utw.x;
-      sx += -kz * uzw.y; sy += kz * uzw.x;
-      dv = c2(-sx, -sy);
-    }
-    dvs[mm] = dv;
-    dvs32[mm] = make_float2(f64_to_f32(dv.x), f64_to_f32(dv.y));
-    if (DFS && !INC) {
-      const float2 x = split_df(dv.x), y = split_df(dv.y);
-      dvs_df[mm] = make_float4(x.x, x.y, y.x, y.y);
+      dvs32[mm] = make_float2(-sx, -sy);
+    } else if constexpr (DFS) {
+      float sx = 0.f, tx = 0.f, sy = 0.f, ty = 0.f;
+      if (k < NTNZ) {
+        const float2* Dw = tb.Ddf + (1 - spar[mm]) * STEN * NR + STEN * (NR - 1) + IW;
+        dfloat urwx{0.f, 0.f}, urwy = urwx, utwx = urwx, utwy = urwx;
+        for (int j = 0; j <= IW; j++) {
+          const int row = NR - 1 - IW + j;
+          const float4 a = dfslot(R, row * LM + mm), b = dfslot(R, LN + row * LM + mm);
+          const dfloat s0 = df_add(df_re(a), df_re(b)), s1 = df_add(df_im(a), df_im(b));
+          const dfloat urx{0.5f * s0.hi, 0.5f * s0.lo}, ury{0.5f * s1.hi, 0.5f * s1.lo};
+          const dfloat de = ld_df(Dw + j);
+          df_add_prod(sx, tx, de, urx);
+          df_add_prod(sy, ty, de, ury);
+          if (j == IW) {
+            urwx = urx; urwy = ury;
+            const dfloat d0 = df_sub(df_im(a), df_im(b)), d1 = df_sub(df_re(a), df_re(b));
+            utwx = dfloat{0.5f * d0.hi, 0.5f * d0.lo};
+            utwy = dfloat{-0.5f * d1.hi, -0.5f * d1.lo};
+          }
+        }
+        const float4 z = dfslot(R, 2 * LN + (NR - 1) * LM + mm);
+        const dfloat kt = skt_df[mm], kz = skz_df[mm];
+        const dfloat one{1.f, 0.f};
+        df_add_prod(sx, tx, one, urwx); df_add_prod(sy, ty, one, urwy);
+        df_sub_prod(sx, tx, kt, utwy); df_add_prod(sy, ty, kt, utwx);
+        df_sub_prod(sx, tx, kz, df_im(z)); df_add_prod(sy, ty, kz, df_re(z));
+      }
+      const dfloat dx = df_norm(sx, tx), dy = df_norm(sy, ty);
+      dvs_df[mm] = make_float4(-dx.hi, -dx.lo, -dy.hi, -dy.lo);
+    } else {
+      if (k < NTNZ) {
+        double kt = skt[mm], kz = skz[mm];
+        int tab = 1 - spar[mm];
+        const double* Dw = tb.D + tab * STEN * NR + STEN * (NR - 1) + IW;
+        double sx = 0.0, sy = 0.0;
+        double2 urw = c2(0, 0), utw = c2(0, 0);
+        for (int j = 0; j <= IW; j++) {
+          int row = NR - 1 - IW + j;
+          const double2 a = R[row * LM + mm], b = R[LN + row * LM + mm];
+          double2 ur = c2(0.5 * (a.x + b.x), 0.5 * (a.y + b.y));
+          double de = __ldg(Dw + j);
+          sx += de * ur.x;
+          sy += de * ur.y;
+          if (j == IW) { urw = ur; utw = c2(0.5 * (a.y - b.y), -0.5 * (a.x - b.x)); }
+        }
+        const double2 uzw = R[2 * LN + (NR - 1) * LM + mm];
+        sx += urw.x; sy += urw.y;
+        sx += -kt * utw.y; sy += kt * utw.x;
+        sx += -kz * uzw.y; sy += kz * uzw.x;
+        dv = c2(-sx, -sy);
+      }
+      dvs[mm] = dv;
     }
   }
   __syncthreads();
