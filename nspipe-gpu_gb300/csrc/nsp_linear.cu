@@ -157,8 +157,10 @@ __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commi
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
-// Depth of the factor ring of the double-float solves, in batches of four rows.
+// Depth of the factor ring of the double-float solves, in batches of four rows, and of
+// the increment pass's pressure ring, which lives in its lines' free upper halves.
 constexpr int RING_B = 3;
+constexpr int RING_DEEP = 8;
 // Shared memory of one kind's ring: [RING_B][4 rows][4 slots][LM] double-float factors.
 constexpr size_t ring_bytes(int LM) { return (size_t)RING_B * 16 * LM * sizeof(dfloat); }
 // Dynamic shared memory of a linear-pass block beyond its 4 radial lines (mixed form): the
@@ -174,19 +176,20 @@ inline size_t ring_extra(int NR, int LM) {
 
 // solve_line<V, V> (V = dfloat: double-float; V = float: FP32, the increment pass's
 // Helmholtz solves) with the factor rows staged through a shared-memory ring:
-// the copies of batch b + RING_B - 1 are in flight while batch b computes, so the rows
+// the copies of batch b + RB - 1 are in flight while batch b computes, so the rows
 // wait on shared memory instead of L2.  The two threads of a line (part 0 and 1, adjacent
 // lanes, both calling) share the copies -- part 0 fetches slots 0-1, part 1 slots 2-3 --
 // and meet at __syncwarp(pair) after each wait and before a slot is refilled.  Slots:
 // forward L(i-3), L(i-2), L(i-1); backward U(i+3), U(i+2), U(i+1), 1/U_ii.  Rows past the
-// last full batch read the table directly.
-template <int LM, typename V>
+// last full batch read the table directly.  RB: ring depth in batches; RS: element
+// stride of the ring (2: the free upper halves of line slots that hold FP32 pairs).
+template <int LM, int RB, int RS, typename V>
 __device__ __forceinline__ void solve_line_ring(V* X, int ld, const V* __restrict__ f, int NTNZ, int NR,
                                                 V* ring, int mm, int part, unsigned pair) {
   const size_t rs = (size_t)NFAC * NTNZ;
   const int nb = NR / 4;
+  auto at = [&](int b, int e) { return ring + (((b % RB) * 16 + e) * LM + mm) * RS; };
   auto issue = [&](int b, bool fwd) {
-    V* dst = ring + (b % RING_B) * 16 * LM + mm;
 #pragma unroll
     for (int r = 0; r < 4; r++) {
       const int row = fwd ? 4 * b + r : NR - 1 - 4 * b - r;
@@ -194,29 +197,28 @@ __device__ __forceinline__ void solve_line_ring(V* X, int ld, const V* __restric
       for (int q = 0; q < 2; q++) {
         const int slot = 2 * part + q, e = fwd ? slot : 6 - slot;
         if (!fwd || slot < 3) {
-          if constexpr (sizeof(V) == 8) cp_async8(dst + (r * 4 + slot) * LM, f + row * rs + (size_t)e * NTNZ);
-          else cp_async4(dst + (r * 4 + slot) * LM, f + row * rs + (size_t)e * NTNZ);
+          if constexpr (sizeof(V) == 8) cp_async8(at(b, r * 4 + slot), f + row * rs + (size_t)e * NTNZ);
+          else cp_async4(at(b, r * 4 + slot), f + row * rs + (size_t)e * NTNZ);
         }
       }
     }
   };
   V xm1{}, xm2{}, xm3{};
 #pragma unroll
-  for (int b = 0; b < RING_B - 1; b++) {
+  for (int b = 0; b < RB - 1; b++) {
     if (b < nb) issue(b, true);
     cp_async_commit();
   }
   for (int b = 0; b < nb; b++) {
-    if (b + RING_B - 1 < nb) issue(b + RING_B - 1, true);
+    if (b + RB - 1 < nb) issue(b + RB - 1, true);
     cp_async_commit();
-    cp_async_wait<RING_B - 1>();
+    cp_async_wait<RB - 1>();
     __syncwarp(pair);
-    const V* src = ring + (b % RING_B) * 16 * LM + mm;
     V l[4][3], x[4];
 #pragma unroll
     for (int r = 0; r < 4; r++) {
 #pragma unroll
-      for (int j = 0; j < 3; j++) l[r][j] = src[(r * 4 + j) * LM];
+      for (int j = 0; j < 3; j++) l[r][j] = *at(b, r * 4 + j);
       x[r] = X[(4 * b + r) * ld];
     }
 #pragma unroll
@@ -235,21 +237,20 @@ __device__ __forceinline__ void solve_line_ring(V* X, int ld, const V* __restric
   }
   V xp1{}, xp2{}, xp3{};
 #pragma unroll
-  for (int b = 0; b < RING_B - 1; b++) {
+  for (int b = 0; b < RB - 1; b++) {
     if (b < nb) issue(b, false);
     cp_async_commit();
   }
   for (int b = 0; b < nb; b++) {
-    if (b + RING_B - 1 < nb) issue(b + RING_B - 1, false);
+    if (b + RB - 1 < nb) issue(b + RB - 1, false);
     cp_async_commit();
-    cp_async_wait<RING_B - 1>();
+    cp_async_wait<RB - 1>();
     __syncwarp(pair);
-    const V* src = ring + (b % RING_B) * 16 * LM + mm;
     V u[4][4], x[4];
 #pragma unroll
     for (int r = 0; r < 4; r++) {
 #pragma unroll
-      for (int j = 0; j < 4; j++) u[r][j] = src[(r * 4 + j) * LM];
+      for (int j = 0; j < 4; j++) u[r][j] = *at(b, r * 4 + j);
       x[r] = X[(NR - 1 - 4 * b - r) * ld];
     }
 #pragma unroll
@@ -727,10 +728,18 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   if (tid < 2 * LM) {
     const int mm = tid >> 1, part = tid & 1;
     if (k0 + mm < NTNZ && fac_ok(3, k0 + mm)) {
-      if constexpr (DFS)
-        solve_line_ring<LM>(reinterpret_cast<dfloat*>(P + mm) + part, 2 * LM,
-                            facdf + 3 * (size_t)NR * NFAC * NTNZ + k0 + mm, NTNZ, NR, ringD, mm, part,
-                            3u << ((tid & 31) & ~1));
+      dfloat* X = reinterpret_cast<dfloat*>(P + mm) + part;
+      const dfloat* fp = facdf + 3 * (size_t)NR * NFAC * NTNZ + k0 + mm;
+      const unsigned pair = 3u << ((tid & 31) & ~1);
+      if constexpr (INC) {
+        // the increment pass's lines hold FP32 pairs here: a deep ring in their slots'
+        // free upper halves (3 NR LM entries, RING_DEEP x 16 LM needed)
+        if (3 * NR >= 16 * RING_DEEP)
+          solve_line_ring<LM, RING_DEEP, 2>(X, 2 * LM, fp, NTNZ, NR, reinterpret_cast<dfloat*>(R) + 1, mm, part, pair);
+        else
+          solve_line_ring<LM, RING_B, 1>(X, 2 * LM, fp, NTNZ, NR, ringD, mm, part, pair);
+      } else if constexpr (DFS)
+        solve_line_ring<LM, RING_B, 1>(X, 2 * LM, fp, NTNZ, NR, ringD, mm, part, pair);
       else
         solve_line(reinterpret_cast<double*>(P + mm) + part, 2 * LM, fac + 3 * (size_t)NR * NFAC * NTNZ + k0 + mm,
                    NTNZ, NR);
@@ -835,13 +844,14 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     const int tf = tid - F0;
     const int c = tf / (2 * LM), rem = tf - c * 2 * LM, mm = rem >> 1, part = rem & 1;
     if (k0 + mm < NTNZ && fac_ok(c, k0 + mm)) {
-      if constexpr (INC)  // FP32 on the hi parts (lo stays 0): an increment of a well-conditioned operator
-        solve_line_ring<LM>(reinterpret_cast<float*>(R + c * LN + mm) + 2 * part, 4 * LM,
+      if constexpr (INC)  // FP32 on the hi parts (lo stays 0): an increment of a well-conditioned operator;
+                          // FP32 factors, so twice the batches in a ring of the same bytes
+        solve_line_ring<LM, 2 * RING_B, 1>(reinterpret_cast<float*>(R + c * LN + mm) + 2 * part, 4 * LM,
                             tb.fac32 + (size_t)ps * 4 * NR * NFAC * NTNZ + (size_t)c * NR * NFAC * NTNZ + k0 + mm,
-                            NTNZ, NR, reinterpret_cast<float*>(ringF) + (size_t)c * RING_B * 16 * LM, mm, part,
+                            NTNZ, NR, reinterpret_cast<float*>(ringF) + (size_t)c * 2 * RING_B * 16 * LM, mm, part,
                             3u << ((tid & 31) & ~1));
       else if constexpr (DFS)
-        solve_line_ring<LM>(reinterpret_cast<dfloat*>(R + c * LN + mm) + part, 2 * LM,
+        solve_line_ring<LM, RING_B, 1>(reinterpret_cast<dfloat*>(R + c * LN + mm) + part, 2 * LM,
                             facdf + (size_t)c * NR * NFAC * NTNZ + k0 + mm, NTNZ, NR,
                             ringF + (size_t)c * RING_B * 16 * LM, mm, part, 3u << ((tid & 31) & ~1));
       else
