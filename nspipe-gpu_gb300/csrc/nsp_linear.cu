@@ -1,5 +1,6 @@
 // nsp_linear.cu -- the linear part of the predictor and corrector, one CTA per
-// block of LM (m, k_z) mode lines of one member, all in FP64.
+// block of LM (m, k_z) mode lines of one member: all FP64 in the plain FP64 form;
+// double-float, FP32 and FP64 in the mixed form (DFS and INC below).
 //
 // One launch replaces the ~28 launches of predictor()/corrector()
 // (mod_integrate.cu:164-228): decoupleForward/Backward (mod_utils.cu:30-59),
@@ -13,10 +14,12 @@
 //
 // The radial lines of the block's modes are staged in shared memory as
 // [component][r][mode]; pointwise and stencil phases use all threads over
-// (r, mode), the banded solves one thread per (component, mode) sweeping r with
-// the precomputed factors (read coalesced across modes).  The explicit
-// Laplacian of u^n is applied straight from the state in global memory (no uw
-// array, no shared-memory staging), so a block holds 4 radial lines per mode.
+// (r, mode), the banded solves two threads per (component, mode) -- the real and
+// imaginary parts -- sweeping r with the precomputed factors (read coalesced across
+// modes; in the mixed form staged through a shared-memory ring).  The explicit
+// Laplacian of u^n is applied from the state in global memory (FP64 form) or from a
+// shared-memory tile of its FP32 mirror (mixed form), so a block holds 4 radial lines
+// per mode.
 #include <cstdio>
 
 #include "nsp_bounds.cuh"
@@ -303,7 +306,8 @@ __device__ __forceinline__ double2 df_value(double2* a, int e) {
 }
 
 // At least 1024 threads per SM resident (4 radial lines of 48 points x 16 modes
-// is 49 KB of shared memory, so four 256-thread blocks fit): 64 registers.
+// is 49 KB of shared memory, 55 KB with the mixed form's factor rings, so four
+// 256-thread blocks fit): 64 registers.
 //
 // INC (mixed form, corrector passes): the pass is affine in its right-hand side, so
 // iterate i+1 is iterate i plus the linear part of the pass applied to
@@ -311,16 +315,18 @@ __device__ __forceinline__ double2 df_value(double2* a, int e) {
 //   u_{i+1} = u_i + (d_im/2) L(N_i - N_{i-1}),
 // L = divergence, pressure solve, gradient, Helmholtz solves, influence correction
 // and the flux correction without its Qdes term (equal to the full pass in exact
-// arithmetic).  The increment is small next to u, so the divergence and gradient
-// stencils run in FP32 on it; the banded solves, the influence correction and the
-// update of u stay in FP64.  N_{i-1} is kept in RHSW (the predictor stores N(u^n)
-// there in the mixed form).  Without INC the kernel is the full pass, and in the
-// mixed form it takes only the predictor.
+// arithmetic).  The increment is small next to u, so its divergence and gradient
+// stencils, influence correction, mode (0,0) constraints and flux fix run in FP32, its
+// Helmholtz solves in FP32 (well-conditioned operators), its pressure solve in
+// double-float (condition numbers up to ~1e6); only the update of u is FP64.  N_{i-1}
+// is kept in RHSW32 (the predictor stores N(u^n) there in the mixed form).  Without INC
+// the kernel is the full pass, and in the mixed form it takes only the predictor.
 //
-// DFS (mixed form, both passes): the banded solves in double-float (nsp_df.cuh) with
-// the factors split the same way, about 48 bits: the FP64 pipe's share of the pass was
-// mostly its banded solves.  In the full pass the solves' inputs are split from FP64
-// and their results summed back to FP64; the increment passes' inputs are FP32 already.
+// DFS (mixed form, both passes): FP64-class arithmetic in double-float (nsp_df.cuh),
+// about 48 bits, with the factors, stencils and correction profiles split the same way:
+// on GB300 an FP64 instruction costs 64 times an FP32 one's issue.  The predictor splits
+// u^n once, runs its stencils, solves and corrections in double-float and sums the
+// result back to FP64 when it stores the state.
 template <int LM, int NTH, bool INC, bool DFS>
 __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 : (1024 / NTH)))
     linear_k(Tables tb, Bufs bf, Ctl* ctl) {
@@ -377,7 +383,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   const double c_ex = tb.sscal[4 * ps], Qc = tb.sscal[4 * ps + 2];
   const int tid = threadIdx.x, nth = blockDim.x;
   if (tid == 0) bad = 0;
-  if (tid < LM) {  // wavenumbers once per block instead of per point (the FP64 pipe is the bound)
+  if (tid < LM) {  // wavenumbers once per block instead of per point
     int k = k0 + tid, it = k / NZ, l = k - it * NZ, m = it < NT / 2 ? it : it - NT;
     const double kt = tb.kts * (double)m, kz = tb.kzs * (double)l;
     skt[tid] = kt;
@@ -722,8 +728,7 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     return NSP_IN_BOUNDS(tb, ((size_t)c * NR + NR - 1) * NFAC * NTNZ + 6 * (size_t)NTNZ + k,
                          (size_t)4 * NR * NFAC * NTNZ, BC_LIN_FACTOR);
   };
-  // Increment passes: the solves in double-float (nsp_df.cuh) with the factors split the
-  // same way -- the FP64 pipe's share of this pass was almost all its banded solves.
+  // Mixed form: the pressure solve in double-float (nsp_df.cuh), the factors split the same way.
   const dfloat* facdf = reinterpret_cast<const dfloat*>(tb.facdf) + (size_t)ps * 4 * NR * NFAC * NTNZ;
   if (tid < 2 * LM) {
     const int mm = tid >> 1, part = tid & 1;
@@ -945,9 +950,9 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
   __syncthreads();
 
   // G2. u += (-div_wall) V (both at half scale), back to full-scale r/theta, mode (0,0) constraints.
-  // Increment passes: in FP32 on the increment (the solves' FP64 results rounded), into the
-  // FP32 halves of the slots -- the increment needs FP32's relative precision, the update of
-  // u in stage I stays FP64.
+  // Increment passes: in FP32 on the increment (the solves' results, their hi parts), into
+  // the FP32 halves of the slots -- the increment needs FP32's relative precision, the update
+  // of u in stage I stays FP64.  The mixed predictor: in double-float.
   if constexpr (INC) {
     const float2* Vp32 = tb.V32 + (size_t)ps * 3 * S;
     for (int p = tid; p < LN; p += nth) {
