@@ -157,6 +157,7 @@ __device__ __forceinline__ void cp_async4(void* dst, const void* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(d), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void prefetch_l2(const void* p) { asm volatile("prefetch.global.L2 [%0];\n" ::"l"(p)); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
 
@@ -728,6 +729,18 @@ __global__ void __launch_bounds__(NTH, NTH >= 1024 ? 1 : ((1024 / NTH) < 2 ? 2 :
     return NSP_IN_BOUNDS(tb, ((size_t)c * NR + NR - 1) * NFAC * NTNZ + 6 * (size_t)NTNZ + k,
                          (size_t)4 * NR * NFAC * NTNZ, BC_LIN_FACTOR);
   };
+  // Increment passes: the warps that wait through the solves first prefetch into L2 the
+  // rows of u_i that stage I reads (128-byte lines of 8 complex values; the first value
+  // of each line clamped into the row).
+  if constexpr (INC) {
+    if (tid >= 2 * LM) {
+      constexpr int LPR = (LM + 7) / 8;  // lines per row segment
+      for (int e = tid - 2 * LM; e < 3 * NR * LPR; e += nth - 2 * LM) {
+        const int c = e / (NR * LPR), q = e - c * NR * LPR, i = q / LPR, k = min(k0 + 8 * (q - i * LPR), NTNZ - 1);
+        prefetch_l2(Ui + (size_t)c * S + (size_t)i * NTNZ + k);
+      }
+    }
+  }
   // Mixed form: the pressure solve in double-float (nsp_df.cuh), the factors split the same way.
   const dfloat* facdf = reinterpret_cast<const dfloat*>(tb.facdf) + (size_t)ps * 4 * NR * NFAC * NTNZ;
   if (tid < 2 * LM) {
