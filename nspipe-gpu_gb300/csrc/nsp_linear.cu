@@ -277,8 +277,9 @@ __device__ __forceinline__ void solve_line_ring(V* X, int ld, const V* __restric
 
 // The low half of a line slot holds an FP32 pair in the increment passes.
 __device__ __forceinline__ float2& f32slot(double2* a, int e) { return reinterpret_cast<float2*>(a)[2 * e]; }
-// Around their banded solves the increment passes hold a line slot as two double-float
-// parts (re.hi, re.lo, im.hi, im.lo): the same 16 bytes, so the solve addresses one part
+// The mixed passes hold a line slot as two double-float parts (re.hi, re.lo, im.hi,
+// im.lo) -- the predictor from its right-hand side to its correction, the increment
+// passes around their banded solves: the same 16 bytes, so a solve addresses one part
 // where the FP64 pass addresses one double.
 __device__ __forceinline__ float4& dfslot(double2* a, int e) { return reinterpret_cast<float4*>(a)[e]; }
 __device__ __forceinline__ void put_df(double2* a, int e, float x, float y) { dfslot(a, e) = make_float4(x, 0.f, y, 0.f); }
