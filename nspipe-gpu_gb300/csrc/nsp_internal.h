@@ -83,7 +83,7 @@ struct Tables {
 __device__ __forceinline__ int member_set(const Tables& tb, int mloc) { return tb.nsets > 1 ? tb.mset[mloc] : 0; }
 #endif
 
-constexpr int LIN_VARIANTS = 11;
+constexpr int LIN_VARIANTS = 12;
 int linear_default_variant(int NR);
 bool linear_variant_fits(int v, int NR);
 void linear_shape(int v, int* LM, int* NTH);  // modes per block, threads of a variant

@@ -1383,10 +1383,11 @@ __global__ void lusolve_k(Tables tb, int kind, const double2* rhs, double2* sol)
 // Block shapes of the linear pass (modes per block, threads): the candidates of the
 // setup-time autotuner.  Shared memory per block is 4 radial lines per mode.  Wide
 // blocks (32, 64 modes) give the solve phases one or more full warps on every SM
-// sub-partition; narrow ones more blocks per SM.
+// sub-partition; narrow ones more blocks per SM; 16 x 512 keeps 16-mode blocks at
+// 1024 threads per SM where NR is large enough that two of them fill its shared memory.
 #define NSP_LIN_SHAPES(X) \
   X(0, 16, 256) X(1, 8, 128) X(2, 8, 256) X(3, 4, 128) X(4, 12, 192) X(5, 12, 256) X(6, 24, 384) X(7, 32, 512) \
-  X(8, 32, 256) X(9, 64, 512) X(10, 64, 1024)
+  X(8, 32, 256) X(9, 64, 512) X(10, 64, 1024) X(11, 16, 512)
 struct LinShape { int LM, NTH; };
 static const LinShape kLinShapes[LIN_VARIANTS] = {
 #define NSP_LIN_ENTRY(v, lm, nth) {lm, nth},
