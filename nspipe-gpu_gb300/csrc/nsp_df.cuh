@@ -23,10 +23,14 @@ struct __align__(8) dfloat {
 
 __device__ __forceinline__ dfloat df_make(float x) { return dfloat{x, 0.f}; }
 
-// (s, t) := two-sum(s, t) renormalised: s + t exactly, hi = fl(s + t).
+// (s, t) renormalised to hi = fl(s + t), lo = the rest, by Dekker's fast two-sum: exact
+// when |s| >= |t|.  Here t only ever holds the accumulated rounding terms of the values
+// summed into s (a few ulps of the largest of them), so where cancellation leaves
+// |s| < |t| the result's error is an ulp of t, about 2^-48 of those values -- the
+// form's own accuracy -- for half the operations of the full two-sum.
 __device__ __forceinline__ dfloat df_norm(float s, float t) {
-  const float h = __fadd_rn(s, t), v = __fsub_rn(h, s);
-  return dfloat{h, __fadd_rn(__fsub_rn(s, __fsub_rn(h, v)), __fsub_rn(t, v))};
+  const float h = __fadd_rn(s, t);
+  return dfloat{h, __fsub_rn(t, __fsub_rn(h, s))};
 }
 
 // s + t -= a b: the high product leaves s exactly by two-sum, its rounding error and
