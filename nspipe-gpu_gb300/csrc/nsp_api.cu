@@ -797,9 +797,8 @@ int nsp_setup(nsp_ctx* c) {
           (rc = dalloc(c, &vdf, sizeof(float2) * 2 * V_n)) || (rc = dalloc(c, &f32, sizeof(float) * fac_n)))
         return rc;
       launch_to_f32(tb.V, v32, (long long)V_n, c->st);
-      launch_split_df(tb.fac, fdf, (long long)fac_n, c->st);
+      launch_split_fac(tb.fac, fdf, f32, (long long)fac_n, (int)NTNZ, c->st);
       launch_split_df(reinterpret_cast<const double*>(tb.V), vdf, 2 * (long long)V_n, c->st);
-      launch_to_f32_real(tb.fac, f32, (long long)fac_n, c->st);
       CK(cudaGetLastError());
       tb.V32 = v32;
       tb.facdf = fdf;

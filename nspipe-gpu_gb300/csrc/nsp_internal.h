@@ -53,8 +53,8 @@ struct Tables {
   const double* fac;   // [4][NR][7][NTNZ]: banded LU factors of u+, u-, u_z, p
   const double2* V;    // [3][NR][NTNZ]: influence-matrix correction profiles (+, -, z)
   const float2* V32;   // mixed form: the same in FP32 (the corrector increments' correction)
-  const float2* facdf;  // mixed form: fac as double-float pairs (hi, lo) (the linear passes' solves)
-  const float* fac32;   // mixed form: fac in FP32 (the increment passes' Helmholtz solves)
+  const float2* facdf;  // mixed form: fac as double-float pairs (hi, lo), backward entries divided by U_ii
+  const float* fac32;   // mixed form: the same in FP32 (the increment passes' Helmholtz solves)
   const float2* Vdf;    // mixed form: V as double-float pairs, real and imaginary part of each entry
   const float2* Ddf;    // mixed form: D, Ddiv and 1/r as double-float pairs (the predictor's stencils)
   const float2* Ddivdf;
@@ -168,7 +168,7 @@ cudaError_t noalloc_scratch(int device, void** ptr);
 // FP32 copy of nmem x 3 x S complex values (the mixed form's transform input).
 void launch_to_f32(const double2* src, float2* dst, long long n, cudaStream_t st);
 void launch_split_df(const double* src, float2* dst, long long n, cudaStream_t st);
-void launch_to_f32_real(const double* src, float* dst, long long n, cudaStream_t st);
+void launch_split_fac(const double* fac, float2* dfo, float* f32o, long long n, int NTNZ, cudaStream_t st);
 // The FP32 mirror and its radial derivative (DR32) of a group's state U (mixed form).
 void launch_mirror(const Tables& tb, const double2* U, float2* U32, float2* DR32, cudaStream_t st);
 int kernels_per_nonlinear();

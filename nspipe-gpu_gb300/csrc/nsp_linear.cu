@@ -72,12 +72,23 @@ __device__ __forceinline__ void fwd_row(dfloat& x, const dfloat* l, dfloat& xm1,
   x = df_norm(s, t);
   xm3 = xm2; xm2 = xm1; xm1 = x;
 }
+// The mixed form's factor tables hold U'(i, i+j) = U(i, i+j) / U_ii (split_fac_k), so a
+// backward row is x = y / U_ii - U'3 x3 - U'2 x2 - U'1 x1: the division of y, which is
+// known early, stays off the dependency chain.
 __device__ __forceinline__ void bwd_row(dfloat& x, const dfloat* u, dfloat& xp1, dfloat& xp2, dfloat& xp3) {
-  float s = x.hi, t = x.lo;
+  const dfloat y = df_mul(x, u[3]);
+  float s = y.hi, t = y.lo;
   df_sub_prod(s, t, u[0], xp3);
   df_sub_prod(s, t, u[1], xp2);
   df_sub_prod(s, t, u[2], xp1);
-  x = df_mul(df_norm(s, t), u[3]);
+  x = df_norm(s, t);
+  xp3 = xp2; xp2 = xp1; xp1 = x;
+}
+__device__ __forceinline__ void bwd_row(float& x, const float* u, float& xp1, float& xp2, float& xp3) {
+  x *= u[3];
+  x = fmaf(-u[0], xp3, x);
+  x = fmaf(-u[1], xp2, x);
+  x = fmaf(-u[2], xp1, x);
   xp3 = xp2; xp2 = xp1; xp1 = x;
 }
 

@@ -792,14 +792,25 @@ void launch_split_df(const double* src, float2* dst, long long n, cudaStream_t s
   split_df_k<<<blocks, 256, 0, st>>>(src, dst, n);
 }
 
-__global__ void to_f32_real_k(const double* __restrict__ src, float* __restrict__ dst, long long n) {
-  for (long long h = blockIdx.x * (long long)blockDim.x + threadIdx.x; h < n; h += (long long)gridDim.x * blockDim.x)
-    dst[h] = f64_to_f32(src[h]);
+// The banded-LU factor tables [kk][NR][NFAC][NTNZ] in double-float and FP32 for the
+// mixed form's solves, with the backward entries U(i, i+j) (entries 4..6) pre-divided by
+// U_ii (times entry 3, 1/U_ii): a backward row is then x_i = y_i / U_ii - sum U'_ij x_j,
+// the division applied to y_i off the row-to-row dependency chain.
+__global__ void split_fac_k(const double* __restrict__ fac, float2* __restrict__ dfo, float* __restrict__ f32o,
+                            long long n, int NTNZ) {
+  for (long long h = blockIdx.x * (long long)blockDim.x + threadIdx.x; h < n; h += (long long)gridDim.x * blockDim.x) {
+    const long long k = h % NTNZ, re = h / NTNZ, e = re % NFAC;
+    double x = fac[h];
+    if (e >= 4) x *= fac[(re - e + 3) * NTNZ + k];
+    const float hi = f64_to_f32(x);
+    dfo[h] = make_float2(hi, f64_to_f32(x - f32_to_f64(hi)));
+    f32o[h] = hi;
+  }
 }
 
-void launch_to_f32_real(const double* src, float* dst, long long n, cudaStream_t st) {
+void launch_split_fac(const double* fac, float2* dfo, float* f32o, long long n, int NTNZ, cudaStream_t st) {
   int blocks = (int)std::min<long long>((n + 255) / 256, 152LL * 16);
-  to_f32_real_k<<<blocks, 256, 0, st>>>(src, dst, n);
+  split_fac_k<<<blocks, 256, 0, st>>>(fac, dfo, f32o, n, NTNZ);
 }
 
 }  // namespace nsp
