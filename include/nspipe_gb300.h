@@ -44,7 +44,8 @@ extern "C" {
                                 taken as the reference takes them                   */
 
 #define NSP_FP64 0  /* plain form: every operation in FP64 (matches the reference)         */
-#define NSP_MIXED 1 /* transforms + nonlinear product in FP32; solves, BCs, state in FP64 */
+#define NSP_MIXED 1 /* transforms + nonlinear product in FP32 (theta DFT 3xTF32); solves and corrections
+                             in double-float (FP32 pairs) or FP32 on corrector increments; state in FP64 */
 
 /* Run-time copy of the reference's compile-time parameters (head.h:16-61). */
 typedef struct nsp_params {
@@ -167,7 +168,8 @@ int nsp_nonlinear_static(nsp_ctx* ctx, int member, const void* u3, void* n3);
  * mod_linear.cu:664-679): kind 0 = u+, 1 = u-, 2 = u_z, 3 = pressure.  rhs and sol
  * are device arrays of NR*NT*NZ complex doubles (rhs is not modified).  Kinds 4..7:
  * the solve of kind - 4 in double-float (FP32 pairs, about 48 bits), the form the
- * mixed form's corrector passes use; mixed-form contexts only (NSP_ERR_ARG otherwise). */
+ * mixed form's predictor (all kinds) and corrector passes (kind 3) use; mixed-form
+ * contexts only (NSP_ERR_ARG otherwise). */
 int nsp_lusolve(nsp_ctx* ctx, int member, int kind, const void* rhs, void* sol);
 
 /* Diagnostics of one member (synchronises the context's stream). */
