@@ -1584,6 +1584,12 @@ int nsp_describe(nsp_ctx* c, char* buf, int cap) {
   s += c->precision == NSP_MIXED ? "mixed" : "fp64";
   s += "\", \"graph\": ";
   s += c->use_graph ? "true" : "false";
+  // the arithmetic of the linear passes (the transforms' is each group's "theta"/"z_stage")
+  s += c->precision == NSP_MIXED
+           ? ", \"linear\": {\"predictor\": \"double-float (FP32 pairs) stencils, solves and corrections; FP64 state\", "
+             "\"corrector\": \"increment pass: FP32 stencils, corrections and Helmholtz solves, double-float "
+             "pressure solve, FP64 update\"}"
+           : ", \"linear\": {\"predictor\": \"fp64\", \"corrector\": \"fp64\"}";
   s += ", \"groups\": [";
   for (size_t k = 0; k < c->groups.size(); k++) {
     const Tables& tb = c->groups[k].tb;

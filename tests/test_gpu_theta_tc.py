@@ -19,9 +19,12 @@ def test_theta_path_selection(nsp, monkeypatch):
     d = st.describe()
     assert d["precision"] == "mixed"
     assert d["groups"][0]["theta"] == "tcgen05-3xtf32"
+    assert "double-float" in d["linear"]["predictor"] and "FP32" in d["linear"]["corrector"]
     st.close()
     st = stepper(nsp, "c0", nsp.NSP_FP64)
-    assert st.describe()["groups"][0]["theta"] == "fft-fp64"
+    d = st.describe()
+    assert d["groups"][0]["theta"] == "fft-fp64"
+    assert d["linear"] == {"predictor": "fp64", "corrector": "fp64"}
     st.close()
     # lengths without a compiled tile shape keep the FFT kernels
     st = stepper(nsp, "s2", nsp.NSP_MIXED)
